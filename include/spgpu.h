@@ -1,0 +1,203 @@
+/*
+ * spgpu.h — C ABI of the GB300 SpatialPy simulation engine (libspgpu.so).
+ *
+ * The reference engine has no in-process ABI: spatialpy.Solver generates a C++
+ * model file, builds `ssa_sdpd.exe` with SCons and runs one process per
+ * trajectory (spatialpy/solvers/solver.py:443-507 compile, :510-607 run), which
+ * writes `outputN.vtk` files (src/output.cpp:104-229).  This header replaces
+ * that process + file boundary with plain C calls over caller-owned arrays:
+ *
+ *   sp_create    replaces Solver.compile() + the generated model file
+ *                (solver.py:100-158 __create_propensity_file, :208-288
+ *                __get_input_constants, :375-419 __get_system_config) and the
+ *                engine set-up in propensity_file_template.cpp:101-142
+ *                (init_all_particles, initialize_rdme).
+ *   sp_run       replaces the per-trajectory subprocess loop of Solver.run
+ *                (solver.py:547-605) and the engine main loop run_simulation
+ *                (src/simulate_threads.cpp:171-312), including the NSM event
+ *                loop (src/simulate_rdme.cpp:211-472) and the SDPD particle
+ *                step (src/simulate.cpp:56-173, src/model.cpp:39-329).
+ *   sp_status    replaces the engine's exit codes / printf diagnostics on
+ *                negative counts and NaN state (simulate_rdme.cpp:288-294,
+ *                395-400; particle.cpp:88-126): errors are reported per
+ *                trajectory instead of exit(1).
+ *   sp_last_error  replaces the stdout text Solver.run streams back
+ *                (solver.py:32-43) when it raises SimulationError.
+ *   sp_destroy   replaces Solver.__del__ removing build_dir (solver.py:90-98).
+ *
+ * All arrays are caller-owned.  Every entry point returns SP_OK (0) or a
+ * negative SP_E* code; sp_last_error() then describes the failure.  No
+ * callbacks are made into the caller.  A handle is used by one host thread at a
+ * time; separate handles are independent.
+ */
+#ifndef SPGPU_H
+#define SPGPU_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SP_ABI_VERSION 1
+
+/* ---- return codes ------------------------------------------------------ */
+#define SP_OK              0
+#define SP_E_INVALID     (-1)   /* bad argument (sizes, NULL, out-of-range index) */
+#define SP_E_CUDA        (-2)   /* a CUDA runtime call failed */
+#define SP_E_NOMEM       (-3)   /* device allocation failed */
+#define SP_E_UNSUPPORTED (-4)   /* model feature outside this engine (e.g. custom propensity) */
+#define SP_E_TRAJECTORY  (-5)   /* at least one trajectory ended with an error status */
+#define SP_E_TIMEOUT     (-6)   /* the caller's wall-clock limit ran out */
+
+/* ---- per-trajectory status words (sp_traj_status.code) ----------------- */
+#define SP_TRAJ_OK               0
+#define SP_TRAJ_NEG_COUNT        1  /* a count went negative (simulate_rdme.cpp:288-294, 395-400) */
+#define SP_TRAJ_NAN_STATE        2  /* NaN/inf in particle state (particle.cpp:88-126) */
+#define SP_TRAJ_SELECT_OVERFLOW  3  /* no channel could be selected (simulate_rdme.cpp:277-279, 381-389) */
+#define SP_TRAJ_BUDGET_EXHAUSTED 4  /* event budget / deadline of one launch ran out; resumable */
+
+/* ---- mass-action reaction kinds ----------------------------------------
+ * Propensity forms generated by Reaction._create_mass_action
+ * (spatialpy/core/reaction.py:260-313) and evaluated in the generated C++
+ * with left-to-right operator order:                                       */
+#define SP_RXN_ZERO   0   /* k * vol                       (0th order)     */
+#define SP_RXN_FIRST  1   /* k * x[a]                      (1st order)     */
+#define SP_RXN_SECOND 2   /* k * x[a] * x[b] / vol         (a != b)        */
+#define SP_RXN_DIMER  3   /* k * x[a] * (x[a] - 1) / vol   (2a -> ...)     */
+
+/* ---- NSM selection rule -------------------------------------------------- */
+#define SP_SELECT_EXACT     0  /* uniform rescaled for the channel choice; the
+                                  event past a step boundary is not executed */
+#define SP_SELECT_REFERENCE 1  /* reproduces simulate_rdme.cpp: rand1 reused
+                                  unscaled (:253-261, :317-321) and one event
+                                  past each step boundary executed (:233-238) */
+
+/* ---- SDPD arithmetic ------------------------------------------------------ */
+#define SP_PREC_F32 0
+#define SP_PREC_F64 1
+
+/*
+ * One model instance: the arrays Model.compile_prep() + Solver.compile()
+ * bake into the generated C++ (solver.py:208-288, 312-331, 375-419).
+ * Layout follows ParticleSystem/Particle (include/particle_system.hpp:44-107,
+ * include/particle.hpp:43-100), as structure-of-arrays.
+ */
+typedef struct sp_scenario {
+    int32_t dimension;            /* 1, 2 or 3 (ParticleSystem::dimension) */
+    int32_t num_particles;        /* N: particles == voxels */
+    const double*  x;             /* [N*3] positions */
+    const double*  v;             /* [N*3] initial velocities; NULL = zero */
+    const int32_t* type;          /* [N] type id in 1..num_types */
+    const double*  mass;          /* [N] */
+    const double*  rho;           /* [N] */
+    const double*  nu;            /* [N] */
+    const uint8_t* fixed;         /* [N] solidTag (1 = fixed/wall particle) */
+    int32_t num_types;            /* T: type ids 1..T (type 0 = unassigned, rejected) */
+
+    int32_t num_species;          /* S */
+    int32_t num_reactions;        /* R */
+    const double*  rxn_rate;      /* [R] mass-action rate constant k */
+    const int32_t* rxn_kind;      /* [R] SP_RXN_* */
+    const int32_t* rxn_reactants; /* [R*2] species a, b (-1 when unused) */
+    const uint8_t* rxn_allowed;   /* [R*(T+1)] 1 if reaction fires in type t (restrict_to); NULL = all */
+    const int64_t* jcN;           /* [R+1] stoichiometry CSC column pointers (model.py:252-268) */
+    const int64_t* irN;           /* [jcN[R]] species index of each change */
+    const int32_t* prN;           /* [jcN[R]] change in copy number */
+    const double*  diffusion;     /* [S*T] D(s,t) = diffusion[s*T + t-1] (solver.py:269-286) */
+
+    double h;                     /* SPH support radius (Domain.find_h, domain.py:751-769) */
+    double rho0, c0, P0;          /* reference density, sound speed, background pressure */
+    double gravity[3];
+    double dt;                    /* TimeSpan.timestep_size */
+    int32_t num_steps;            /* nt (TimeSpan.num_timesteps) */
+    int32_t static_domain;        /* Model.staticDomain */
+    int32_t num_outputs;          /* len(TimeSpan.output_steps) */
+    const int32_t* output_steps;  /* [num_outputs] ascending step indices */
+} sp_scenario;
+
+typedef struct sp_options {
+    int32_t device;               /* CUDA device ordinal */
+    int32_t sdpd_precision;       /* SP_PREC_F32 (default) or SP_PREC_F64 */
+    int32_t nsm_variant;          /* 0 = autotuned, 1 = sequential warp, 2 = speculative batch warp */
+    int32_t reserved;
+    int64_t event_budget;         /* max events per trajectory per launch (0 = default) */
+} sp_options;
+
+/*
+ * One ensemble run (Solver.run(number_of_trajectories, seed), solver.py:510).
+ * Trajectory j runs instance `instance[j]` (NULL = instance 0) with Philox key
+ * `seeds[j]` (the reference uses seed+j, solver.py:558-559).
+ */
+typedef struct sp_run_args {
+    int32_t num_trajectories;
+    int32_t selection;            /* SP_SELECT_* */
+    const int32_t*  instance;     /* [ntraj] or NULL */
+    const uint64_t* seeds;        /* [ntraj] */
+    const uint32_t* const* u0;    /* [num_instances] -> [N_i*S_i] initial counts, voxel-major */
+    int32_t buffers_on_device;    /* 1: every pointer in sp_outputs/u0 is device memory */
+    int32_t want_counts;          /* write per-output counts */
+    int32_t want_moments;         /* write per-instance moment sums over trajectories */
+    int32_t want_particles;       /* write per-output particle state (non-static) */
+    double  timeout_s;            /* 0 = none; else SP_E_TIMEOUT once exceeded */
+} sp_run_args;
+
+typedef struct sp_outputs {
+    /* [sum_j num_outputs_j * N_j * S_j] int32, trajectory-major then output, voxel, species */
+    int32_t* counts;
+    /* [sum_i num_outputs_i * N_i * S_i * 2] int64: (sum x, sum x^2) over the
+       trajectories of instance i */
+    int64_t* moments;
+    /* [sum_i num_outputs_i * N_i * 3] positions / velocities, [.. * N_i] rho */
+    double* particle_x;
+    double* particle_v;
+    double* particle_rho;
+    /* [ntraj*2] (reaction events, diffusion events) — the engine counters
+       total_reactions / total_diffusion (simulate_rdme.cpp:310, 445) */
+    int64_t* event_counts;
+} sp_outputs;
+
+typedef struct sp_traj_status {
+    int32_t code;                 /* SP_TRAJ_* */
+    int32_t voxel;                /* voxel of the failing event, -1 if none */
+    double  time;                 /* simulation time reached */
+    int64_t events;               /* events executed */
+} sp_traj_status;
+
+typedef struct sp_handle sp_handle;
+
+int         sp_abi_version(void);
+int         sp_create(const sp_scenario* scenarios, int32_t num_scenarios,
+                      const sp_options* opts, sp_handle** out);
+int         sp_run(sp_handle* h, const sp_run_args* args, sp_outputs* out);
+int         sp_status(sp_handle* h, int32_t trajectory, sp_traj_status* st);
+const char* sp_last_error(sp_handle* h);
+void        sp_destroy(sp_handle* h);
+
+/*
+ * Inspection entry points (test and tooling use).  They copy device state of
+ * instance `inst` into caller buffers.
+ *
+ * sp_get_neighbors mirrors Particle::neighbors after find_neighbors
+ * (particle.cpp:150-210, 240-294): for particle i, count[i] entries at
+ * idx/dist/dWdr/Dij[i*kmax ...] in ascending distance order (ties by index).
+ * Returns SP_E_INVALID if any particle has more than kmax neighbours.
+ */
+int sp_get_neighbors(sp_handle* h, int32_t inst, int32_t kmax, int32_t* count,
+                     int32_t* idx, double* dist, double* dWdr, double* Dij);
+/* Ddiag[i*S+s] (nsm_core__initialize_diff_propensities, simulate_rdme.cpp:131-152) */
+int sp_get_ddiag(sp_handle* h, int32_t inst, double* ddiag);
+/* Current particle state of instance inst: x[N*3], v[N*3], rho[N]. */
+int sp_get_particles(sp_handle* h, int32_t inst, double* x, double* v, double* rho);
+/* Advance the SDPD flow of instance inst by nsteps without species
+   (take_step substeps 0-2, simulate.cpp:33-48), from its current state. */
+int sp_sdpd_advance(sp_handle* h, int32_t inst, int32_t nsteps);
+/* Device time in milliseconds of the last sp_run / sp_sdpd_advance
+   (CUDA events on the handle's stream) and kernel launches issued by it. */
+int sp_last_timing(sp_handle* h, double* ms, int64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPGPU_H */

@@ -1,0 +1,241 @@
+"""TEST INFRASTRUCTURE: ctypes front end of the CPU oracle.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` import this package.  It wraps
+
+* ``oracle/build/libsporacle.so`` — the project's C restatement of the
+  SpatialPy hot path (``sp_oracle.c``, ``sdpd_oracle.c``), and
+* ``oracle/_ref/libspref*.so`` — the unmodified reference engine linked with
+  ``ref_driver.cpp`` (built by ``build_ref.sh`` where the reference sources
+  are available).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from spatialpy_gb300.abi import SpScenario, scenario_struct
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "build", "libsporacle.so")
+REF_DIR = os.path.join(HERE, "_ref")
+
+_p = C.POINTER
+_lib = None
+
+
+def build(quiet: bool = True) -> str:
+    """Compile the C restatement (make in oracle/)."""
+    out = subprocess.run(["make", "-C", HERE], capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
+    return LIB
+
+
+def build_reference() -> bool:
+    """Build oracle/_ref from the reference sources; False when they are absent."""
+    script = os.path.join(HERE, "build_ref.sh")
+    out = subprocess.run(["bash", script], capture_output=True, text=True)
+    return out.returncode == 0
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = C.CDLL(LIB)
+        L.spo_philox4x32_10.argtypes = [_p(C.c_uint32), _p(C.c_uint32), _p(C.c_uint32)]
+        L.spo_neglog.argtypes = [C.c_double]
+        L.spo_neglog.restype = C.c_double
+        L.spo_neighbors.argtypes = [C.c_int32, C.c_int32, _p(C.c_double), _p(C.c_double),
+                                    C.c_double, _p(C.c_double), _p(C.c_double), C.c_int32,
+                                    _p(C.c_int32), _p(C.c_int32), _p(C.c_double),
+                                    _p(C.c_double), _p(C.c_double)]
+        L.spo_diffusion_tables.argtypes = [_p(SpScenario), C.c_int32, _p(C.c_int32),
+                                           _p(C.c_int32), _p(C.c_double), _p(C.c_double),
+                                           _p(C.c_double)]
+        L.spo_nsm_trajectory.argtypes = [_p(SpScenario), _p(C.c_uint32), C.c_uint64, C.c_int32,
+                                         _p(C.c_int32), _p(C.c_int64)]
+        L.spo_nsm_ensemble.argtypes = [_p(SpScenario), _p(C.c_uint32), _p(C.c_uint64),
+                                       C.c_int32, C.c_int32, C.c_int32, _p(C.c_int32),
+                                       _p(C.c_int64), _p(C.c_int32)]
+        for fn in (L.spo_sdpd_f64, L.spo_sdpd_f32):
+            fn.argtypes = [_p(SpScenario), C.c_int32, C.c_int32, C.c_int32, C.c_int32] + \
+                [_p(C.c_double)] * 7 + [_p(C.c_int32)]
+        _lib = L
+    return _lib
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(_p(t)) if a is not None else C.cast(None, _p(t))
+
+
+def philox(ctr, key) -> np.ndarray:
+    c = np.ascontiguousarray(ctr, np.uint32)
+    k = np.ascontiguousarray(key, np.uint32)
+    o = np.zeros(4, np.uint32)
+    lib().spo_philox4x32_10(_ptr(c, C.c_uint32), _ptr(k, C.c_uint32), _ptr(o, C.c_uint32))
+    return o
+
+
+def neglog(u: float) -> float:
+    return lib().spo_neglog(float(u))
+
+
+def neighbors(sc, kmax: int = 64, xq=None, xt=None):
+    """(count, idx, dist, dWdr, Dij) with the reference predicate and order."""
+    n = sc.num_particles
+    xq = np.ascontiguousarray(sc.x if xq is None else xq, np.float64)
+    xt = np.ascontiguousarray(sc.x if xt is None else xt, np.float64)
+    cnt = np.zeros(n, np.int32)
+    idx = np.full((n, kmax), -1, np.int32)
+    dist = np.zeros((n, kmax))
+    dw = np.zeros((n, kmax))
+    dij = np.zeros((n, kmax))
+    rc = lib().spo_neighbors(n, sc.dimension, _ptr(xq, C.c_double), _ptr(xt, C.c_double), sc.h,
+                             _ptr(sc.mass, C.c_double), _ptr(sc.rho, C.c_double), kmax,
+                             _ptr(cnt, C.c_int32), _ptr(idx, C.c_int32), _ptr(dist, C.c_double),
+                             _ptr(dw, C.c_double), _ptr(dij, C.c_double))
+    if rc != 0:
+        raise ValueError("neighbour list overflow; raise kmax")
+    return cnt, idx, dist, dw, dij
+
+
+def diffusion_tables(sc, cnt, idx, dij):
+    kmax = idx.shape[1]
+    s = scenario_struct(sc)
+    dd = np.zeros((sc.num_particles, sc.num_species))
+    cdf = np.zeros((sc.num_particles, sc.num_species, kmax))
+    lib().spo_diffusion_tables(C.byref(s), kmax, _ptr(cnt, C.c_int32), _ptr(idx, C.c_int32),
+                               _ptr(np.ascontiguousarray(dij), C.c_double), _ptr(dd, C.c_double),
+                               _ptr(cdf, C.c_double))
+    return dd, cdf
+
+
+def nsm_trajectory(sc, seed: int, selection: int = 0, u0=None):
+    u0 = np.ascontiguousarray(sc.u0 if u0 is None else u0, np.uint32)
+    s = scenario_struct(sc)
+    out = np.zeros((len(sc.output_steps), sc.num_particles, sc.num_species), np.int32)
+    ev = np.zeros(2, np.int64)
+    st = lib().spo_nsm_trajectory(C.byref(s), _ptr(u0, C.c_uint32), seed, selection,
+                                  _ptr(out, C.c_int32), _ptr(ev, C.c_int64))
+    return out, ev, st
+
+
+def nsm_ensemble(sc, seeds, selection: int = 0, threads: int = 0, want_counts: bool = True,
+                 u0=None):
+    """Returns (counts [ntraj,T,N,S] or None, events [ntraj,2], status [ntraj], threads)."""
+    u0 = np.ascontiguousarray(sc.u0 if u0 is None else u0, np.uint32)
+    seeds = np.ascontiguousarray(seeds, np.uint64)
+    nt = len(seeds)
+    s = scenario_struct(sc)
+    out = (np.zeros((nt, len(sc.output_steps), sc.num_particles, sc.num_species), np.int32)
+           if want_counts else None)
+    ev = np.zeros((nt, 2), np.int64)
+    st = np.zeros(nt, np.int32)
+    used = lib().spo_nsm_ensemble(C.byref(s), _ptr(u0, C.c_uint32), _ptr(seeds, C.c_uint64), nt,
+                                  selection, threads, _ptr(out, C.c_int32), _ptr(ev, C.c_int64),
+                                  _ptr(st, C.c_int32))
+    return out, ev, st, used
+
+
+class SdpdState:
+    def __init__(self, sc):
+        n = sc.num_particles
+        self.x = sc.x.copy()
+        self.v = np.zeros((n, 3)) if sc.v is None else sc.v.copy()
+        self.vt = np.zeros((n, 3))
+        self.rho = sc.rho.copy()
+        self.F = np.zeros((n, 3))
+        self.Fbp = np.zeros((n, 3))
+        self.Frho = np.zeros(n)
+        self.step = 0
+        self.nbr_count = np.zeros(n, np.int32)
+
+
+def sdpd(sc, state: SdpdState, nsteps: int, precision: str = "f64", mode: int = 2,
+         kmax: int = 64) -> SdpdState:
+    """Advance the SDPD oracle in place.  mode bit 1 = Gauss-Seidel BVF reads,
+    bit 2 = start-of-step neighbour points (both reference behaviours)."""
+    s = scenario_struct(sc)
+    fn = lib().spo_sdpd_f64 if precision == "f64" else lib().spo_sdpd_f32
+    rc = fn(C.byref(s), state.step, nsteps, mode, kmax, _ptr(state.x, C.c_double),
+            _ptr(state.v, C.c_double), _ptr(state.vt, C.c_double), _ptr(state.rho, C.c_double),
+            _ptr(state.F, C.c_double), _ptr(state.Fbp, C.c_double), _ptr(state.Frho, C.c_double),
+            _ptr(state.nbr_count, C.c_int32))
+    if rc != 0:
+        raise RuntimeError(f"SDPD oracle failed (rc={rc})")
+    state.step += nsteps
+    return state
+
+
+# ---------------------------------------------------------------------------
+# the compiled reference engine (oracle/_ref)
+# ---------------------------------------------------------------------------
+_ref = {}
+
+
+def reference_available(variant: str = "") -> bool:
+    return os.path.exists(os.path.join(REF_DIR, f"libspref{variant}.so"))
+
+
+def ref_lib(variant: str = ""):
+    """variant: '' (stock -O2), '_exact' (rescaled selection), '_O0' (as shipped)."""
+    if variant not in _ref:
+        path = os.path.join(REF_DIR, f"libspref{variant}.so")
+        if not os.path.exists(path):
+            raise OSError(f"{path} missing: run oracle/build_ref.sh where the reference exists")
+        L = C.CDLL(path)
+        L.spref_neighbors.argtypes = [_p(SpScenario), C.c_int32, _p(C.c_int32), _p(C.c_int32),
+                                      _p(C.c_double), _p(C.c_double), _p(C.c_double)]
+        L.spref_nsm.argtypes = [_p(SpScenario), _p(C.c_uint32), C.c_uint64, _p(C.c_int32),
+                                _p(C.c_int64)]
+        L.spref_sdpd.argtypes = [_p(SpScenario), C.c_int32, _p(C.c_double), _p(C.c_double),
+                                 _p(C.c_double)]
+        _ref[variant] = L
+    return _ref[variant]
+
+
+def ref_neighbors(sc, kmax: int = 64):
+    n = sc.num_particles
+    s = scenario_struct(sc)
+    cnt = np.zeros(n, np.int32)
+    idx = np.full((n, kmax), -1, np.int32)
+    dist = np.zeros((n, kmax))
+    dw = np.zeros((n, kmax))
+    dij = np.zeros((n, kmax))
+    rc = ref_lib().spref_neighbors(C.byref(s), kmax, _ptr(cnt, C.c_int32), _ptr(idx, C.c_int32),
+                                   _ptr(dist, C.c_double), _ptr(dw, C.c_double),
+                                   _ptr(dij, C.c_double))
+    if rc != 0:
+        raise ValueError(f"reference neighbour search failed ({rc})")
+    return cnt, idx, dist, dw, dij
+
+
+def ref_nsm(sc, seed: int, variant: str = "", u0=None):
+    u0 = np.ascontiguousarray(sc.u0 if u0 is None else u0, np.uint32)
+    s = scenario_struct(sc)
+    out = np.zeros((len(sc.output_steps), sc.num_particles, sc.num_species), np.int32)
+    ev = np.zeros(2, np.int64)
+    rc = ref_lib(variant).spref_nsm(C.byref(s), _ptr(u0, C.c_uint32), seed, _ptr(out, C.c_int32),
+                                    _ptr(ev, C.c_int64))
+    if rc != 0:
+        raise RuntimeError(f"reference NSM failed ({rc})")
+    return out, ev
+
+
+def ref_sdpd(sc, nsteps: int):
+    n = sc.num_particles
+    s = scenario_struct(sc)
+    x = np.zeros((n, 3))
+    v = np.zeros((n, 3))
+    rho = np.zeros(n)
+    rc = ref_lib().spref_sdpd(C.byref(s), nsteps, _ptr(x, C.c_double), _ptr(v, C.c_double),
+                              _ptr(rho, C.c_double))
+    if rc != 0:
+        raise RuntimeError(f"reference SDPD failed ({rc})")
+    return x, v, rho

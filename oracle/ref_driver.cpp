@@ -1,0 +1,281 @@
+/*
+ * ref_driver.cpp — TEST INFRASTRUCTURE (oracle).  Project-written driver that
+ * links the UNMODIFIED SpatialPy C++ engine sources (compiled by
+ * oracle/build_ref.sh into oracle/_ref/) and exposes them through a small C
+ * API for the parity tests and the CPU baseline.  Nothing in the product
+ * links or loads this file.
+ *
+ * It replaces the code that Solver.compile() would generate from
+ * propensity_file_template.cpp (main at :101-142): the particle set-up of
+ * init_all_particles (:73-90), the mass-action propensity functions
+ * (solver.py:344-373 from reaction.py:260-313), get_next_output
+ * (solver.py:290-299), an empty applyBoundaryConditions (no BCs), and
+ * `rng`/`debug_flag`.  The step loop replays run_simulation
+ * (src/simulate_threads.cpp:232-281) with one worker thread and no output
+ * thread: per step buildKDTree, take_step substeps 0,1,2 over all particles
+ * in vector order, then simulate_rdme.
+ */
+#include <cstdint>
+#include <cstring>
+#include <cstdio>
+#include <vector>
+#include <random>
+
+#include "particle_system.hpp"
+#include "simulate.hpp"
+#include "simulate_rdme.hpp"
+#include "model.hpp"
+#include "propensities.hpp"
+#include "spgpu.h"
+
+int debug_flag = 0;
+std::mt19937_64 rng;
+
+namespace Spatialpy {
+void buildKDTree(ParticleSystem *system);   /* simulate_threads.cpp:80 */
+double *parameters = nullptr;
+
+namespace {
+constexpr int kMaxRxn = 64;
+int g_R = 0, g_T = 0;
+int g_kind[kMaxRxn];
+double g_k[kMaxRxn];
+int g_a[kMaxRxn], g_b[kMaxRxn];
+std::vector<uint8_t> g_allowed;   /* [R*(T+1)] */
+std::vector<unsigned int> g_outsteps;
+size_t g_outidx = 0;
+
+/* Mass-action propensity with the operator order of the generated C++
+ * (e.g. "k_birth*vol", "k*A*B/vol"); x is the engine's unsigned int* xx read
+ * as int like the generated functions' `const int *x`. */
+template <int R>
+double massaction(const unsigned int *xu, double, double vol, double *, int sd) {
+    const int *x = reinterpret_cast<const int *>(xu);
+    if (!g_allowed.empty() && !g_allowed[(size_t)R * (g_T + 1) + sd]) return 0.0;
+    const double k = g_k[R];
+    switch (g_kind[R]) {
+        case SP_RXN_ZERO:   return k * vol;
+        case SP_RXN_FIRST:  return k * x[g_a[R]];
+        case SP_RXN_SECOND: return k * x[g_a[R]] * x[g_b[R]] / vol;
+        default:            return k * x[g_a[R]] * (x[g_a[R]] - 1) / vol;
+    }
+}
+
+template <int... Is> struct Table {
+    static PropensityFun *make() {
+        static PropensityFun t[] = {(PropensityFun)&massaction<Is>...};
+        return t;
+    }
+};
+template <int N, int... Is> struct Gen : Gen<N - 1, N - 1, Is...> {};
+template <int... Is> struct Gen<0, Is...> { using type = Table<Is...>; };
+}  // namespace
+
+unsigned int get_next_output(ParticleSystem *) {
+    if (g_outidx < g_outsteps.size()) return g_outsteps[g_outidx++];
+    return 0xffffffffu;
+}
+void applyBoundaryConditions(Particle *, ParticleSystem *) {}
+}  // namespace Spatialpy
+
+using namespace Spatialpy;
+
+namespace {
+
+struct Built {
+    ParticleSystem *sys = nullptr;
+    std::vector<size_t> irN, jcN, irG, jcG;
+    std::vector<int> prN;
+    std::vector<unsigned int> u0;
+    std::vector<int> Ndense;
+    ~Built() { delete sys; }
+};
+
+int load_network(const sp_scenario *sc) {
+    if (sc->num_reactions > kMaxRxn) return SP_E_UNSUPPORTED;
+    g_R = sc->num_reactions;
+    g_T = sc->num_types;
+    for (int r = 0; r < g_R; r++) {
+        g_kind[r] = sc->rxn_kind[r];
+        g_k[r] = sc->rxn_rate[r];
+        g_a[r] = sc->rxn_reactants[2 * r];
+        g_b[r] = sc->rxn_reactants[2 * r + 1];
+    }
+    g_allowed.clear();
+    if (sc->rxn_allowed) g_allowed.assign(sc->rxn_allowed, sc->rxn_allowed + (size_t)g_R * (g_T + 1));
+    g_outsteps.assign(sc->output_steps, sc->output_steps + sc->num_outputs);
+    g_outidx = 0;
+    return SP_OK;
+}
+
+/* Dependency graph as Model.__create_dependency_graph builds it for
+ * mass-action models (model.py:187-250): column s lists reactions having s as
+ * reactant; column S+r lists reactions whose reactants are touched by r. */
+void dep_graph(const sp_scenario *sc, Built &b) {
+    const int S = sc->num_species, R = sc->num_reactions;
+    std::vector<std::vector<int>> reac(R), touched(R);
+    for (int r = 0; r < R; r++) {
+        for (int q = 0; q < 2; q++) {
+            int a = sc->rxn_reactants[2 * r + q];
+            if (a >= 0) reac[r].push_back(a);
+        }
+        for (int64_t i = sc->jcN[r]; i < sc->jcN[r + 1]; i++) touched[r].push_back((int)sc->irN[i]);
+        for (int a : reac[r]) touched[r].push_back(a);
+    }
+    std::vector<std::vector<char>> G(R, std::vector<char>(S + R, 0));
+    for (int s = 0; s < S; s++)
+        for (int j = 0; j < R; j++)
+            for (int a : reac[j]) if (a == s) G[j][s] = 1;
+    for (int r = 0; r < R; r++)
+        for (int s : touched[r])
+            for (int j = 0; j < R; j++)
+                for (int a : reac[j]) if (a == s) G[j][S + r] = 1;
+    b.jcG.assign(1, 0);
+    for (int c = 0; c < S + R; c++) {
+        for (int r = 0; r < R; r++) if (G[r][c]) b.irG.push_back(r);
+        b.jcG.push_back(b.irG.size());
+    }
+}
+
+int build(const sp_scenario *sc, Built &b, int with_rdme) {
+    int rc = load_network(sc);
+    if (rc) return rc;
+    const int S = sc->num_species, R = sc->num_reactions, N = sc->num_particles;
+    b.sys = new ParticleSystem(sc->num_types, 0, 0, with_rdme ? S : 0, with_rdme ? R : 0, 0);
+    ParticleSystem *sys = b.sys;
+    sys->static_domain = sc->static_domain != 0;
+    sys->dt = sc->dt;
+    sys->nt = sc->num_steps;
+    sys->h = sc->h;
+    sys->rho0 = sc->rho0;
+    sys->c0 = sc->c0;
+    sys->P0 = sc->P0;
+    sys->dimension = sc->dimension;
+    for (int d = 0; d < 3; d++) sys->gravity[d] = sc->gravity[d];
+    sys->subdomain_diffusion_matrix = sc->diffusion;
+    sys->stoch_rxn_propensity_functions = Gen<kMaxRxn>::type::make();
+    sys->chem_rxn_rhs_functions = nullptr;
+    sys->stoichiometric_matrix = nullptr;
+    sys->species_names = nullptr;
+    sys->particles.reserve(N);
+    for (int i = 0; i < N; i++) {
+        Particle p(sys, (unsigned)i, sc->x[3 * i], sc->x[3 * i + 1], sc->x[3 * i + 2], sc->type[i],
+                   sc->nu[i], sc->mass[i], 0.0, sc->rho[i], sc->fixed[i]);
+        /* The engine never initialises these before take_step1 reads them
+           (particle.cpp:70-83); the oracle starts them at zero. */
+        for (int d = 0; d < 3; d++) {
+            p.vt[d] = p.F[d] = p.Fbp[d] = p.normal[d] = 0.0;
+            p.old_x[d] = p.x[d];
+            p.old_v[d] = 0.0;
+            if (sc->v) p.v[d] = sc->v[3 * i + d];
+        }
+        p.Frho = 0.0;
+        p.bvf_phi = 0.0;
+        p.old_rho = p.rho;
+        p.particle_index = (size_t)i;
+        sys->particles.emplace_back(p);
+    }
+    if (with_rdme && S > 0) {
+        b.irN.assign(sc->irN, sc->irN + sc->jcN[R]);
+        b.jcN.assign(sc->jcN, sc->jcN + R + 1);
+        b.prN.assign(sc->prN, sc->prN + sc->jcN[R]);
+        dep_graph(sc, b);
+    }
+    return SP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+/* Neighbour lists as the engine builds them (kd-tree + find_neighbors). */
+int spref_neighbors(const sp_scenario *sc, int32_t kmax, int32_t *count, int32_t *idx,
+                    double *dist, double *dwdr, double *dij) {
+    Built b;
+    int rc = build(sc, b, 0);
+    if (rc) return rc;
+    ParticleSystem *sys = b.sys;
+    buildKDTree(sys);
+    Particle *base = &sys->particles[0];
+    for (size_t i = 0; i < sys->particles.size(); i++) {
+        Particle &p = sys->particles[i];
+        p.find_neighbors(sys);
+        if ((int)p.neighbors.size() > kmax) return SP_E_INVALID;
+        count[i] = (int32_t)p.neighbors.size();
+        for (size_t k = 0; k < p.neighbors.size(); k++) {
+            const NeighborNode &n = p.neighbors[k];
+            idx[i * kmax + k] = (int32_t)(n.data - base);
+            dist[i * kmax + k] = n.dist;
+            dwdr[i * kmax + k] = n.dWdr;
+            dij[i * kmax + k] = n.D_i_j;
+        }
+    }
+    return SP_OK;
+}
+
+/*
+ * One NSM trajectory on a static domain, seeded like `ssa_sdpd.exe -s seed`
+ * (template :127).  out: [num_outputs][N][S] counts at output steps.
+ * counters: (total_reactions, total_diffusion).
+ */
+int spref_nsm(const sp_scenario *sc, const uint32_t *u0, uint64_t seed, int32_t *out,
+              int64_t *counters) {
+    Built b;
+    int rc = build(sc, b, 1);
+    if (rc) return rc;
+    ParticleSystem *sys = b.sys;
+    const int S = sc->num_species, N = sc->num_particles;
+    b.u0.assign(u0, u0 + (size_t)N * S);
+    rng = std::mt19937_64(seed);
+    initialize_rdme(sys, b.irN.data(), b.jcN.data(), b.prN.data(), b.irG.data(), b.jcG.data(),
+                    b.u0.data());
+    buildKDTree(sys);
+    unsigned int next_output = get_next_output(sys);
+    int oi = 0;
+    for (sys->current_step = 0; sys->current_step < sys->nt; sys->current_step++) {
+        if (sys->current_step >= next_output && oi < sc->num_outputs) {
+            std::memcpy(out + (size_t)oi * N * S, b.u0.data(), sizeof(uint32_t) * N * S);
+            oi++;
+            next_output = get_next_output(sys);
+        }
+        if (!sys->static_domain) return SP_E_UNSUPPORTED;
+        if (sys->current_step == 0)
+            for (auto &p : sys->particles) p.find_neighbors(sys);
+        simulate_rdme(sys, sys->current_step);
+    }
+    if (oi < sc->num_outputs) {
+        std::memcpy(out + (size_t)oi * N * S, b.u0.data(), sizeof(uint32_t) * N * S);
+        oi++;
+    }
+    counters[0] = sys->total_reactions;
+    counters[1] = sys->total_diffusion;
+    return SP_OK;
+}
+
+/*
+ * SDPD flow without species: nsteps engine steps (substeps 0,1,2 over all
+ * particles in order, single-threaded).  Writes final x[N*3], v[N*3],
+ * rho[N], and the last neighbour counts.
+ */
+int spref_sdpd(const sp_scenario *sc, int32_t nsteps, double *x, double *v, double *rho) {
+    Built b;
+    int rc = build(sc, b, 0);
+    if (rc) return rc;
+    ParticleSystem *sys = b.sys;
+    for (sys->current_step = 0; sys->current_step < (unsigned)nsteps; sys->current_step++) {
+        buildKDTree(sys);
+        for (unsigned sub = 0; sub < 3; sub++)
+            for (auto &p : sys->particles) take_step(&p, sys, sys->current_step, sub);
+    }
+    for (size_t i = 0; i < sys->particles.size(); i++) {
+        const Particle &p = sys->particles[i];
+        for (int d = 0; d < 3; d++) {
+            x[3 * i + d] = p.x[d];
+            v[3 * i + d] = p.v[d];
+        }
+        rho[i] = p.rho;
+    }
+    return SP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,275 @@
+/*
+ * sdpd_oracle_impl.h — TEST INFRASTRUCTURE.  Body of the SDPD oracle,
+ * included by sdpd_oracle.c once per arithmetic type (REAL = double/float,
+ * SPO_FN = function name).  Restates the engine step
+ * (src/simulate.cpp:56-173, src/model.cpp:39-329, src/particle.cpp:150-294)
+ * with one thread, in particle order.  Constants are cast to REAL so the
+ * float build computes in float throughout.
+ */
+#define K_(c) ((REAL)(c))
+
+static int SPO_NB(int n, int dim, const REAL *xq, const REAL *xt, REAL h, const REAL *mass,
+                  const REAL *rho, int kmax, int32_t *count, int32_t *idx, REAL *dist,
+                  REAL *dwdr) {
+    /* same predicate and order as spo_neighbors, in REAL arithmetic */
+    REAL lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    for (int d = 0; d < dim; d++) {
+        lo[d] = hi[d] = xt[d];
+        for (int i = 0; i < n; i++) {
+            REAL a = xt[3 * i + d], b = xq[3 * i + d];
+            if (a < lo[d]) lo[d] = a;
+            if (b < lo[d]) lo[d] = b;
+            if (a > hi[d]) hi[d] = a;
+            if (b > hi[d]) hi[d] = b;
+        }
+    }
+    const double cs = (double)h * 1.000001;
+    int nc[3] = {1, 1, 1};
+    for (int d = 0; d < dim; d++) nc[d] = (int)floor(((double)hi[d] - lo[d]) / cs) + 1;
+    const long ncell = (long)nc[0] * nc[1] * nc[2];
+    int32_t *start = (int32_t *)calloc((size_t)ncell + 1, sizeof(int32_t));
+    int32_t *cell = (int32_t *)malloc(sizeof(int32_t) * n);
+    int32_t *order = (int32_t *)malloc(sizeof(int32_t) * n);
+#define CELLD(p, d) ((d) < dim ? (int)fmin(nc[d] - 1, floor(((double)(p) - lo[d]) / cs)) : 0)
+    for (int i = 0; i < n; i++) {
+        cell[i] = (int32_t)(((long)CELLD(xt[3 * i], 0) * nc[1] + CELLD(xt[3 * i + 1], 1)) * nc[2] +
+                            CELLD(xt[3 * i + 2], 2));
+        start[cell[i] + 1]++;
+    }
+    for (long c = 0; c < ncell; c++) start[c + 1] += start[c];
+    int32_t *fill = (int32_t *)malloc(sizeof(int32_t) * ncell);
+    memcpy(fill, start, sizeof(int32_t) * ncell);
+    for (int i = 0; i < n; i++) order[fill[cell[i]]++] = i;
+    free(fill);
+    const REAL sq = h * h;
+    const REAL alpha = dim == 3 ? K_(105) / (K_(16) * K_(M_PI) * h * h * h)
+                     : dim == 2 ? K_(5) / (K_(M_PI) * h * h) : h;
+    int rc = 0;
+    REAL *cd2 = (REAL *)malloc(sizeof(REAL) * (kmax + 1));
+    int32_t *cj = (int32_t *)malloc(sizeof(int32_t) * (kmax + 1));
+    for (int i = 0; i < n && !rc; i++) {
+        const REAL *q = xq + 3 * i;
+        int qc[3];
+        for (int d = 0; d < 3; d++) qc[d] = CELLD(q[d], d);
+        int m = 0;
+        for (int a = qc[0] - 1; a <= qc[0] + 1 && !rc; a++) {
+            if (a < 0 || a >= nc[0]) continue;
+            for (int b = qc[1] - 1; b <= qc[1] + 1 && !rc; b++) {
+                if (b < 0 || b >= nc[1]) continue;
+                for (int c = qc[2] - 1; c <= qc[2] + 1 && !rc; c++) {
+                    if (c < 0 || c >= nc[2]) continue;
+                    long cid = ((long)a * nc[1] + b) * nc[2] + c;
+                    for (int32_t t = start[cid]; t < start[cid + 1]; t++) {
+                        int j = order[t];
+                        const REAL *p = xt + 3 * j;
+                        REAL d2 = 0;
+                        int d;
+                        for (d = 0; d < dim; d++) {
+                            REAL tt = q[d] - p[d];
+                            d2 = d2 + tt * tt;
+                            if (d2 > sq) break;
+                        }
+                        if (d < dim || d2 == 0) continue;
+                        if (SQRT(d2) > h) continue;
+                        if (m >= kmax) { rc = -1; break; }
+                        int k = m++;
+                        while (k > 0 && (d2 < cd2[k - 1] || (d2 == cd2[k - 1] && j < cj[k - 1]))) {
+                            cd2[k] = cd2[k - 1];
+                            cj[k] = cj[k - 1];
+                            k--;
+                        }
+                        cd2[k] = d2;
+                        cj[k] = j;
+                    }
+                }
+            }
+        }
+        count[i] = m;
+        for (int k = 0; k < m; k++) {
+            const REAL r = SQRT(cd2[k]);
+            const REAL R = r / h;
+            idx[(size_t)i * kmax + k] = cj[k];
+            dist[(size_t)i * kmax + k] = r;
+            dwdr[(size_t)i * kmax + k] = alpha * (K_(-12) * r / (h * h)) * ((K_(1) - R) * (K_(1) - R));
+        }
+    }
+#undef CELLD
+    free(cd2); free(cj); free(start); free(cell); free(order);
+    (void)mass; (void)rho;
+    return rc;
+}
+
+int SPO_FN(const sp_scenario *sc, int32_t step0, int32_t nsteps, int32_t mode, int32_t kmax,
+           double *x_io, double *v_io, double *vt_io, double *rho_io, double *F_io,
+           double *Fbp_io, double *Frho_io, int32_t *nbr_count) {
+    const int n = sc->num_particles, dim = sc->dimension;
+    const REAL h = (REAL)sc->h, dt = (REAL)sc->dt, rho0 = (REAL)sc->rho0, P0 = (REAL)sc->P0;
+    const REAL g[3] = {(REAL)sc->gravity[0], (REAL)sc->gravity[1], (REAL)sc->gravity[2]};
+    const REAL alpha = dim == 3 ? K_(105) / (K_(16) * K_(M_PI) * h * h * h)
+                     : dim == 2 ? K_(5) / (K_(M_PI) * h * h) : h;
+    REAL *x = (REAL *)malloc(sizeof(REAL) * 3 * n), *xt = (REAL *)malloc(sizeof(REAL) * 3 * n);
+    REAL *v = (REAL *)malloc(sizeof(REAL) * 3 * n), *vt = (REAL *)malloc(sizeof(REAL) * 3 * n);
+    REAL *F = (REAL *)malloc(sizeof(REAL) * 3 * n), *Fbp = (REAL *)malloc(sizeof(REAL) * 3 * n);
+    REAL *rho = (REAL *)malloc(sizeof(REAL) * n), *orho = (REAL *)malloc(sizeof(REAL) * n);
+    REAL *Frho = (REAL *)malloc(sizeof(REAL) * n), *m = (REAL *)malloc(sizeof(REAL) * n);
+    REAL *nu = (REAL *)malloc(sizeof(REAL) * n), *nrm = (REAL *)malloc(sizeof(REAL) * 3 * n);
+    REAL *ndist = (REAL *)malloc(sizeof(REAL) * (size_t)n * kmax);
+    REAL *ndw = (REAL *)malloc(sizeof(REAL) * (size_t)n * kmax);
+    int32_t *nidx = (int32_t *)malloc(sizeof(int32_t) * (size_t)n * kmax);
+    int32_t *ncnt = (int32_t *)malloc(sizeof(int32_t) * n);
+    for (int i = 0; i < 3 * n; i++) {
+        x[i] = (REAL)x_io[i]; v[i] = (REAL)v_io[i]; vt[i] = (REAL)vt_io[i];
+        F[i] = (REAL)F_io[i]; Fbp[i] = (REAL)Fbp_io[i];
+    }
+    for (int i = 0; i < n; i++) {
+        rho[i] = (REAL)rho_io[i]; Frho[i] = (REAL)Frho_io[i];
+        m[i] = (REAL)sc->mass[i]; nu[i] = (REAL)sc->nu[i];
+    }
+    int rc = 0;
+    for (int step = step0; step < step0 + nsteps && !rc; step++) {
+        memcpy(xt, x, sizeof(REAL) * 3 * n);            /* kd-tree points of this step */
+        /* substep 0: take_step1 (simulate.cpp:56-109) */
+        for (int i = 0; i < n; i++) {
+            for (int d = 0; d < 3; d++)
+                if (isnan((double)x[3 * i + d]) || !isfinite((double)x[3 * i + d]) ||
+                    isnan((double)v[3 * i + d]) || !isfinite((double)v[3 * i + d])) rc = 2;
+            if (isnan((double)rho[i]) || !isfinite((double)rho[i])) rc = 2;
+            if (!sc->fixed[i] && !sc->static_domain) {
+                for (int d = 0; d < 3; d++) {
+                    v[3 * i + d] = v[3 * i + d] + K_(0.5) * dt * F[3 * i + d];
+                    vt[3 * i + d] = v[3 * i + d] + K_(0.5) * dt * Fbp[3 * i + d];
+                    x[3 * i + d] = x[3 * i + d] + dt * vt[3 * i + d];
+                }
+                rho[i] = rho[i] + K_(0.5) * dt * Frho[i];
+            }
+            for (int d = 0; d < 3; d++) { F[3 * i + d] = g[d]; Fbp[3 * i + d] = 0; }
+            Frho[i] = 0;
+            orho[i] = rho[i];
+        }
+        if (rc) break;
+        /* neighbour lists used by substeps 1-2 (particle.cpp:240-294): at step 0
+           from the unmoved points; later from moved queries against the
+           start-of-step points (mode 2) or against moved points */
+        const REAL *q = (step == 0) ? xt : x;
+        const REAL *tp = (step == 0 || (mode & 2)) ? xt : x;
+        if (SPO_NB(n, dim, q, tp, h, m, rho, kmax, ncnt, nidx, ndist, ndw)) { rc = -1; break; }
+        /* substep 1: pairwiseForce (model.cpp:39-191) */
+        for (int i = 0; i < n; i++) {
+            const REAL Pi = P0 * (rho[i] / rho0 - K_(1.0));
+            REAL Fi[3] = {F[3 * i], F[3 * i + 1], F[3 * i + 2]};
+            REAL Fb[3] = {Fbp[3 * i], Fbp[3 * i + 1], Fbp[3 * i + 2]};
+            REAL Fr = Frho[i];
+            for (int k = 0; k < ncnt[i]; k++) {
+                const int j = nidx[(size_t)i * kmax + k];
+                const REAL r = ndist[(size_t)i * kmax + k];
+                const REAL R = r / h;
+                if (R > K_(1.0) || r == 0) continue;
+                const REAL dWdr = ndw[(size_t)i * kmax + k];
+                REAL dx[3] = {0, 0, 0}, dv[3] = {0, 0, 0}, dvdx = 0;
+                for (int d = 0; d < dim; d++) {
+                    dx[d] = x[3 * i + d] - x[3 * j + d];
+                    dv[d] = v[3 * i + d] - v[3 * j + d];
+                    dvdx = dvdx + dv[d] * dx[d];
+                }
+                const REAL Pj = P0 * (rho[j] / rho0 - K_(1.0));
+                REAL pg = Pi / (rho[i] * rho[i]) + Pj / (rho[j] * rho[j]);
+                if (pg < 0) pg = -Pi / (rho[i] * rho[i]) + Pj / (rho[j] * rho[j]);
+                const REAL rh = r + K_(0.001) * h;
+                const REAL fp = K_(-1.0) * m[j] * pg * dWdr / rh;
+                const REAL fv = m[j] * (K_(2.0) * (nu[i] * nu[j]) / (nu[i] + nu[j])) * (K_(1) / rh) * dWdr /
+                                (rho[i] * rho[j]);
+                const REAL vi = m[i] / rho[i], vj = m[j] / rho[j];
+                const REAL ss = vi * vi + vj * vj;
+                const REAL fbp = K_(-10.0) * P0 * (K_(1.0) / m[i]) * ss * dWdr / rh;
+                REAL ft[3];
+                for (int a = 0; a < 3; a++) {
+                    REAL tt0 = K_(0.5) * ((rho[i] * v[3 * i + a] * (vt[3 * i + 0] - v[3 * i + 0])) +
+                                         (rho[j] * v[3 * j + a] * (vt[3 * j + 0] - v[3 * j + 0])));
+                    REAL tt1 = K_(0.5) * ((rho[i] * v[3 * i + a] * (vt[3 * i + 1] - v[3 * i + 1])) +
+                                         (rho[j] * v[3 * j + a] * (vt[3 * j + 1] - v[3 * j + 1])));
+                    REAL tt2 = K_(0.5) * ((rho[i] * v[3 * i + a] * (vt[3 * i + 2] - v[3 * i + 2])) +
+                                         (rho[j] * v[3 * j + a] * (vt[3 * j + 2] - v[3 * j + 2])));
+                    ft[a] = (K_(1.0) / m[i]) * ss * (tt0 * dx[0] + tt1 * dx[1] + tt2 * dx[2]) * dWdr / rh;
+                }
+                for (int d = 0; d < dim; d++) {
+                    Fi[d] = Fi[d] + (fp * dx[d] + fv * dv[d] + ft[d]);
+                    Fb[d] = Fb[d] + fbp * dx[d];
+                }
+                const REAL tvi = (v[3 * i] - vt[3 * i]) * dx[0] + (v[3 * i + 1] - vt[3 * i + 1]) * dx[1] +
+                                 (v[3 * i + 2] - vt[3 * i + 2]) * dx[2];
+                const REAL tvj = (v[3 * j] - vt[3 * j]) * dx[0] + (v[3 * j + 1] - vt[3 * j + 1]) * dx[1] +
+                                 (v[3 * j + 2] - vt[3 * j + 2]) * dx[2];
+                /* the reference's middle term (model.cpp:144) is multiplied by
+                   0.0 and omitted here */
+                Fr = Fr + rho[i] * vj * dvdx * (K_(1) / rh) * dWdr -
+                     vj * (rho[i] * tvi + rho[j] * tvj) * (K_(1.0) / rh) * dWdr;
+            }
+            for (int d = 0; d < 3; d++) { F[3 * i + d] = Fi[d]; Fbp[3 * i + d] = Fb[d]; }
+            Frho[i] = Fr;
+        }
+        /* substep 2: take_step2 (simulate.cpp:132-173) */
+        const REAL *rb = (mode & 1) ? rho : orho;   /* density read by the BVF pass */
+        for (int i = 0; i < n; i++) {
+            const int fluid = !sc->fixed[i] && !sc->static_domain;
+            const int wall = sc->fixed[i] && !sc->static_domain;
+            if (fluid)
+                for (int d = 0; d < 3; d++) v[3 * i + d] = v[3 * i + d] + K_(0.5) * dt * F[3 * i + d];
+            if ((fluid || wall) && step % 20 == 0) {            /* filterDensity, model.cpp:194-233 */
+                REAL num = 0, den = 0;
+                for (int k = 0; k < ncnt[i]; k++) {
+                    const int j = nidx[(size_t)i * kmax + k];
+                    const REAL r = ndist[(size_t)i * kmax + k];
+                    const REAL R = r / h;
+                    if (R > K_(1.0) || r == 0) continue;
+                    const REAL omr = K_(1) - R;
+                    const REAL W = alpha * ((K_(1) + K_(3) * R) * (omr * omr * omr));
+                    num = num + orho[j] * W;
+                    den = den + W;
+                }
+                rho[i] = num / den;
+            }
+            if (fluid) {
+                rho[i] = rho[i] + K_(0.5) * dt * Frho[i];
+                /* computeBoundaryVolumeFraction, model.cpp:236-313 */
+                REAL nw[3] = {0, 0, 0}, vos = 0, vtot = 0;
+                for (int d = 0; d < dim; d++) vt[3 * i + d] = 0;
+                for (int k = 0; k < ncnt[i]; k++) {
+                    const int j = nidx[(size_t)i * kmax + k];
+                    const REAL r = ndist[(size_t)i * kmax + k];
+                    const REAL R = r / h;
+                    if (R > K_(1.0) || r == 0) continue;
+                    const REAL omr = K_(1) - R;
+                    const REAL W = alpha * ((K_(1) + K_(3) * R) * (omr * omr * omr));
+                    const REAL dWdr = ndw[(size_t)i * kmax + k];
+                    REAL dx[3] = {0, 0, 0};
+                    for (int d = 0; d < dim; d++) dx[d] = x[3 * i + d] - x[3 * j + d];
+                    const REAL vj = m[j] / rb[j];
+                    const REAL vv = vj * vj;
+                    if (sc->fixed[j]) vos = vos + vv * W;
+                    vtot = vtot + vv * W;
+                    if (sc->fixed[j])
+                        for (int a = 0; a < 3; a++) nw[a] = nw[a] + vv * dx[a] * dWdr / (r + K_(0.001) * h);
+                }
+                for (int a = 0; a < 3; a++) nw[a] = nw[a] / vtot;
+                const REAL nn = SQRT(nw[0] * nw[0] + nw[1] * nw[1] + nw[2] * nw[2]);
+                for (int a = 0; a < 3; a++) nrm[3 * i + a] = -nw[a] / nn;
+                const REAL phi = FABS(vos / vtot);
+                /* applyBoundaryVolumeFraction, model.cpp:316-329 */
+                const REAL vdn = v[3 * i] * nrm[3 * i] + v[3 * i + 1] * nrm[3 * i + 1] +
+                                 v[3 * i + 2] * nrm[3 * i + 2];
+                if (phi >= K_(0.5))
+                    for (int d = 0; d < dim; d++)
+                        v[3 * i + d] = -v[3 * i + d] + K_(2.0) * FMAX(K_(0.0), vdn) * nrm[3 * i + d];
+            }
+        }
+    }
+    for (int i = 0; i < 3 * n; i++) {
+        x_io[i] = x[i]; v_io[i] = v[i]; vt_io[i] = vt[i]; F_io[i] = F[i]; Fbp_io[i] = Fbp[i];
+    }
+    for (int i = 0; i < n; i++) { rho_io[i] = rho[i]; Frho_io[i] = Frho[i]; }
+    if (nbr_count) memcpy(nbr_count, ncnt, sizeof(int32_t) * n);
+    free(x); free(xt); free(v); free(vt); free(F); free(Fbp); free(rho); free(orho); free(Frho);
+    free(m); free(nu); free(nrm); free(ndist); free(ndw); free(nidx); free(ncnt);
+    return rc;
+}
+#undef K_

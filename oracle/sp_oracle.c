@@ -1,0 +1,502 @@
+/*
+ * sp_oracle.c — TEST INFRASTRUCTURE.  CPU restatement of the SpatialPy NSM
+ * hot path (see sp_oracle.h).  Compiled with -ffp-contract=off so every
+ * floating-point operation rounds exactly as written; the GPU engine uses the
+ * same operation order and is compared with this file bit for bit.
+ */
+#include "sp_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+#include <unistd.h>
+
+/* ------------------------------------------------------------------------
+ * Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as
+ * easy as 1, 2, 3", SC'11): 10 rounds of two 32x32->64 multiplies with the
+ * published multipliers and Weyl key increments.
+ * ------------------------------------------------------------------------ */
+void spo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+    uint32_t k0 = key[0], k1 = key[1];
+    for (int r = 0; r < 10; r++) {
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        c0 = hi1 ^ c1 ^ k0;
+        c1 = lo1;
+        c2 = hi0 ^ c3 ^ k1;
+        c3 = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+/* u in (0,1) from 32 random bits: (r + 1/2) 2^-32, exact in double */
+static inline double u01(uint32_t r) { return ((double)r + 0.5) * (1.0 / 4294967296.0); }
+
+/* ------------------------------------------------------------------------
+ * -log(u), u in (0,1).  Cody-Waite style reduction u = m 2^e with m in
+ * [sqrt(1/2), sqrt(2)), then log m = 2 atanh(z), z = (m-1)/(m+1), summed as
+ * the Maclaurin series of atanh (coefficients 1/(2k+1)) to w^10, w = z^2,
+ * |z| <= 0.1716 so the truncation error is below 1e-18.  ln 2 is split into
+ * a head with the low 21 mantissa bits cleared (e * head is exact for
+ * |e| < 2^21) and the double nearest to ln 2 - head.
+ * ------------------------------------------------------------------------ */
+double spo_neglog(double u) {
+    uint64_t b;
+    memcpy(&b, &u, 8);
+    int e = (int)((b >> 52) & 0x7ff) - 1023;
+    b = (b & 0x000fffffffffffffull) | 0x3ff0000000000000ull;   /* m in [1,2) */
+    double m;
+    memcpy(&m, &b, 8);
+    if (m > 1.4142135623730951) { m = m * 0.5; e = e + 1; }
+    double z = (m - 1.0) / (m + 1.0);
+    double w = z * z;
+    double p = 1.0 / 21.0;
+    p = p * w + 1.0 / 19.0;
+    p = p * w + 1.0 / 17.0;
+    p = p * w + 1.0 / 15.0;
+    p = p * w + 1.0 / 13.0;
+    p = p * w + 1.0 / 11.0;
+    p = p * w + 1.0 / 9.0;
+    p = p * w + 1.0 / 7.0;
+    p = p * w + 1.0 / 5.0;
+    p = p * w + 1.0 / 3.0;
+    p = p * w + 1.0;
+    double logm = (2.0 * z) * p;
+    const double ln2_hi = 6.931471803691238e-01;    /* 0x3fe62e42fee00000 */
+    const double ln2_lo = 1.9082149292705877e-10;   /* 0x3dea39ef35793c76 */
+    double ed = (double)e;
+    double r = ed * ln2_hi + (ed * ln2_lo + logm);
+    return -r;
+}
+
+/* ------------------------------------------------------------------------
+ * Neighbour search with the ANN fixed-radius predicate.
+ * ------------------------------------------------------------------------ */
+typedef struct { double d2; int32_t j; } cand_t;
+
+static int cand_less(const cand_t *a, const cand_t *b) {
+    return a->d2 < b->d2 || (a->d2 == b->d2 && a->j < b->j);
+}
+
+static double kernel_alpha(int dim, double h) {
+    /* particle.cpp:168-175 (1D: `5 / 4 * h` is integer 5/4 = 1 times h) */
+    if (dim == 3) return 105 / (16 * M_PI * h * h * h);
+    if (dim == 2) return 5 / (M_PI * h * h);
+    return 1 * h;
+}
+
+int spo_neighbors(int32_t n, int32_t dim, const double *xq, const double *xt, double h,
+                  const double *mass, const double *rho, int32_t kmax, int32_t *count,
+                  int32_t *idx, double *dist, double *dwdr, double *dij) {
+    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    for (int d = 0; d < dim; d++) {
+        lo[d] = hi[d] = xt[d];
+        for (int i = 0; i < n; i++) {
+            double a = xt[3 * i + d], b = xq[3 * i + d];
+            if (a < lo[d]) lo[d] = a;
+            if (b < lo[d]) lo[d] = b;
+            if (a > hi[d]) hi[d] = a;
+            if (b > hi[d]) hi[d] = b;
+        }
+    }
+    const double cs = h * 1.0000001;
+    int nc[3] = {1, 1, 1};
+    for (int d = 0; d < dim; d++) nc[d] = (int)floor((hi[d] - lo[d]) / cs) + 1;
+    const long ncell = (long)nc[0] * nc[1] * nc[2];
+    int32_t *start = (int32_t *)calloc((size_t)ncell + 1, sizeof(int32_t));
+    int32_t *cell = (int32_t *)malloc(sizeof(int32_t) * (size_t)n);
+    int32_t *order = (int32_t *)malloc(sizeof(int32_t) * (size_t)n);
+    #define CELLC(p, d) ((d) < dim ? (int)fmin(nc[d] - 1, floor(((p) - lo[d]) / cs)) : 0)
+    for (int i = 0; i < n; i++) {
+        int c0 = CELLC(xt[3 * i], 0), c1 = CELLC(xt[3 * i + 1], 1), c2 = CELLC(xt[3 * i + 2], 2);
+        cell[i] = (int32_t)(((long)c0 * nc[1] + c1) * nc[2] + c2);
+        start[cell[i] + 1]++;
+    }
+    for (long c = 0; c < ncell; c++) start[c + 1] += start[c];
+    int32_t *fill = (int32_t *)malloc(sizeof(int32_t) * (size_t)ncell);
+    memcpy(fill, start, sizeof(int32_t) * (size_t)ncell);
+    for (int i = 0; i < n; i++) order[fill[cell[i]]++] = i;
+    free(fill);
+
+    const double sq = h * h;          /* ANNdist dist = system->h * system->h (particle.cpp:253) */
+    const double alpha = kernel_alpha(dim, h);
+    int rc = 0;
+    cand_t *cand = (cand_t *)malloc(sizeof(cand_t) * (size_t)(kmax + 1));
+    for (int i = 0; i < n && rc == 0; i++) {
+        const double *q = xq + 3 * i;
+        int qc[3];
+        for (int d = 0; d < 3; d++) qc[d] = CELLC(q[d], d);
+        int m = 0;
+        for (int a = qc[0] - 1; a <= qc[0] + 1; a++) {
+            if (a < 0 || a >= nc[0]) continue;
+            for (int b = qc[1] - 1; b <= qc[1] + 1; b++) {
+                if (b < 0 || b >= nc[1]) continue;
+                for (int c = qc[2] - 1; c <= qc[2] + 1; c++) {
+                    if (c < 0 || c >= nc[2]) continue;
+                    long cid = ((long)a * nc[1] + b) * nc[2] + c;
+                    for (int32_t t = start[cid]; t < start[cid + 1]; t++) {
+                        int j = order[t];
+                        const double *p = xt + 3 * j;
+                        double d2 = 0;
+                        int d;
+                        for (d = 0; d < dim; d++) {       /* kd_fix_rad_search.cpp:160-170 */
+                            double tt = q[d] - p[d];
+                            d2 = d2 + tt * tt;
+                            if (d2 > sq) break;
+                        }
+                        if (d < dim || d2 == 0) continue;  /* :173-174, no self match */
+                        if (sqrt(d2) > h) continue;         /* particle.cpp:160-162 */
+                        if (m >= kmax) { rc = -1; break; }
+                        cand_t cd = {d2, j};
+                        int k = m++;
+                        while (k > 0 && cand_less(&cd, &cand[k - 1])) { cand[k] = cand[k - 1]; k--; }
+                        cand[k] = cd;
+                    }
+                    if (rc) break;
+                }
+                if (rc) break;
+            }
+            if (rc) break;
+        }
+        count[i] = m;
+        for (int k = 0; k < m; k++) {
+            const int j = cand[k].j;
+            const double r2 = cand[k].d2;
+            const double r = sqrt(r2);
+            /* particle.cpp:165-187 */
+            const double R = r / h;
+            const double dW = alpha * (-12 * r / (h * h)) * ((1 - R) * (1 - R));
+            const double ih = 1.0 / h;
+            const double ihsq = ih * ih;
+            const double dhr = h - r;
+            const double wfd = -25.066903536973515383e0 * dhr * dhr * ihsq * ihsq * ihsq * ih;
+            const double D = -2.0 * (mass[i] * mass[j]) / (mass[i] + mass[j]) * (rho[i] + rho[j]) /
+                             (rho[i] * rho[j]) * r2 * wfd / (r2 + 0.01 * h * h);
+            idx[(size_t)i * kmax + k] = j;
+            if (dist) dist[(size_t)i * kmax + k] = r;
+            if (dwdr) dwdr[(size_t)i * kmax + k] = dW;
+            if (dij) dij[(size_t)i * kmax + k] = D;
+        }
+    }
+    #undef CELLC
+    free(cand);
+    free(start);
+    free(cell);
+    free(order);
+    return rc;
+}
+
+void spo_diffusion_tables(const sp_scenario *sc, int32_t kmax, const int32_t *count,
+                          const int32_t *idx, const double *dij, double *ddiag, double *cdf) {
+    const int S = sc->num_species, T = sc->num_types;
+    for (int i = 0; i < sc->num_particles; i++) {
+        for (int s = 0; s < S; s++) {
+            double acc = 0.0;
+            for (int k = 0; k < count[i]; k++) {
+                const int j = idx[(size_t)i * kmax + k];
+                const double dc = sc->diffusion[s * T + (sc->type[j] - 1)];
+                acc = acc + dc * dij[(size_t)i * kmax + k];     /* simulate_rdme.cpp:146-147 */
+                if (cdf) cdf[((size_t)i * S + s) * kmax + k] = acc;
+            }
+            ddiag[(size_t)i * S + s] = acc;
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------
+ * NSM
+ * ------------------------------------------------------------------------ */
+typedef struct {
+    const sp_scenario *sc;
+    int N, S, R, T, K;
+    int32_t *cnt, *idx;
+    double *cdf, *ddiag, *vol;
+} nsm_tables_t;
+
+static int tables_build(const sp_scenario *sc, nsm_tables_t *t) {
+    const int N = sc->num_particles;
+    memset(t, 0, sizeof(*t));
+    t->sc = sc;
+    t->N = N;
+    t->S = sc->num_species;
+    t->R = sc->num_reactions;
+    t->T = sc->num_types;
+    int K = 16;
+    for (;;) {
+        t->cnt = (int32_t *)malloc(sizeof(int32_t) * N);
+        t->idx = (int32_t *)malloc(sizeof(int32_t) * (size_t)N * K);
+        double *dij = (double *)malloc(sizeof(double) * (size_t)N * K);
+        int rc = spo_neighbors(N, sc->dimension, sc->x, sc->x, sc->h, sc->mass, sc->rho, K,
+                               t->cnt, t->idx, NULL, NULL, dij);
+        if (rc == 0) {
+            t->K = K;
+            t->cdf = (double *)malloc(sizeof(double) * (size_t)N * t->S * K);
+            t->ddiag = (double *)malloc(sizeof(double) * (size_t)N * t->S);
+            spo_diffusion_tables(sc, K, t->cnt, t->idx, dij, t->ddiag, t->cdf);
+            free(dij);
+            break;
+        }
+        free(t->cnt);
+        free(t->idx);
+        free(dij);
+        K *= 2;
+    }
+    t->vol = (double *)malloc(sizeof(double) * N);
+    for (int i = 0; i < N; i++) t->vol[i] = sc->mass[i] / sc->rho[i];
+    return 0;
+}
+
+static void tables_free(nsm_tables_t *t) {
+    free(t->cnt); free(t->idx); free(t->cdf); free(t->ddiag); free(t->vol);
+}
+
+/* mass-action propensity, operator order of the generated code */
+static inline double prop(const sp_scenario *sc, int r, const int32_t *x, double vol, int type) {
+    if (sc->rxn_allowed && !sc->rxn_allowed[(size_t)r * (sc->num_types + 1) + type]) return 0.0;
+    const double k = sc->rxn_rate[r];
+    const int a = sc->rxn_reactants[2 * r], b = sc->rxn_reactants[2 * r + 1];
+    switch (sc->rxn_kind[r]) {
+        case SP_RXN_ZERO: return k * vol;
+        case SP_RXN_FIRST: return k * (double)x[a];
+        case SP_RXN_SECOND: return k * (double)x[a] * (double)x[b] / vol;
+        default: return k * (double)x[a] * (double)(x[a] - 1) / vol;
+    }
+}
+
+static inline void voxel_rates(const nsm_tables_t *t, int v, const int32_t *x, double vol,
+                               double *srr, double *sdr) {
+    double a = 0.0;
+    for (int r = 0; r < t->R; r++) a = a + prop(t->sc, r, x, vol, t->sc->type[v]);
+    double d = 0.0;
+    for (int s = 0; s < t->S; s++) d = d + t->ddiag[(size_t)v * t->S + s] * (double)x[s];
+    *srr = a;
+    *sdr = d;
+}
+
+/* indexed binary heap over (tau, voxel) */
+typedef struct { int n; int32_t *heap, *pos; double *tau; } heap_t;
+
+static inline int hless(const heap_t *h, int a, int b) {
+    return h->tau[a] < h->tau[b] || (h->tau[a] == h->tau[b] && a < b);
+}
+static void hswap(heap_t *h, int i, int j) {
+    int32_t a = h->heap[i], b = h->heap[j];
+    h->heap[i] = b; h->heap[j] = a;
+    h->pos[b] = i; h->pos[a] = j;
+}
+static void hfix(heap_t *h, int v) {
+    int i = h->pos[v];
+    while (i > 0) {
+        int p = (i - 1) / 2;
+        if (!hless(h, h->heap[i], h->heap[p])) break;
+        hswap(h, i, p);
+        i = p;
+    }
+    for (;;) {
+        int l = 2 * i + 1, r = l + 1, m = i;
+        if (l < h->n && hless(h, h->heap[l], h->heap[m])) m = l;
+        if (r < h->n && hless(h, h->heap[r], h->heap[m])) m = r;
+        if (m == i) break;
+        hswap(h, i, m);
+        i = m;
+    }
+}
+
+static inline double draw_time(double t, double e, double a) {
+    return a > 0.0 ? t + e / a : HUGE_VAL;
+}
+
+static int nsm_run(const nsm_tables_t *t, const uint32_t *u0, uint64_t seed, int selection,
+                   int32_t *out, int64_t *ev) {
+    const sp_scenario *sc = t->sc;
+    const int N = t->N, S = t->S, K = t->K;
+    int32_t *x = (int32_t *)malloc(sizeof(int32_t) * (size_t)N * S);
+    for (size_t i = 0; i < (size_t)N * S; i++) x[i] = (int32_t)u0[i];
+    heap_t h;
+    h.n = N;
+    h.heap = (int32_t *)malloc(sizeof(int32_t) * N);
+    h.pos = (int32_t *)malloc(sizeof(int32_t) * N);
+    h.tau = (double *)malloc(sizeof(double) * N);
+    const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    /* queue build at t0 = 0 (NRMConstant_v5::build, :52-71): stream 1 */
+    for (int v = 0; v < N; v++) {
+        double srr, sdr;
+        voxel_rates(t, v, x + (size_t)v * S, t->vol[v], &srr, &sdr);
+        uint32_t ctr[4] = {(uint32_t)v, 0u, 1u, 0u}, r[4];
+        spo_philox4x32_10(ctr, key, r);
+        h.tau[v] = draw_time(0.0, spo_neglog(u01(r[0])), srr + sdr);
+        h.heap[v] = v;
+        h.pos[v] = v;
+    }
+    for (int i = N / 2 - 1; i >= 0; i--) {      /* heapify */
+        int j = i;
+        for (;;) {
+            int l = 2 * j + 1, rr = l + 1, m = j;
+            if (l < N && hless(&h, h.heap[l], h.heap[m])) m = l;
+            if (rr < N && hless(&h, h.heap[rr], h.heap[m])) m = rr;
+            if (m == j) break;
+            hswap(&h, j, m);
+            j = m;
+        }
+    }
+    uint64_t evn = 0;
+    int64_t nrx = 0, ndf = 0;
+    int status = SP_TRAJ_OK;
+    int oi = 0;
+    const int nout = sc->num_outputs;
+    for (int step = 0; step < sc->num_steps && status == SP_TRAJ_OK; step++) {
+        while (oi < nout && sc->output_steps[oi] <= step) {
+            if (out) for (size_t i = 0; i < (size_t)N * S; i++) out[(size_t)oi * N * S + i] = x[i];
+            oi++;
+        }
+        const double t_end = sc->dt * (double)step + sc->dt;   /* simulate_rdme.cpp:67,215 */
+        for (;;) {
+            const int v = h.heap[0];
+            const double tt = h.tau[v];
+            if (tt == HUGE_VAL) break;
+            if (selection == SP_SELECT_EXACT && tt > t_end) break;
+            uint32_t ctr[4] = {(uint32_t)evn, (uint32_t)(evn >> 32), 0u, 0u}, r[4];
+            spo_philox4x32_10(ctr, key, r);
+            evn++;
+            const double ua = u01(r[0]), ub = u01(r[1]);
+            const double e0 = spo_neglog(u01(r[2])), e1 = spo_neglog(u01(r[3]));
+            int32_t *xv = x + (size_t)v * S;
+            double srr, sdr;
+            voxel_rates(t, v, xv, t->vol[v], &srr, &sdr);
+            const double tot = srr + sdr;
+            if (ua <= srr / tot) {                               /* :255 */
+                const double target = selection == SP_SELECT_EXACT ? ua * tot : ua * srr;
+                double cum = 0.0;
+                int re = -1, last = -1;
+                for (int q = 0; q < t->R; q++) {
+                    const double a = prop(sc, q, xv, t->vol[v], sc->type[v]);
+                    cum = cum + a;
+                    if (a > 0.0) {
+                        last = q;
+                        if (target <= cum) { re = q; break; }
+                    }
+                }
+                if (re < 0) re = last;
+                if (re < 0) { status = SP_TRAJ_SELECT_OVERFLOW; break; }
+                for (int64_t i = sc->jcN[re]; i < sc->jcN[re + 1]; i++) {   /* :285-296 */
+                    xv[sc->irN[i]] += sc->prN[i];
+                    if (xv[sc->irN[i]] < 0) status = SP_TRAJ_NEG_COUNT;
+                }
+                if (status) break;
+                voxel_rates(t, v, xv, t->vol[v], &srr, &sdr);
+                h.tau[v] = draw_time(tt, e0, srr + sdr);
+                hfix(&h, v);
+                nrx++;
+            } else {
+                const double target = selection == SP_SELECT_EXACT ? ua * tot - srr : ua * sdr;
+                double cum = 0.0;
+                int sp = -1, last = -1;
+                for (int s = 0; s < S; s++) {                      /* :319-321 */
+                    const double wgt = t->ddiag[(size_t)v * S + s] * (double)xv[s];
+                    cum = cum + wgt;
+                    if (wgt > 0.0) {
+                        last = s;
+                        if (target <= cum) { sp = s; break; }
+                    }
+                }
+                if (sp < 0) sp = last;
+                if (sp < 0) { status = SP_TRAJ_SELECT_OVERFLOW; break; }
+                const double target2 = ub * t->ddiag[(size_t)v * S + sp];   /* :353-354 */
+                const double *c = t->cdf + ((size_t)v * S + sp) * K;
+                int k = -1, lastk = -1;
+                double prev = 0.0;
+                for (int q = 0; q < t->cnt[v]; q++) {             /* :359-367 */
+                    if (c[q] > prev) {
+                        lastk = q;
+                        if (c[q] > target2) { k = q; break; }
+                    }
+                    prev = c[q];
+                }
+                if (k < 0) k = lastk;
+                if (k < 0) { status = SP_TRAJ_SELECT_OVERFLOW; break; }
+                const int w = t->idx[(size_t)v * K + k];
+                int32_t *xw = x + (size_t)w * S;
+                xv[sp] -= 1;                                          /* :394-402 */
+                xw[sp] += 1;
+                voxel_rates(t, v, xv, t->vol[v], &srr, &sdr);
+                h.tau[v] = draw_time(tt, e0, srr + sdr);
+                hfix(&h, v);
+                /* the engine evaluates the destination's reactions with the
+                   source voxel's volume (simulate_rdme.cpp:431-433) */
+                const double volw = selection == SP_SELECT_REFERENCE ? t->vol[v] : t->vol[w];
+                voxel_rates(t, w, xw, volw, &srr, &sdr);
+                h.tau[w] = draw_time(tt, e1, srr + sdr);
+                hfix(&h, w);
+                ndf++;
+            }
+            if (selection == SP_SELECT_REFERENCE && tt > t_end) break;   /* :233 */
+        }
+    }
+    while (out && oi < nout) {
+        for (size_t i = 0; i < (size_t)N * S; i++) out[(size_t)oi * N * S + i] = x[i];
+        oi++;
+    }
+    ev[0] = nrx;
+    ev[1] = ndf;
+    free(x); free(h.heap); free(h.pos); free(h.tau);
+    return status;
+}
+
+int spo_nsm_trajectory(const sp_scenario *sc, const uint32_t *u0, uint64_t seed, int32_t selection,
+                       int32_t *out, int64_t *ev) {
+    nsm_tables_t t;
+    tables_build(sc, &t);
+    int st = nsm_run(&t, u0, seed, selection, out, ev);
+    tables_free(&t);
+    return st;
+}
+
+typedef struct {
+    const nsm_tables_t *t;
+    const uint32_t *u0;
+    const uint64_t *seeds;
+    int ntraj, selection;
+    int32_t *out;
+    int64_t *ev;
+    int32_t *status;
+    int next;
+    pthread_mutex_t mu;
+} ens_t;
+
+static void *ens_worker(void *arg) {
+    ens_t *e = (ens_t *)arg;
+    const size_t per = (size_t)e->t->sc->num_outputs * e->t->N * e->t->S;
+    for (;;) {
+        pthread_mutex_lock(&e->mu);
+        int j = e->next++;
+        pthread_mutex_unlock(&e->mu);
+        if (j >= e->ntraj) break;
+        int st = nsm_run(e->t, e->u0, e->seeds[j], e->selection, e->out ? e->out + per * j : NULL,
+                         e->ev + 2 * j);
+        if (e->status) e->status[j] = st;
+    }
+    return NULL;
+}
+
+int spo_nsm_ensemble(const sp_scenario *sc, const uint32_t *u0, const uint64_t *seeds,
+                     int32_t ntraj, int32_t selection, int32_t threads, int32_t *out,
+                     int64_t *ev, int32_t *status) {
+    nsm_tables_t t;
+    tables_build(sc, &t);
+    if (threads <= 0) threads = (int)sysconf(_SC_NPROCESSORS_ONLN);
+    if (threads > ntraj) threads = ntraj;
+    if (threads < 1) threads = 1;
+    ens_t e = {&t, u0, seeds, ntraj, selection, out, ev, status, 0, PTHREAD_MUTEX_INITIALIZER};
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * threads);
+    for (int i = 0; i < threads; i++) pthread_create(&th[i], NULL, ens_worker, &e);
+    for (int i = 0; i < threads; i++) pthread_join(th[i], NULL);
+    free(th);
+    tables_free(&t);
+    return threads;
+}

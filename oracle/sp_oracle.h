@@ -1,0 +1,81 @@
+/*
+ * sp_oracle.h — TEST INFRASTRUCTURE.  CPU restatement ("oracle") of the
+ * SpatialPy engine hot path, used only by tests/, the smoke check and the
+ * CPU-baseline leg of bench.py.  It is never linked into libspgpu.so.
+ *
+ * NSM semantics follow nsm_core__take_step (src/simulate_rdme.cpp:211-472)
+ * and the NRM queue contract (src/NRMConstant_v5.cpp): per-voxel next-event
+ * times, fresh exponential draws for every voxel an event touches, events
+ * in increasing time.  The random streams are Philox4x32-10 (Salmon et al.,
+ * SC'11) keyed by the trajectory seed, so the GPU engine can be checked
+ * against this file event for event; against the reference's own
+ * mt19937_64 streams the comparison is statistical.
+ *
+ * Parity status: pinned.  The neighbour sets, dWdr and D_ij match the compiled
+ * reference (oracle/_ref, built by build_ref.sh) element-wise; the NSM
+ * ensembles match reference ensembles statistically (tests/golden/).
+ */
+#ifndef SP_ORACLE_H
+#define SP_ORACLE_H
+#include <stdint.h>
+#include "../include/spgpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Philox4x32-10 block: out = philox(ctr, key) */
+void spo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+/* -log(u) for u in (0,1), evaluated with a fixed operation order */
+double spo_neglog(double u);
+
+/* Neighbour lists (particle.cpp:150-210, kd_fix_rad_search.cpp:160-176):
+ * ascending r^2, ties by index; kmax per particle.  Positions `xq` are query
+ * points, `xt` the searched points (pass the same array for a static search).
+ * Returns 0, or -1 if a list overflows kmax. */
+int spo_neighbors(int32_t n, int32_t dim, const double *xq, const double *xt, double h,
+                  const double *mass, const double *rho, int32_t kmax, int32_t *count,
+                  int32_t *idx, double *dist, double *dwdr, double *dij);
+
+/* Ddiag[i*S+s] and cumulative weights cdf[(i*S+s)*kmax + k] from the lists
+ * (simulate_rdme.cpp:131-152 and the destination scan :353-367). */
+void spo_diffusion_tables(const sp_scenario *sc, int32_t kmax, const int32_t *count,
+                          const int32_t *idx, const double *dij, double *ddiag, double *cdf);
+
+/*
+ * Run one NSM trajectory on a static domain.
+ * out: [num_outputs][N][S] counts (may be NULL); ev: (reactions, diffusions).
+ * Returns SP_TRAJ_* status.
+ */
+int spo_nsm_trajectory(const sp_scenario *sc, const uint32_t *u0, uint64_t seed, int32_t selection,
+                       int32_t *out, int64_t *ev);
+
+/* Ensemble over `ntraj` seeds with `threads` POSIX threads (0 = all cores).
+ * out: [ntraj][num_outputs][N][S] or NULL; ev: [ntraj*2]. */
+int spo_nsm_ensemble(const sp_scenario *sc, const uint32_t *u0, const uint64_t *seeds,
+                     int32_t ntraj, int32_t selection, int32_t threads, int32_t *out,
+                     int64_t *ev, int32_t *status);
+
+/*
+ * Advance one NSM trajectory over an explicit window with caller-provided
+ * diffusion tables: used by the coupled SDPD test.  State in/out:
+ * counts[N*S], tau[N] (next-event times), ev_counter (Philox event index).
+ */
+
+/* SDPD flow (sdpd_oracle.c), FP64 and FP32 builds.  mode bits:
+ *   1 = Gauss-Seidel density reads in the boundary-volume-fraction pass (the
+ *       order a single engine thread produces, model.cpp:284-288)
+ *   2 = neighbour distances between moved query and start-of-step points (the
+ *       kd-tree is built once per step, simulate_threads.cpp:80-108)
+ * State arrays are [N*3] / [N] in double; nsteps engine steps from step0. */
+int spo_sdpd_f64(const sp_scenario *sc, int32_t step0, int32_t nsteps, int32_t mode, int32_t kmax,
+                 double *x, double *v, double *vt, double *rho, double *F, double *Fbp,
+                 double *Frho, int32_t *nbr_count);
+int spo_sdpd_f32(const sp_scenario *sc, int32_t step0, int32_t nsteps, int32_t mode, int32_t kmax,
+                 double *x, double *v, double *vt, double *rho, double *F, double *Fbp,
+                 double *Frho, int32_t *nbr_count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,663 @@
+// engine.cu — the C ABI of libspgpu (include/spgpu.h): handle lifecycle,
+// device set-up of model instances, and the host loop of an ensemble run.
+//
+// sp_create  = Solver.compile() + engine set-up (solver.py:443-507,
+//              propensity_file_template.cpp:101-142)
+// sp_run     = Solver.run()'s trajectory loop (solver.py:547-605) + the
+//              engine step loop run_simulation (simulate_threads.cpp:171-312)
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "neighbors.cuh"
+#include "sdpd.cuh"
+
+namespace spg {
+void launch_nsm_init(NsmTraj* trajs, const NsmInstance* insts, int ntraj, int max_leaf,
+                     int max_levels, const uint32_t* const* u0, cudaStream_t st);
+void launch_nsm_advance(bool ref, NsmTraj* trajs, const NsmInstance* insts, int ntraj,
+                        int step_end, double dt, long long budget, long long max_ns, int* work,
+                        int num_sms, cudaStream_t st);
+void launch_nsm_snapshot(const NsmTraj* trajs, const NsmInstance* insts, int ntraj,
+                         int32_t* counts, const long long* count_off, long long* moments,
+                         const long long* mom_off, int out_index, cudaStream_t st);
+}  // namespace spg
+
+using namespace spg;
+
+namespace {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t n = 0;
+};
+
+struct Instance {
+    int N = 0, S = 0, R = 0, T = 0, K = 0, dim = 0;
+    bool is_static = true;
+    double h = 0, rho0 = 0, c0 = 0, P0 = 0, g[3] = {0, 0, 0};
+    std::vector<double> x_host;
+    // device arrays
+    double *x = nullptr, *mass = nullptr, *rho = nullptr, *nu = nullptr, *vol = nullptr;
+    int *type = nullptr;
+    uint8_t* fixed = nullptr;
+    int *nbr_cnt = nullptr, *nbr_idx = nullptr;
+    double *nbr_dist = nullptr, *nbr_dwdr = nullptr, *nbr_dij = nullptr;
+    double *cdf = nullptr, *ddiag = nullptr;
+    double *rate = nullptr, *diffusion = nullptr;
+    int *kind = nullptr, *reac = nullptr, *jcN = nullptr, *irN = nullptr, *prN = nullptr;
+    uint8_t* allowed = nullptr;
+    uint32_t* u0 = nullptr;   // device copy for the current run
+    NsmInstance desc{};
+    SdpdState* sdpd = nullptr;
+};
+
+}  // namespace
+
+struct sp_handle {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    sp_options opt{};
+    std::vector<Instance> inst;
+    std::vector<void*> allocs;
+    NsmInstance* d_insts = nullptr;
+    double dt = 0;
+    int num_steps = 0;
+    std::vector<int> output_steps;
+    // run state
+    int traj_cap = 0;
+    size_t traj_bytes = 0;
+    void* traj_mem = nullptr;
+    NsmTraj* d_trajs = nullptr;
+    std::vector<NsmTraj> h_trajs;
+    int* d_work = nullptr;
+    std::string err;
+    double last_ms = 0;
+    long long last_launches = 0;
+};
+
+int spg_set_cuda_error(sp_handle* h, cudaError_t e, const char* what, const char* file, int line) {
+    if (h) {
+        char buf[512];
+        snprintf(buf, sizeof buf, "CUDA error %s (%s) at %s:%d: %s", cudaGetErrorName(e), what,
+                 file, line, cudaGetErrorString(e));
+        h->err = buf;
+    }
+    return e == cudaErrorMemoryAllocation ? SP_E_NOMEM : SP_E_CUDA;
+}
+
+static int fail(sp_handle* h, int code, const std::string& msg) {
+    if (h) h->err = msg;
+    return code;
+}
+
+template <typename T>
+static int dev_upload(sp_handle* h, T** dst, const T* src, size_t n) {
+    *dst = nullptr;
+    if (n == 0) return SP_OK;
+    SP_CUDA_TRY(cudaMalloc((void**)dst, sizeof(T) * n));
+    h->allocs.push_back(*dst);
+    if (src) SP_CUDA_TRY(cudaMemcpyAsync(*dst, src, sizeof(T) * n, cudaMemcpyHostToDevice, h->st));
+    return SP_OK;
+}
+
+template <typename T>
+static int dev_alloc(sp_handle* h, T** dst, size_t n) {
+    return dev_upload<T>(h, dst, nullptr, n);
+}
+
+static int validate(sp_handle* h, const sp_scenario& s, int i) {
+    char b[256];
+#define REQ(cond, msg)                                           \
+    if (!(cond)) {                                               \
+        snprintf(b, sizeof b, "scenario %d: %s", i, msg);        \
+        return fail(h, SP_E_INVALID, b);                         \
+    }
+    REQ(s.dimension >= 1 && s.dimension <= 3, "dimension must be 1, 2 or 3");
+    REQ(s.num_particles >= 1, "num_particles must be >= 1");
+    REQ(s.x && s.type && s.mass && s.rho && s.nu && s.fixed, "particle arrays must be set");
+    REQ(s.num_types >= 1, "num_types must be >= 1");
+    REQ(s.num_species >= 0 && s.num_species <= 32, "num_species must be in 0..32");
+    REQ(s.num_reactions >= 0 && s.num_reactions <= 1024, "num_reactions must be in 0..1024");
+    REQ(s.h > 0, "h (basis function width) can not be zero");
+    REQ(s.dt > 0 && s.num_steps >= 0, "dt must be > 0");
+    REQ(s.num_outputs >= 1 && s.output_steps, "output_steps must be set");
+    for (int k = 0; k < s.num_outputs; k++) {
+        REQ(s.output_steps[k] >= 0 && s.output_steps[k] <= s.num_steps, "output step out of range");
+        REQ(k == 0 || s.output_steps[k] > s.output_steps[k - 1], "output steps must ascend");
+    }
+    for (int p = 0; p < s.num_particles; p++) {
+        REQ(s.type[p] >= 1 && s.type[p] <= s.num_types, "particle type out of 1..num_types");
+        REQ(s.rho[p] != 0.0, "Rho must be a positive value");
+    }
+    if (s.num_species > 0) {
+        REQ(s.diffusion, "diffusion matrix must be set");
+        if (s.num_reactions > 0) {
+            REQ(s.rxn_rate && s.rxn_kind && s.rxn_reactants && s.jcN && s.irN && s.prN,
+                "reaction tables must be set");
+            REQ(s.jcN[0] == 0, "jcN[0] must be 0");
+        }
+        for (int r = 0; r < s.num_reactions; r++) {
+            const int k = s.rxn_kind[r];
+            REQ(k >= SP_RXN_ZERO && k <= SP_RXN_DIMER, "unknown reaction kind");
+            const int a = s.rxn_reactants[2 * r], bb = s.rxn_reactants[2 * r + 1];
+            REQ(k == SP_RXN_ZERO || (a >= 0 && a < s.num_species), "reactant index out of range");
+            REQ(k != SP_RXN_SECOND || (bb >= 0 && bb < s.num_species), "second reactant out of range");
+            REQ(s.jcN[r + 1] >= s.jcN[r], "jcN must be non-decreasing");
+            for (int64_t q = s.jcN[r]; q < s.jcN[r + 1]; q++)
+                REQ(s.irN[q] >= 0 && s.irN[q] < s.num_species, "irN out of range");
+        }
+    }
+#undef REQ
+    return SP_OK;
+}
+
+static void tree_layout(NsmInstance& d, int N) {
+    d.leaf_stride = (N + 31) / 32 * 32;
+    int size = d.leaf_stride, l = 0, off = 0;
+    d.level_size[0] = N;
+    d.level_off[0] = 0;
+    do {
+        size = (size + 31) / 32;
+        l++;
+        d.level_size[l] = size;
+        d.level_off[l] = off;
+        off += size;
+    } while (size > 1 && l < kMaxLevels);
+    d.levels = l;
+    d.num_nodes = off;
+}
+
+static int setup_instance(sp_handle* h, const sp_scenario& s, Instance& I) {
+    I.N = s.num_particles;
+    I.S = s.num_species;
+    I.R = s.num_reactions;
+    I.T = s.num_types;
+    I.dim = s.dimension;
+    I.h = s.h;
+    I.rho0 = s.rho0;
+    I.c0 = s.c0;
+    I.P0 = s.P0;
+    for (int d = 0; d < 3; d++) I.g[d] = s.gravity[d];
+    I.is_static = s.static_domain != 0;
+    const int N = I.N;
+    I.x_host.assign(s.x, s.x + 3 * (size_t)N);
+    int rc;
+    if ((rc = dev_upload(h, &I.x, s.x, 3 * (size_t)N))) return rc;
+    if ((rc = dev_upload(h, &I.type, s.type, N))) return rc;
+    if ((rc = dev_upload(h, &I.mass, s.mass, N))) return rc;
+    if ((rc = dev_upload(h, &I.rho, s.rho, N))) return rc;
+    if ((rc = dev_upload(h, &I.nu, s.nu, N))) return rc;
+    if ((rc = dev_upload(h, &I.fixed, s.fixed, N))) return rc;
+    std::vector<double> vol(N);
+    for (int p = 0; p < N; p++) vol[p] = s.mass[p] / s.rho[p];   // simulate_rdme.cpp:123
+    if ((rc = dev_upload(h, &I.vol, vol.data(), N))) return rc;
+    // reaction tables
+    const int R = I.R, S = I.S, T = I.T;
+    std::vector<int> jc(R + 1, 0), ir, pr;
+    if (R > 0) {
+        for (int r = 0; r <= R; r++) jc[r] = (int)s.jcN[r];
+        ir.assign(s.irN, s.irN + s.jcN[R]);
+        pr.assign(s.prN, s.prN + s.jcN[R]);
+        if ((rc = dev_upload(h, &I.rate, s.rxn_rate, R))) return rc;
+        if ((rc = dev_upload(h, &I.kind, s.rxn_kind, R))) return rc;
+        if ((rc = dev_upload(h, &I.reac, s.rxn_reactants, 2 * (size_t)R))) return rc;
+        if (s.rxn_allowed && (rc = dev_upload(h, &I.allowed, s.rxn_allowed, (size_t)R * (T + 1))))
+            return rc;
+    }
+    if ((rc = dev_upload(h, &I.jcN, jc.data(), jc.size()))) return rc;
+    if (!ir.empty()) {
+        if ((rc = dev_upload(h, &I.irN, ir.data(), ir.size()))) return rc;
+        if ((rc = dev_upload(h, &I.prN, pr.data(), pr.size()))) return rc;
+    }
+    if (S > 0 && (rc = dev_upload(h, &I.diffusion, s.diffusion, (size_t)S * T))) return rc;
+
+    if (I.is_static) {
+        // neighbour lists once (take_step1 at step 0, simulate.cpp:62-64)
+        CellGrid g = make_grid(s.x, N, I.dim, I.h);
+        int *cell, *hist, *start, *fill, *order, *flag;
+        if ((rc = dev_alloc(h, &cell, N))) return rc;
+        if ((rc = dev_alloc(h, &hist, g.ncell))) return rc;
+        if ((rc = dev_alloc(h, &start, (size_t)g.ncell + 1))) return rc;
+        if ((rc = dev_alloc(h, &fill, g.ncell))) return rc;
+        if ((rc = dev_alloc(h, &order, N))) return rc;
+        if ((rc = dev_alloc(h, &flag, 1))) return rc;
+        int kmax = 32;
+        for (;;) {
+            int *cnt, *idx;
+            double *dist, *dw, *dij;
+            if ((rc = dev_alloc(h, &cnt, N))) return rc;
+            if ((rc = dev_alloc(h, &idx, (size_t)N * kmax))) return rc;
+            if ((rc = dev_alloc(h, &dist, (size_t)N * kmax))) return rc;
+            if ((rc = dev_alloc(h, &dw, (size_t)N * kmax))) return rc;
+            if ((rc = dev_alloc(h, &dij, (size_t)N * kmax))) return rc;
+            const int over = run_neighbor_search(I.x, I.x, N, g, I.h, I.mass, I.rho, kmax, cnt, idx,
+                                                 dist, dw, dij, cell, hist, start, fill, order,
+                                                 flag, h->st);
+            SP_CUDA_TRY(cudaGetLastError());
+            if (!over) {
+                I.K = kmax;
+                I.nbr_cnt = cnt;
+                I.nbr_idx = idx;
+                I.nbr_dist = dist;
+                I.nbr_dwdr = dw;
+                I.nbr_dij = dij;
+                break;
+            }
+            if (kmax >= 256) return fail(h, SP_E_UNSUPPORTED, "more than 256 neighbours within h");
+            kmax *= 2;
+        }
+        if (S > 0) {
+            if ((rc = dev_alloc(h, &I.ddiag, (size_t)N * S))) return rc;
+            if ((rc = dev_alloc(h, &I.cdf, (size_t)N * S * I.K))) return rc;
+            launch_diffusion_tables(N, S, T, I.K, I.type, I.nbr_cnt, I.nbr_idx, I.nbr_dij,
+                                    I.diffusion, I.ddiag, I.cdf, h->st);
+            SP_CUDA_TRY(cudaGetLastError());
+        }
+    } else {
+        I.sdpd = sdpd_create(s, h->opt.sdpd_precision, h->st, &h->err);
+        if (!I.sdpd) return SP_E_CUDA;
+    }
+    NsmInstance& d = I.desc;
+    d.N = N;
+    d.S = S;
+    d.R = R;
+    d.T = T;
+    d.K = I.K;
+    tree_layout(d, N);
+    d.type = I.type;
+    d.vol = I.vol;
+    d.nbr_cnt = I.nbr_cnt;
+    d.nbr_idx = I.nbr_idx;
+    d.cdf = I.cdf;
+    d.ddiag = I.ddiag;
+    d.rate = I.rate;
+    d.kind = I.kind;
+    d.reac = I.reac;
+    d.allowed = I.allowed;
+    d.jcN = I.jcN;
+    d.irN = I.irN;
+    d.prN = I.prN;
+    return SP_OK;
+}
+
+extern "C" {
+
+int sp_abi_version(void) { return SP_ABI_VERSION; }
+
+int sp_create(const sp_scenario* scenarios, int32_t num_scenarios, const sp_options* opts,
+              sp_handle** out) {
+    if (!out) return SP_E_INVALID;
+    *out = nullptr;
+    if (!scenarios || num_scenarios < 1) return SP_E_INVALID;
+    sp_handle* h = new sp_handle();
+    if (opts) h->opt = *opts;
+    *out = h;
+    h->device = h->opt.device;
+    SP_CUDA_TRY(cudaSetDevice(h->device));
+    SP_CUDA_TRY(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device));
+    SP_CUDA_TRY(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+    SP_CUDA_TRY(cudaEventCreate(&h->e0));
+    SP_CUDA_TRY(cudaEventCreate(&h->e1));
+    for (int i = 0; i < num_scenarios; i++) {
+        int rc = validate(h, scenarios[i], i);
+        if (rc) return rc;
+    }
+    const sp_scenario& s0 = scenarios[0];
+    h->dt = s0.dt;
+    h->num_steps = s0.num_steps;
+    h->output_steps.assign(s0.output_steps, s0.output_steps + s0.num_outputs);
+    for (int i = 1; i < num_scenarios; i++) {
+        const sp_scenario& s = scenarios[i];
+        if (s.dt != s0.dt || s.num_steps != s0.num_steps || s.num_outputs != s0.num_outputs ||
+            !std::equal(s.output_steps, s.output_steps + s.num_outputs, s0.output_steps))
+            return fail(h, SP_E_INVALID, "all instances of one handle need the same time span");
+    }
+    h->inst.resize(num_scenarios);
+    std::vector<NsmInstance> descs(num_scenarios);
+    for (int i = 0; i < num_scenarios; i++) {
+        int rc = setup_instance(h, scenarios[i], h->inst[i]);
+        if (rc) return rc;
+        descs[i] = h->inst[i].desc;
+    }
+    int rc = dev_upload(h, &h->d_insts, descs.data(), descs.size());
+    if (rc) return rc;
+    if ((rc = dev_alloc(h, &h->d_work, 1))) return rc;
+    SP_CUDA_TRY(cudaStreamSynchronize(h->st));
+    return SP_OK;
+}
+
+static int ensure_traj(sp_handle* h, int ntraj, const int* inst) {
+    size_t bytes = sizeof(NsmTraj) * (size_t)ntraj;
+    std::vector<size_t> off(ntraj);
+    auto align = [](size_t b) { return (b + 255) / 256 * 256; };
+    bytes = align(bytes);
+    for (int j = 0; j < ntraj; j++) {
+        const NsmInstance& d = h->inst[inst[j]].desc;
+        off[j] = bytes;
+        bytes += align(sizeof(int32_t) * (size_t)d.N * d.S);
+        bytes += align(sizeof(double) * (size_t)d.leaf_stride);
+        bytes += align(sizeof(TreeNode) * (size_t)d.num_nodes);
+    }
+    if (bytes > h->traj_bytes) {
+        if (h->traj_mem) cudaFree(h->traj_mem);
+        h->traj_mem = nullptr;
+        h->traj_bytes = 0;
+        SP_CUDA_TRY(cudaMalloc(&h->traj_mem, bytes));
+        h->traj_bytes = bytes;
+    }
+    char* base = (char*)h->traj_mem;
+    h->d_trajs = (NsmTraj*)base;
+    h->h_trajs.assign(ntraj, NsmTraj{});
+    for (int j = 0; j < ntraj; j++) {
+        const NsmInstance& d = h->inst[inst[j]].desc;
+        NsmTraj& T = h->h_trajs[j];
+        T.inst = inst[j];
+        char* p = base + off[j];
+        T.x = (int32_t*)p;
+        p += align(sizeof(int32_t) * (size_t)d.N * d.S);
+        T.leaf = (double*)p;
+        p += align(sizeof(double) * (size_t)d.leaf_stride);
+        T.node = (TreeNode*)p;
+    }
+    return SP_OK;
+}
+
+int sp_run(sp_handle* h, const sp_run_args* a, sp_outputs* out) {
+    if (!h) return SP_E_INVALID;
+    if (!a || a->num_trajectories < 1 || !a->seeds || !a->u0)
+        return fail(h, SP_E_INVALID, "sp_run: num_trajectories, seeds and u0 are required");
+    if (a->selection != SP_SELECT_EXACT && a->selection != SP_SELECT_REFERENCE)
+        return fail(h, SP_E_INVALID, "sp_run: unknown selection mode");
+    SP_CUDA_TRY(cudaSetDevice(h->device));
+    const auto wall0 = std::chrono::steady_clock::now();
+    const int ntraj = a->num_trajectories;
+    const int ninst = (int)h->inst.size();
+    std::vector<int> inst(ntraj, 0);
+    for (int j = 0; j < ntraj; j++) {
+        inst[j] = a->instance ? a->instance[j] : 0;
+        if (inst[j] < 0 || inst[j] >= ninst) return fail(h, SP_E_INVALID, "instance index out of range");
+        if (!h->inst[inst[j]].is_static)
+            return fail(h, SP_E_UNSUPPORTED, "sp_run: moving (non-static) domains are run by sp_sdpd_advance");
+        if (h->inst[inst[j]].S == 0) return fail(h, SP_E_INVALID, "sp_run: model has no species");
+    }
+    int rc = ensure_traj(h, ntraj, inst.data());
+    if (rc) return rc;
+    for (int j = 0; j < ntraj; j++) {
+        NsmTraj& T = h->h_trajs[j];
+        T.key0 = (uint32_t)a->seeds[j];
+        T.key1 = (uint32_t)(a->seeds[j] >> 32);
+        T.status = SP_TRAJ_OK;
+        T.step = 0;
+        T.err_voxel = -1;
+        T.evn = 0;
+        T.nrx = T.ndf = 0;
+        T.t_last = 0.0;
+    }
+    cudaStream_t st = h->st;
+    long long launches = 0;
+    SP_CUDA_TRY(cudaEventRecord(h->e0, st));
+    SP_CUDA_TRY(cudaMemcpyAsync(h->d_trajs, h->h_trajs.data(), sizeof(NsmTraj) * ntraj,
+                                cudaMemcpyHostToDevice, st));
+    // initial counts (u0 per instance)
+    std::vector<const uint32_t*> u0ptr(ninst, nullptr);
+    std::vector<void*> tmp;
+    auto cleanup = [&]() {
+        for (void* p : tmp) cudaFree(p);
+    };
+    for (int i = 0; i < ninst; i++) {
+        const Instance& I = h->inst[i];
+        if (!a->u0[i]) continue;
+        if (a->buffers_on_device) {
+            u0ptr[i] = a->u0[i];
+        } else {
+            void* d = nullptr;
+            cudaError_t e = cudaMalloc(&d, sizeof(uint32_t) * (size_t)I.N * I.S);
+            if (e != cudaSuccess) { cleanup(); return spg_set_cuda_error(h, e, "cudaMalloc u0", __FILE__, __LINE__); }
+            tmp.push_back(d);
+            cudaMemcpyAsync(d, a->u0[i], sizeof(uint32_t) * (size_t)I.N * I.S,
+                            cudaMemcpyHostToDevice, st);
+            u0ptr[i] = (const uint32_t*)d;
+        }
+    }
+    for (int j = 0; j < ntraj; j++)
+        if (!u0ptr[inst[j]]) { cleanup(); return fail(h, SP_E_INVALID, "u0 missing for an instance in use"); }
+    const uint32_t** d_u0 = nullptr;
+    {
+        cudaError_t e = cudaMalloc(&d_u0, sizeof(void*) * ninst);
+        if (e != cudaSuccess) { cleanup(); return spg_set_cuda_error(h, e, "cudaMalloc", __FILE__, __LINE__); }
+        tmp.push_back(d_u0);
+        cudaMemcpyAsync(d_u0, u0ptr.data(), sizeof(void*) * ninst, cudaMemcpyHostToDevice, st);
+    }
+    int max_leaf = 0, max_levels = 0;
+    for (int j = 0; j < ntraj; j++) {
+        const NsmInstance& d = h->inst[inst[j]].desc;
+        max_leaf = std::max(max_leaf, d.leaf_stride);
+        max_levels = std::max(max_levels, d.levels);
+    }
+    launch_nsm_init(h->d_trajs, h->d_insts, ntraj, max_leaf, max_levels, d_u0, st);
+    launches += 2 + max_levels;
+    // output buffers
+    const int nout = (int)h->output_steps.size();
+    std::vector<long long> count_off(ntraj), mom_off(ninst);
+    long long ctot = 0, mtot = 0;
+    for (int j = 0; j < ntraj; j++) {
+        count_off[j] = ctot;
+        ctot += (long long)nout * h->inst[inst[j]].N * h->inst[inst[j]].S;
+    }
+    for (int i = 0; i < ninst; i++) {
+        mom_off[i] = mtot;
+        mtot += (long long)nout * h->inst[i].N * h->inst[i].S;
+    }
+    int32_t* d_counts = nullptr;
+    long long* d_mom = nullptr;
+    long long *d_coff = nullptr, *d_moff = nullptr;
+    auto dmalloc = [&](void** p, size_t b) -> int {
+        cudaError_t e = cudaMalloc(p, b);
+        if (e != cudaSuccess) return spg_set_cuda_error(h, e, "cudaMalloc outputs", __FILE__, __LINE__);
+        tmp.push_back(*p);
+        return SP_OK;
+    };
+    const bool want_counts = a->want_counts && out && out->counts;
+    const bool want_mom = a->want_moments && out && out->moments;
+    if (want_counts) {
+        if (a->buffers_on_device) d_counts = out->counts;
+        else if ((rc = dmalloc((void**)&d_counts, sizeof(int32_t) * ctot))) { cleanup(); return rc; }
+        if ((rc = dmalloc((void**)&d_coff, sizeof(long long) * ntraj))) { cleanup(); return rc; }
+        cudaMemcpyAsync(d_coff, count_off.data(), sizeof(long long) * ntraj, cudaMemcpyHostToDevice, st);
+    }
+    if (want_mom) {
+        if (a->buffers_on_device) d_mom = (long long*)out->moments;
+        else if ((rc = dmalloc((void**)&d_mom, sizeof(long long) * 2 * mtot))) { cleanup(); return rc; }
+        if ((rc = dmalloc((void**)&d_moff, sizeof(long long) * ninst))) { cleanup(); return rc; }
+        cudaMemcpyAsync(d_moff, mom_off.data(), sizeof(long long) * ninst, cudaMemcpyHostToDevice, st);
+        cudaMemsetAsync(d_mom, 0, sizeof(long long) * 2 * mtot, st);
+    }
+    const bool ref = a->selection == SP_SELECT_REFERENCE;
+    const long long budget = h->opt.event_budget > 0 ? h->opt.event_budget : (1ll << 62);
+    const long long max_ns = 2000000000ll;
+    int result = SP_OK;
+    for (int k = 0; k < nout && result == SP_OK; k++) {
+        const int target = h->output_steps[k];
+        if (target > 0) {
+            for (int attempt = 0;; attempt++) {
+                launch_nsm_advance(ref, h->d_trajs, h->d_insts, ntraj, target, h->dt, budget, max_ns,
+                                   h->d_work, h->num_sms, st);
+                launches++;
+                cudaError_t e = cudaGetLastError();
+                if (e != cudaSuccess) { cleanup(); return spg_set_cuda_error(h, e, "nsm_advance", __FILE__, __LINE__); }
+                e = cudaMemcpyAsync(h->h_trajs.data(), h->d_trajs, sizeof(NsmTraj) * ntraj,
+                                    cudaMemcpyDeviceToHost, st);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+                if (e != cudaSuccess) { cleanup(); return spg_set_cuda_error(h, e, "nsm_advance sync", __FILE__, __LINE__); }
+                bool again = false;
+                for (int j = 0; j < ntraj; j++) {
+                    NsmTraj& T = h->h_trajs[j];
+                    if (T.status == SP_TRAJ_BUDGET_EXHAUSTED) {
+                        T.status = SP_TRAJ_OK;
+                        again = true;
+                    } else if (T.status != SP_TRAJ_OK) {
+                        result = SP_E_TRAJECTORY;
+                    }
+                }
+                if (result != SP_OK) break;
+                if (a->timeout_s > 0) {
+                    const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - wall0).count();
+                    if (el > a->timeout_s) { result = SP_E_TIMEOUT; break; }
+                }
+                if (!again) break;
+                // resume: statuses were reset on the host copy
+                cudaMemcpyAsync(h->d_trajs, h->h_trajs.data(), sizeof(NsmTraj) * ntraj,
+                                cudaMemcpyHostToDevice, st);
+            }
+        }
+        if (result != SP_OK) break;
+        if (want_counts || want_mom) {
+            launch_nsm_snapshot(h->d_trajs, h->d_insts, ntraj, want_counts ? d_counts : nullptr,
+                                d_coff, want_mom ? d_mom : nullptr, d_moff, k, st);
+            launches++;
+        }
+    }
+    cudaEventRecord(h->e1, st);
+    if (result == SP_OK || result == SP_E_TRAJECTORY) {
+        if (want_counts && !a->buffers_on_device)
+            cudaMemcpyAsync(out->counts, d_counts, sizeof(int32_t) * ctot, cudaMemcpyDeviceToHost, st);
+        if (want_mom && !a->buffers_on_device)
+            cudaMemcpyAsync(out->moments, d_mom, sizeof(long long) * 2 * mtot, cudaMemcpyDeviceToHost, st);
+    }
+    cudaMemcpyAsync(h->h_trajs.data(), h->d_trajs, sizeof(NsmTraj) * ntraj, cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    cleanup();
+    if (e != cudaSuccess) return spg_set_cuda_error(h, e, "sp_run", __FILE__, __LINE__);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, h->e0, h->e1);
+    h->last_ms = ms;
+    h->last_launches = launches;
+    if (out && out->event_counts)
+        for (int j = 0; j < ntraj; j++) {
+            out->event_counts[2 * j] = h->h_trajs[j].nrx;
+            out->event_counts[2 * j + 1] = h->h_trajs[j].ndf;
+        }
+    if (result == SP_E_TRAJECTORY) {
+        for (int j = 0; j < ntraj; j++)
+            if (h->h_trajs[j].status != SP_TRAJ_OK) {
+                char b[256];
+                snprintf(b, sizeof b, "trajectory %d stopped with status %d at voxel %d (t=%g)", j,
+                         h->h_trajs[j].status, h->h_trajs[j].err_voxel, h->h_trajs[j].t_last);
+                h->err = b;
+                break;
+            }
+    } else if (result == SP_E_TIMEOUT) {
+        h->err = "sp_run: timeout";
+    }
+    return result;
+}
+
+int sp_status(sp_handle* h, int32_t traj, sp_traj_status* st) {
+    if (!h || !st) return SP_E_INVALID;
+    if (traj < 0 || traj >= (int)h->h_trajs.size()) return fail(h, SP_E_INVALID, "trajectory out of range");
+    const NsmTraj& T = h->h_trajs[traj];
+    st->code = T.status;
+    st->voxel = T.err_voxel;
+    st->time = T.t_last;
+    st->events = T.nrx + T.ndf;
+    return SP_OK;
+}
+
+const char* sp_last_error(sp_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+void sp_destroy(sp_handle* h) {
+    if (!h) return;
+    cudaSetDevice(h->device);
+    if (h->st) cudaStreamSynchronize(h->st);
+    for (Instance& I : h->inst)
+        if (I.sdpd) sdpd_destroy(I.sdpd);
+    for (void* p : h->allocs) cudaFree(p);
+    if (h->traj_mem) cudaFree(h->traj_mem);
+    if (h->e0) cudaEventDestroy(h->e0);
+    if (h->e1) cudaEventDestroy(h->e1);
+    if (h->st) cudaStreamDestroy(h->st);
+    delete h;
+}
+
+int sp_get_neighbors(sp_handle* h, int32_t inst, int32_t kmax, int32_t* count, int32_t* idx,
+                     double* dist, double* dWdr, double* Dij) {
+    if (!h || inst < 0 || inst >= (int)h->inst.size() || !count || !idx) return SP_E_INVALID;
+    Instance& I = h->inst[inst];
+    SP_CUDA_TRY(cudaSetDevice(h->device));
+    const int N = I.N;
+    int K = I.K;
+    const int *d_cnt = I.nbr_cnt, *d_idx = I.nbr_idx;
+    const double *d_dist = I.nbr_dist, *d_dw = I.nbr_dwdr, *d_dij = I.nbr_dij;
+    if (!I.is_static) return sdpd_copy_neighbors(I.sdpd, kmax, count, idx, dist, dWdr, Dij, &h->err);
+    std::vector<int> c(N), ix((size_t)N * K);
+    std::vector<double> d1((size_t)N * K), d2((size_t)N * K), d3((size_t)N * K);
+    SP_CUDA_TRY(cudaMemcpy(c.data(), d_cnt, sizeof(int) * N, cudaMemcpyDeviceToHost));
+    SP_CUDA_TRY(cudaMemcpy(ix.data(), d_idx, sizeof(int) * N * (size_t)K, cudaMemcpyDeviceToHost));
+    if (d_dist) SP_CUDA_TRY(cudaMemcpy(d1.data(), d_dist, sizeof(double) * N * (size_t)K, cudaMemcpyDeviceToHost));
+    if (d_dw) SP_CUDA_TRY(cudaMemcpy(d2.data(), d_dw, sizeof(double) * N * (size_t)K, cudaMemcpyDeviceToHost));
+    if (d_dij) SP_CUDA_TRY(cudaMemcpy(d3.data(), d_dij, sizeof(double) * N * (size_t)K, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < N; i++) {
+        if (c[i] > kmax) return fail(h, SP_E_INVALID, "kmax smaller than a neighbour count");
+        count[i] = c[i];
+        for (int k = 0; k < c[i]; k++) {
+            const size_t s = (size_t)i * K + k, o = (size_t)i * kmax + k;
+            idx[o] = ix[s];
+            if (dist) dist[o] = d1[s];
+            if (dWdr) dWdr[o] = d2[s];
+            if (Dij) Dij[o] = d3[s];
+        }
+    }
+    return SP_OK;
+}
+
+int sp_get_ddiag(sp_handle* h, int32_t inst, double* ddiag) {
+    if (!h || inst < 0 || inst >= (int)h->inst.size() || !ddiag) return SP_E_INVALID;
+    Instance& I = h->inst[inst];
+    if (!I.ddiag) return fail(h, SP_E_INVALID, "instance has no diffusion tables");
+    SP_CUDA_TRY(cudaMemcpy(ddiag, I.ddiag, sizeof(double) * (size_t)I.N * I.S, cudaMemcpyDeviceToHost));
+    return SP_OK;
+}
+
+int sp_get_particles(sp_handle* h, int32_t inst, double* x, double* v, double* rho) {
+    if (!h || inst < 0 || inst >= (int)h->inst.size()) return SP_E_INVALID;
+    Instance& I = h->inst[inst];
+    SP_CUDA_TRY(cudaSetDevice(h->device));
+    if (I.sdpd) {
+        return sdpd_get_state(I.sdpd, x, v, rho, &h->err);
+    }
+    if (x) SP_CUDA_TRY(cudaMemcpy(x, I.x, sizeof(double) * 3 * I.N, cudaMemcpyDeviceToHost));
+    if (v) std::memset(v, 0, sizeof(double) * 3 * I.N);
+    if (rho) SP_CUDA_TRY(cudaMemcpy(rho, I.rho, sizeof(double) * I.N, cudaMemcpyDeviceToHost));
+    return SP_OK;
+}
+
+int sp_sdpd_advance(sp_handle* h, int32_t inst, int32_t nsteps) {
+    if (!h || inst < 0 || inst >= (int)h->inst.size() || nsteps < 0) return SP_E_INVALID;
+    Instance& I = h->inst[inst];
+    if (!I.sdpd) return fail(h, SP_E_INVALID, "instance is a static domain");
+    SP_CUDA_TRY(cudaSetDevice(h->device));
+    double ms = 0;
+    long long launches = 0;
+    int rc = sdpd_advance(I.sdpd, nsteps, &ms, &launches, &h->err);
+    h->last_ms = ms;
+    h->last_launches = launches;
+    return rc;
+}
+
+int sp_last_timing(sp_handle* h, double* ms, int64_t* launches) {
+    if (!h) return SP_E_INVALID;
+    if (ms) *ms = h->last_ms;
+    if (launches) *launches = h->last_launches;
+    return SP_OK;
+}
+
+}  // extern "C"

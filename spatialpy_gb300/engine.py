@@ -1,0 +1,191 @@
+"""Thin host layer over libspgpu's C ABI (include/spgpu.h).
+
+:class:`Engine` owns one ``sp_handle`` (device copies of one or more model
+instances) and runs ensembles through ``sp_run``.  Every call goes through
+ctypes into the CUDA library; there is no host computation of the hot path
+and no fallback: a missing library or device raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from .abi import SpOptions, SpOutputs, SpRunArgs, SpTrajStatus, ptr
+
+
+class EngineError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"[{code}] {message}")
+        self.code = code
+
+
+class Engine:
+    """Device-resident model instances and their ensemble runs.
+
+    Parameters
+    ----------
+    scenarios : Scenario or list of Scenario
+        Model instances (a list runs heterogeneous batches in one launch).
+    sdpd_precision : "f32" or "f64"
+    nsm_variant : 0 autotuned, 1 sequential warp, 2 speculative batch warp
+    """
+
+    def __init__(self, scenarios, device: int = 0, sdpd_precision: str = "f32",
+                 nsm_variant: int = 0, event_budget: int = 0, lib_path: str | None = None):
+        self.lib = abi.load_library(lib_path)
+        if not isinstance(scenarios, (list, tuple)):
+            scenarios = [scenarios]
+        self.scenarios = list(scenarios)
+        self._structs = (abi.SpScenario * len(scenarios))()
+        for i, sc in enumerate(scenarios):
+            self._structs[i] = abi.scenario_struct(sc)
+        opt = SpOptions()
+        opt.device = device
+        opt.sdpd_precision = abi.SP_PREC_F64 if sdpd_precision == "f64" else abi.SP_PREC_F32
+        opt.nsm_variant = nsm_variant
+        opt.event_budget = event_budget
+        self._h = C.c_void_p()
+        rc = self.lib.sp_create(self._structs, len(scenarios), C.byref(opt), C.byref(self._h))
+        if rc != abi.SP_OK:
+            msg = self.error()
+            self.close()
+            raise EngineError(rc, msg)
+
+    # -- lifecycle ---------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self.lib.sp_destroy(self._h)
+        self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def error(self) -> str:
+        m = self.lib.sp_last_error(self._h)
+        return m.decode() if m else ""
+
+    def _check(self, rc: int):
+        if rc != abi.SP_OK:
+            raise EngineError(rc, self.error())
+
+    # -- runs ----------------------------------------------------------------
+    def run(self, seeds, instance=None, selection: int = abi.SP_SELECT_EXACT,
+            want_counts: bool = True, want_moments: bool = False, u0=None,
+            timeout: float | None = None):
+        """Run one trajectory per seed.
+
+        Returns a dict with ``counts`` (list per trajectory of [T,N,S] int32
+        arrays) when ``want_counts``, ``moments`` (list per instance of
+        [T,N,S,2] int64 sums of x and x^2) when ``want_moments``, ``events``
+        ([ntraj,2] reaction/diffusion counts) and ``status`` codes.
+        """
+        seeds = np.ascontiguousarray(seeds, dtype=np.uint64).reshape(-1)
+        nt = seeds.shape[0]
+        inst = None
+        if instance is not None:
+            inst = np.ascontiguousarray(instance, dtype=np.int32).reshape(nt)
+        u0s = []
+        for i, sc in enumerate(self.scenarios):
+            a = sc.u0 if u0 is None else (u0[i] if isinstance(u0, (list, tuple)) else u0)
+            u0s.append(None if a is None else np.ascontiguousarray(a, dtype=np.uint32))
+        u0p = (C.POINTER(C.c_uint32) * len(u0s))()
+        for i, a in enumerate(u0s):
+            u0p[i] = ptr(a, C.c_uint32)
+        args = SpRunArgs()
+        args.num_trajectories = nt
+        args.selection = selection
+        args.instance = ptr(inst, C.c_int32)
+        args.seeds = ptr(seeds, C.c_uint64)
+        args.u0 = u0p
+        args.buffers_on_device = 0
+        args.want_counts = int(want_counts)
+        args.want_moments = int(want_moments)
+        args.timeout_s = float(timeout or 0.0)
+        T = [len(sc.output_steps) for sc in self.scenarios]
+        idx = np.zeros(nt, np.int64) if inst is None else inst.astype(np.int64)
+        sizes = [T[i] * self.scenarios[i].num_particles * self.scenarios[i].num_species
+                 for i in idx]
+        counts = np.zeros(int(sum(sizes)) if want_counts else 0, np.int32)
+        msizes = [T[i] * sc.num_particles * sc.num_species for i, sc in enumerate(self.scenarios)]
+        moments = np.zeros(2 * int(sum(msizes)) if want_moments else 0, np.int64)
+        events = np.zeros((nt, 2), np.int64)
+        out = SpOutputs()
+        out.counts = ptr(counts if want_counts else None, C.c_int32)
+        out.moments = ptr(moments if want_moments else None, C.c_int64)
+        out.event_counts = ptr(events, C.c_int64)
+        rc = self.lib.sp_run(self._h, C.byref(args), C.byref(out))
+        status = np.array([self.status(j)["code"] for j in range(nt)], np.int32)
+        if rc not in (abi.SP_OK, abi.SP_E_TRAJECTORY, abi.SP_E_TIMEOUT):
+            raise EngineError(rc, self.error())
+        res = {"events": events, "status": status, "rc": rc}
+        if rc != abi.SP_OK:
+            res["error"] = self.error()
+        if want_counts:
+            parts, o = [], 0
+            for j, i in enumerate(idx):
+                sc = self.scenarios[i]
+                parts.append(counts[o:o + sizes[j]].reshape(T[i], sc.num_particles, sc.num_species))
+                o += sizes[j]
+            res["counts"] = parts
+        if want_moments:
+            parts, o = [], 0
+            for i, sc in enumerate(self.scenarios):
+                parts.append(moments[2 * o:2 * (o + msizes[i])].reshape(
+                    T[i], sc.num_particles, sc.num_species, 2))
+                o += msizes[i]
+            res["moments"] = parts
+        return res
+
+    def status(self, j: int) -> dict:
+        st = SpTrajStatus()
+        self._check(self.lib.sp_status(self._h, j, C.byref(st)))
+        return {"code": st.code, "voxel": st.voxel, "time": st.time, "events": st.events}
+
+    def last_timing(self):
+        ms = C.c_double()
+        n = C.c_int64()
+        self._check(self.lib.sp_last_timing(self._h, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    # -- inspection ------------------------------------------------------------
+    def neighbors(self, inst: int = 0, kmax: int = 64):
+        sc = self.scenarios[inst]
+        n = sc.num_particles
+        cnt = np.zeros(n, np.int32)
+        idx = np.full((n, kmax), -1, np.int32)
+        dist = np.zeros((n, kmax))
+        dw = np.zeros((n, kmax))
+        dij = np.zeros((n, kmax))
+        self._check(self.lib.sp_get_neighbors(self._h, inst, kmax, ptr(cnt, C.c_int32),
+                                              ptr(idx, C.c_int32), ptr(dist, C.c_double),
+                                              ptr(dw, C.c_double), ptr(dij, C.c_double)))
+        return cnt, idx, dist, dw, dij
+
+    def ddiag(self, inst: int = 0):
+        sc = self.scenarios[inst]
+        out = np.zeros((sc.num_particles, sc.num_species))
+        self._check(self.lib.sp_get_ddiag(self._h, inst, ptr(out, C.c_double)))
+        return out
+
+    def particles(self, inst: int = 0):
+        n = self.scenarios[inst].num_particles
+        x = np.zeros((n, 3))
+        v = np.zeros((n, 3))
+        rho = np.zeros(n)
+        self._check(self.lib.sp_get_particles(self._h, inst, ptr(x, C.c_double),
+                                              ptr(v, C.c_double), ptr(rho, C.c_double)))
+        return x, v, rho
+
+    def sdpd_advance(self, nsteps: int, inst: int = 0):
+        self._check(self.lib.sp_sdpd_advance(self._h, inst, nsteps))

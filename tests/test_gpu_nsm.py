@@ -1,0 +1,211 @@
+"""GPU NSM parity: libspgpu trajectories against the oracle and the reference.
+
+The GPU engine and the oracle (oracle/sp_oracle.c) consume the same Philox
+streams and round every double-precision operation alike, so counts must be
+identical event for event (bit-exact integer parity).  Against the compiled
+reference engine (mt19937_64 streams) parity is statistical: ensemble means
+and variances inside 99% bands of the reference ensembles in tests/golden/.
+"""
+import numpy as np
+import pytest
+
+from spatialpy_gb300 import abi
+from spatialpy_gb300 import scenario as S
+
+from .conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+
+def _engine(scs, **kw):
+    from spatialpy_gb300.engine import Engine
+    return Engine(scs, **kw)
+
+
+def _dimer_model():
+    sc = S.config_birth_death_2d(n=6, count=40, t_end=4.0, num_points=5)
+    rate, kind, reac, allowed, jcN, irN, prN = S.mass_action(
+        ["A", "B"],
+        [(5.0, {}, {"A": 1}, None), (0.02, {"A": 2}, {"B": 1}, None),
+         (0.3, {"B": 1}, {"A": 2}, None), (0.05, {"A": 1, "B": 1}, {}, None)], 1)
+    u0 = np.zeros((sc.num_particles, 2), np.uint32)
+    u0[:, 0] = sc.u0[:, 0]
+    u0[3, 1] = 7
+    return sc.copy(species=["A", "B"], rxn_rate=rate, rxn_kind=kind, rxn_reactants=reac,
+                   rxn_allowed=allowed, jcN=jcN, irN=irN, prN=prN,
+                   diffusion=np.array([[0.2], [0.05]]), u0=u0, name="dimer")
+
+
+def _restricted_model():
+    """Two types; species A may not enter type 2; birth only in type 2."""
+    sc = S.config_rdme_3d(n=5, nA=60, nB=60, t_end=5.0, num_points=6, dims=2)
+    diff = sc.diffusion.copy()
+    diff[0, 1] = 0.0          # D(A, type 2) = 0: no A moves into type 2
+    return sc.copy(diffusion=diff, name="restricted")
+
+
+CASES = {
+    "birth_death": lambda: S.config_birth_death_2d(),
+    "rdme3d_6": lambda: S.config_rdme_3d(n=6, nA=300, nB=300, t_end=10.0, num_points=11),
+    "rdme2d_12": lambda: S.config_rdme_3d(n=12, nA=200, nB=150, t_end=6.0, num_points=7, dims=2),
+    "dimer": _dimer_model,
+    "restricted": _restricted_model,
+}
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+@pytest.mark.parametrize("selection", [abi.SP_SELECT_EXACT, abi.SP_SELECT_REFERENCE])
+def test_trajectories_bitexact_vs_oracle(oracle_lib, case, selection):
+    sc = CASES[case]()
+    seeds = np.arange(1000, 1008, dtype=np.uint64) * 7919
+    with _engine(sc) as eng:
+        res = eng.run(seeds, selection=selection)
+    assert res["rc"] == abi.SP_OK, res.get("error")
+    for j, s in enumerate(seeds):
+        out, ev, st = oracle_lib.nsm_trajectory(sc, int(s), selection)
+        assert st == 0
+        np.testing.assert_array_equal(res["counts"][j], out, err_msg=f"{case} traj {j}")
+        np.testing.assert_array_equal(res["events"][j], ev)
+
+
+def test_uneven_batch_bitexact(oracle_lib):
+    scs = [S.config_birth_death_2d(n=7, count=30),
+           S.config_birth_death_2d(n=23, count=300, k_birth=3.0),
+           S.config_birth_death_2d(n=2, count=5, D=1.0)]
+    inst = np.array([1, 0, 2, 1, 1, 0, 2, 2], np.int32)
+    seeds = np.arange(50, 58, dtype=np.uint64)
+    with _engine(scs) as eng:
+        res = eng.run(seeds, instance=inst, want_moments=True)
+    assert res["rc"] == abi.SP_OK, res.get("error")
+    for j, s in enumerate(seeds):
+        out, ev, _ = oracle_lib.nsm_trajectory(scs[inst[j]], int(s), 0)
+        np.testing.assert_array_equal(res["counts"][j], out)
+        np.testing.assert_array_equal(res["events"][j], ev)
+    # moments are exact integer sums over each instance's trajectories
+    for i in range(3):
+        xs = np.array([res["counts"][j] for j in range(len(seeds)) if inst[j] == i], np.int64)
+        np.testing.assert_array_equal(res["moments"][i][..., 0], xs.sum(0))
+        np.testing.assert_array_equal(res["moments"][i][..., 1], (xs * xs).sum(0))
+
+
+def test_rerun_is_bit_identical():
+    sc = S.config_rdme_3d(n=6, nA=300, nB=300, t_end=10.0, num_points=11)
+    seeds = np.arange(32, dtype=np.uint64) + 99
+    with _engine(sc) as eng:
+        a = eng.run(seeds)
+        b = eng.run(seeds)
+    for x, y in zip(a["counts"], b["counts"]):
+        np.testing.assert_array_equal(x, y)
+    np.testing.assert_array_equal(a["events"], b["events"])
+
+
+def test_output0_is_u0_and_empty_domain():
+    sc = S.config_birth_death_2d(count=0, k_birth=0.0)
+    with _engine(sc) as eng:
+        res = eng.run(np.arange(4, dtype=np.uint64))
+    for c in res["counts"]:
+        assert c.sum() == 0
+    assert res["events"].sum() == 0
+    sc = S.config_birth_death_2d()
+    with _engine(sc) as eng:
+        res = eng.run(np.arange(4, dtype=np.uint64))
+    for c in res["counts"]:
+        np.testing.assert_array_equal(c[0], sc.u0)      # test_solver.py:127-131
+
+
+def test_neighbors_bitexact(oracle_lib):
+    fx = golden("neighbors.npz")
+    keys = sorted({k.split("/")[0] for k in fx.files})
+    for key in keys:
+        base = S.config_birth_death_2d()
+        x = fx[f"{key}/x"]
+        n = x.shape[0]
+        sc = base.copy(x=x, type=np.ones(n), mass=fx[f"{key}/mass"], rho=fx[f"{key}/rho"],
+                       nu=np.ones(n), fixed=np.ones(n), u0=np.zeros((n, 1)),
+                       dimension=int(fx[f"{key}/dim"]), h=float(fx[f"{key}/h"]))
+        kmax = 256
+        with _engine(sc) as eng:
+            cnt, idx, dist, dw, dij = eng.neighbors(0, kmax)
+        o = oracle_lib.neighbors(sc, kmax)
+        # identical lists and order against the oracle
+        np.testing.assert_array_equal(cnt, o[0], err_msg=key)
+        for a, b in zip((idx, dist, dw, dij), o[1:]):
+            np.testing.assert_array_equal(a, b, err_msg=key)
+        # identical sets and values against the reference engine
+        np.testing.assert_array_equal(cnt, fx[f"{key}/count"], err_msg=key)
+        for i in range(n):
+            c = cnt[i]
+            order = np.argsort(idx[i, :c], kind="stable")
+            np.testing.assert_array_equal(idx[i, :c][order], fx[f"{key}/idx"][i, :c])
+            for a, name in ((dist, "dist"), (dw, "dWdr"), (dij, "Dij")):
+                np.testing.assert_array_equal(a[i, :c][order], fx[f"{key}/{name}"][i, :c],
+                                              err_msg=f"{key}:{name}:{i}")
+
+
+def test_ddiag_bitexact(oracle_lib):
+    for sc in (_restricted_model(), S.config_rdme_3d(n=6, nA=10, nB=10)):
+        with _engine(sc) as eng:
+            dd = eng.ddiag(0)
+        cnt, idx, dist, dw, dij = oracle_lib.neighbors(sc, 64)
+        odd, _ = oracle_lib.diffusion_tables(sc, cnt, idx, dij)
+        np.testing.assert_array_equal(dd, odd)
+
+
+def test_birth_death_exact_statistics():
+    """1,000 trajectories: the total follows the immigration-death law
+    mean(t) = 100 (k_b V / k_d with V = 1 and 100 initial molecules) and
+    var(t) = 100 e^{-t/10}(1-e^{-t/10}) + 100 (1-e^{-t/10})."""
+    sc = S.config_birth_death_2d()
+    n = 1000
+    with _engine(sc) as eng:
+        tot = np.array([c.sum(axis=(1, 2)) for c in
+                        eng.run(np.arange(n, dtype=np.uint64) + 20260101)["counts"]])
+    t = sc.output_times()
+    q = np.exp(-0.1 * t)
+    var = 100 * q * (1 - q) + 100 * (1 - q)
+    mean = tot.mean(0)
+    # 99% joint bands over the 10 outputs (99.9% each)
+    band = 3.29 * np.sqrt(np.maximum(var, 1e-9) / n)
+    assert np.all(np.abs(mean[1:] - 100.0) <= band[1:] + 1e-12), (mean, band)
+    sv = tot.var(0, ddof=1)
+    vband = 3.29 * var * np.sqrt(2.0 / (n - 1))
+    assert np.all(np.abs(sv[1:] - var[1:]) <= vband[1:]), (sv, var)
+
+
+def test_reference_mode_matches_reference_ensemble():
+    """The reused-uniform selection of the stock engine (F1) reproduced on the
+    GPU: per-output mean/variance of the total inside 99.9% bands of the
+    1,000-trajectory reference ensemble, per-voxel means at t=10 in 99% bands
+    for >= 95% of voxels."""
+    g = golden("nsm_birth_death.npz")
+    sc = S.config_birth_death_2d()
+    n = 1000
+    with _engine(sc) as eng:
+        res = eng.run(np.arange(n, dtype=np.uint64) + 7, selection=abi.SP_SELECT_REFERENCE)
+    cnt = np.array(res["counts"])[..., 0]                     # [n, T, N]
+    tot = cnt.sum(-1)
+    for tag, sel_tot in (("stock", tot),):
+        gm, gv, gn = g[f"{tag}/total_mean"], g[f"{tag}/total_var"], int(g[f"{tag}/ntraj"])
+        m, v = sel_tot.mean(0), sel_tot.var(0, ddof=1)
+        se = np.sqrt(v / n + gv / gn)
+        assert np.all(np.abs(m - gm)[1:] <= 3.29 * se[1:]), (m, gm)
+        vm = g[f"{tag}/voxel_mean_last"]
+        vv = g[f"{tag}/voxel_var_last"]
+        mv = cnt[:, -1].mean(0)
+        vse = np.sqrt(cnt[:, -1].var(0, ddof=1) / n + vv / gn)
+        frac = np.mean(np.abs(mv - vm) <= 2.576 * vse + 1e-12)
+        assert frac >= 0.95, frac
+
+
+def test_exact_mode_matches_rescaled_reference_ensemble():
+    g = golden("nsm_rdme_small.npz")
+    sc = S.config_rdme_3d(n=6, nA=300, nB=300, t_end=10.0, num_points=11)
+    n = 400
+    for tag, sel in (("exact", abi.SP_SELECT_EXACT), ("stock", abi.SP_SELECT_REFERENCE)):
+        with _engine(sc) as eng:
+            res = eng.run(np.arange(n, dtype=np.uint64) + 31337, selection=sel)
+        tot = np.array([c.sum(axis=1) for c in res["counts"]])      # [n, T, S]
+        m, v = tot.mean(0), tot.var(0, ddof=1)
+        gm, gv, gn = g[f"{tag}/total_mean"], g[f"{tag}/total_var"], int(g[f"{tag}/ntraj"])
+        se = np.sqrt(v / n + gv / gn)
+        assert np.all(np.abs(m - gm)[1:] <= 3.29 * se[1:] + 1e-9), (tag, m, gm)

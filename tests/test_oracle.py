@@ -1,0 +1,162 @@
+"""CPU tests: the oracle restatement pinned against the reference engine's
+golden vectors (tests/golden/, generated by make_golden.py from the compiled
+reference) and against known answers."""
+import math
+
+import numpy as np
+import pytest
+
+from spatialpy_gb300 import abi
+from spatialpy_gb300 import scenario as S
+
+from .conftest import golden
+
+
+def test_philox_known_answers(oracle_lib):
+    """Random123 known-answer vectors for Philox4x32-10."""
+    kat = [
+        ((0, 0, 0, 0), (0, 0), (0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8)),
+        ((0xffffffff,) * 4, (0xffffffff,) * 2, (0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd)),
+        ((0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344), (0xa4093822, 0x299f31d0),
+         (0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1)),
+    ]
+    for ctr, key, want in kat:
+        assert tuple(int(v) for v in oracle_lib.philox(ctr, key)) == want
+
+
+def test_host_philox_matches_oracle(oracle_lib):
+    from spatialpy_gb300.philox import philox4x32_10
+    rng = np.random.default_rng(3)
+    for _ in range(50):
+        c = rng.integers(0, 2 ** 32, 4, dtype=np.uint64)
+        k = rng.integers(0, 2 ** 32, 2, dtype=np.uint64)
+        assert tuple(philox4x32_10(*c, *k)) == tuple(int(v) for v in oracle_lib.philox(c, k))
+
+
+def test_neglog_accuracy(oracle_lib):
+    for u in np.concatenate([np.geomspace(2 ** -33, 1 - 1e-12, 400), [0.5, 0.25, 0.7071]]):
+        a = oracle_lib.neglog(float(u))
+        b = -math.log(float(u))
+        assert abs(a - b) <= 4e-16 * max(1.0, abs(b)), (u, a, b)
+
+
+def test_neighbors_match_reference_golden(oracle_lib):
+    fx = golden("neighbors.npz")
+    keys = sorted({k.split("/")[0] for k in fx.files})
+    assert len(keys) >= 6
+    for key in keys:
+        base = S.config_birth_death_2d()
+        x = fx[f"{key}/x"]
+        n = x.shape[0]
+        sc = base.copy(x=x, type=np.ones(n), mass=fx[f"{key}/mass"], rho=fx[f"{key}/rho"],
+                       nu=np.ones(n), fixed=np.ones(n), u0=np.zeros((n, 1)),
+                       dimension=int(fx[f"{key}/dim"]), h=float(fx[f"{key}/h"]))
+        cnt, idx, dist, dw, dij = oracle_lib.neighbors(sc, 256)
+        np.testing.assert_array_equal(cnt, fx[f"{key}/count"], err_msg=key)
+        for i in range(n):
+            c = cnt[i]
+            # ascending distance, ties by index
+            assert np.all(np.diff(dist[i, :c]) >= 0)
+            order = np.argsort(idx[i, :c], kind="stable")
+            np.testing.assert_array_equal(idx[i, :c][order], fx[f"{key}/idx"][i, :c])
+            for a, name in ((dist, "dist"), (dw, "dWdr"), (dij, "Dij")):
+                np.testing.assert_array_equal(a[i, :c][order], fx[f"{key}/{name}"][i, :c],
+                                              err_msg=f"{key}:{name}")
+
+
+def _ensemble(sc, n, seed0, selection):
+    out, ev, st, _ = oracle_lib_cached().nsm_ensemble(
+        sc, np.arange(seed0, seed0 + n, dtype=np.uint64), selection)
+    assert st.max() == 0
+    return out, ev
+
+
+_OL = None
+
+
+def oracle_lib_cached():
+    global _OL
+    if _OL is None:
+        import oracle
+        oracle.build()
+        _OL = oracle
+    return _OL
+
+
+def test_birth_death_exact_law(oracle_lib):
+    """exact selection: immigration-death law mean 100, var 100(1-q)+100q(1-q)."""
+    sc = S.config_birth_death_2d()
+    n = 1000
+    out, _ = _ensemble(sc, n, 20260101, abi.SP_SELECT_EXACT)
+    tot = out.sum(axis=(2, 3))
+    q = np.exp(-0.1 * sc.output_times())
+    var = 100 * q * (1 - q) + 100 * (1 - q)
+    assert np.all(np.abs(tot.mean(0)[1:] - 100) <= 3.29 * np.sqrt(var[1:] / n))
+    sv = tot.var(0, ddof=1)
+    assert np.all(np.abs(sv[1:] - var[1:]) <= 3.29 * var[1:] * np.sqrt(2 / (n - 1)))
+
+
+@pytest.mark.parametrize("tag,selection", [("stock", abi.SP_SELECT_REFERENCE),
+                                           ("exact", abi.SP_SELECT_EXACT)])
+def test_birth_death_vs_reference_ensembles(oracle_lib, tag, selection):
+    """Oracle ensembles inside 99.9% bands of the reference's 1,000-trajectory
+    ensembles (stock engine / rescaled-selection engine), per output."""
+    g = golden("nsm_birth_death.npz")
+    sc = S.config_birth_death_2d()
+    n = 1000
+    out, ev = _ensemble(sc, n, 5, selection)
+    tot = out.sum(axis=(2, 3))
+    gm, gv, gn = g[f"{tag}/total_mean"], g[f"{tag}/total_var"], int(g[f"{tag}/ntraj"])
+    se = np.sqrt(tot.var(0, ddof=1) / n + gv / gn)
+    assert np.all(np.abs(tot.mean(0) - gm)[1:] <= 3.29 * se[1:]), (tot.mean(0), gm)
+    # mean event counts (reaction, diffusion) within 5%
+    np.testing.assert_allclose(ev.mean(0), g[f"{tag}/events_mean"], rtol=0.05)
+    # per-voxel means at the last output
+    vm, vv = g[f"{tag}/voxel_mean_last"], g[f"{tag}/voxel_var_last"]
+    last = out[:, -1, :, 0]
+    vse = np.sqrt(last.var(0, ddof=1) / n + vv / gn)
+    assert np.mean(np.abs(last.mean(0) - vm) <= 2.576 * vse) >= 0.95
+
+
+@pytest.mark.parametrize("tag,selection", [("stock", abi.SP_SELECT_REFERENCE),
+                                           ("exact", abi.SP_SELECT_EXACT)])
+def test_rdme_vs_reference_ensembles(oracle_lib, tag, selection):
+    g = golden("nsm_rdme_small.npz")
+    sc = S.config_rdme_3d(n=6, nA=300, nB=300, t_end=10.0, num_points=11)
+    n = 400
+    out, ev = _ensemble(sc, n, 31337, selection)
+    tot = out.sum(axis=2)
+    gm, gv, gn = g[f"{tag}/total_mean"], g[f"{tag}/total_var"], int(g[f"{tag}/ntraj"])
+    se = np.sqrt(tot.var(0, ddof=1) / n + gv / gn)
+    assert np.all(np.abs(tot.mean(0) - gm)[1:] <= 3.29 * se[1:] + 1e-9)
+    np.testing.assert_allclose(ev.mean(0), g[f"{tag}/events_mean"], rtol=0.05)
+
+
+def test_sdpd_oracle_vs_reference_golden(oracle_lib):
+    """FP64 SDPD oracle with the reference's neighbour semantics (moved query
+    points against start-of-step points; Gauss-Seidel density reads) against
+    the compiled engine, and the Jacobi variant used by the GPU."""
+    g = golden("sdpd_small.npz")
+    sc = S.config_dam_break(spacing_div=int(g["spacing_div"]), num_steps=41)
+    for mode in (3, 2):
+        st = oracle_lib.SdpdState(sc)
+        done = 0
+        for nsteps in (1, 5, 21, 41):
+            oracle_lib.sdpd(sc, st, nsteps - done, "f64", mode)
+            done = nsteps
+            rx, rv, rr = g[f"{nsteps}/x"], g[f"{nsteps}/v"], g[f"{nsteps}/rho"]
+            assert np.abs(st.x - rx).max() <= 1e-12
+            assert np.linalg.norm(st.v - rv) <= 1e-9 * max(np.linalg.norm(rv), 1e-30)
+            assert np.abs(st.rho - rr).max() <= 1e-12
+
+
+def test_sdpd_f32_close_to_f64_without_self_pairs(oracle_lib):
+    """Plain FP32 positions track FP64 when neighbour points are not the
+    start-of-step points (mode 0); with them, whether a moved particle meets
+    its own start-of-step point depends on displacements below FP32
+    resolution, which the GPU FP32 path resolves with FP64 anchors."""
+    sc = S.config_dam_break(spacing_div=8, num_steps=41)
+    a = oracle_lib.sdpd(sc, oracle_lib.SdpdState(sc), 41, "f64", 0)
+    b = oracle_lib.sdpd(sc, oracle_lib.SdpdState(sc), 41, "f32", 0)
+    assert np.abs(a.x - b.x).max() <= 1e-6
+    assert np.linalg.norm(a.v - b.v) <= 1e-3 * np.linalg.norm(a.v)
