@@ -1,0 +1,351 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 SpatialPy engine: SSA events/s of the NSM event loop.
+
+Workload (one GPU): the static 3-D RDME model, 40^3 = 64,000 lattice voxels on
+the unit cube, species A, B, C with D = (1e-2, 1e-2, 1e-3), A+B->C (k=1e-3),
+C->A+B (0.1), 0->A on x < 0.1 (5), C->0 (0.05), 10,000 A and 10,000 B
+scattered once, 256 trajectories, exact selection.  One bench step = one
+output interval (t -> t+1) of all 256 trajectories.  The trajectory state
+(256 x 1.3 MB) is larger than L2, so no flush is needed between steps.
+
+  value  device time of K steps (CUDA events on the engine stream), inputs
+         resident in HBM
+  e2e    the same metric through the C ABI with host buffers: sp_run of K
+         intervals from host u0 to host moment sums (H2D + D2H inside)
+  --impl reference  the CPU restatement of the reference algorithm (oracle)
+         on all host cores, same workload and metric
+
+Prints one JSON line on rank 0.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SSA events/s"
+UNIT = "events/s"
+NTRAJ = 256
+SEED0 = 20260101
+# algorithmic bytes per event, 3-D RDME (S=3, R=4, K=32): two voxels x
+# (counts r+w 8S, rates r+w 16R, totals + queue key/time 24) + the selected
+# neighbour row (K x (4 B index + 4 B weight)) for a diffusion event; one
+# voxel + 4 |G_r| dependency entries for a reaction event
+B_DIFF = 2 * (8 * 3 + 16 * 4 + 24) + 8 * 32      # 480
+B_RXN = 8 * 3 + 16 * 4 + 24 + 4 * 5              # 132
+
+
+def workload(intervals: int | None = None):
+    from spatialpy_gb300 import scenario as S
+    if intervals is None:
+        return S.config_rdme_3d()
+    return S.config_rdme_3d(t_end=float(intervals), num_points=intervals + 1)
+
+
+def config_dict(sc):
+    return {
+        "workload": "static 3-D RDME, 40^3 voxels, A+B<->C, 0->A (x<0.1), C->0; "
+                    "256 trajectories, exact selection; step = one output interval",
+        "voxels": int(sc.num_particles), "species": 3, "reactions": 4,
+        "trajectories": NTRAJ, "interval": 1.0,
+        "l2": "no flush: trajectory state 256 x 1.3 MB > L2",
+    }
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int = 0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, x: float) -> float:
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(pg, x: float) -> float:
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t.item())
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(threads: int | None = None, ntraj: int = 64, intervals: int = 2):
+    """The oracle (CPU restatement of the reference algorithm) on the host
+    cores, a bounded sample of the same workload."""
+    import oracle
+    oracle.build()
+    sc = workload(intervals)
+    threads = threads or os.cpu_count() or 1
+    seeds = np.arange(SEED0, SEED0 + ntraj, dtype=np.uint64)
+    t0 = time.perf_counter()
+    _, ev, st, used = oracle.nsm_ensemble(sc, seeds, 0, threads, want_counts=False)
+    dt = time.perf_counter() - t0
+    return {"value": float(ev.sum() / dt), "unit": UNIT, "cores": int(used), "kind": "port",
+            "sample": f"{ntraj} trajectories x {intervals} output intervals "
+                      f"({int(ev.sum())} events, {dt:.1f} s)"}
+
+
+def run_reference(args, rank, pg):
+    """--impl reference: the CPU restatement of the reference on all cores."""
+    if rank != 0:
+        return None
+    import oracle
+    oracle.build()
+    threads = os.cpu_count() or 1
+    seeds = np.arange(SEED0, SEED0 + NTRAJ, dtype=np.uint64)
+    # warm-up: W intervals of a few trajectories
+    oracle.nsm_ensemble(workload(max(1, args.warmup)), seeds[:threads], 0, threads,
+                        want_counts=False)
+    sc = workload(args.steps)
+    t0 = time.perf_counter()
+    _, ev, st, used = oracle.nsm_ensemble(sc, seeds, 0, threads, want_counts=False)
+    dt = time.perf_counter() - t0
+    value = float(ev.sum() / dt)
+    sample = f"{NTRAJ} trajectories x {args.steps} output intervals ({int(ev.sum())} events)"
+    return {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int32 counts, f32 propensities, f64 clock", "data": "synthetic",
+        "config": config_dict(sc),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": int(used), "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+B_SDPD = 200   # algorithmic bytes per particle-step (state r/w, cell key, D_ij row)
+
+
+def run_sdpd(args):
+    """SDPD particle-steps/s on the dam break: 49,152 fluid + 35,544 wall
+    particles, h = 1.5 s, dt = 1e-4, FP32 state (device time of 200 steps
+    after 20 warm-up steps)."""
+    from spatialpy_gb300 import scenario as S
+    from spatialpy_gb300.engine import Engine
+    sc = S.config_dam_break()
+    with Engine(sc, sdpd_precision="f32") as eng:
+        eng.sdpd_advance(20)
+        eng.sdpd_advance(args.sdpd_steps)
+        ms, launches = eng.last_timing()
+    ps = sc.num_particles * args.sdpd_steps / (ms / 1e3)
+    peak, src = measured_peak()
+    achieved = B_SDPD * ps / 1e9
+    return {"metric": "SDPD particle-steps/s", "value": ps, "unit": "particle-steps/s",
+            "steps": args.sdpd_steps, "warmup": 20, "ms_per_step": ms / args.sdpd_steps,
+            "dtype": "f32", "gpu_launches": int(launches),
+            "config": {"workload": "SDPD dam break 1x0.5x0.5, 48x32x32 fluid + 3 wall layers "
+                                   "(84,696 particles), Lucy kernel h=1.5s, dt=1e-4, FP32",
+                       "particles": int(sc.num_particles)},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_source": src,
+                         "bytes_per_particle_step": B_SDPD}}
+
+
+def run_ours(args, world, rank, local, pg):
+    import __graft_entry__ as g
+    g.build()
+    from spatialpy_gb300.engine import Engine
+
+    sc = workload()
+    seeds = np.arange(SEED0, SEED0 + NTRAJ, dtype=np.uint64) + np.uint64(rank * 1000003)
+    eng = Engine(sc, device=0)
+    eng.start(seeds, want_moments=False)
+    eng.advance(args.warmup)
+
+    def events_now():
+        return sum(eng.status(j)["events"] for j in range(NTRAJ))
+
+    def split_now():
+        return eng._run["events"]
+
+    e0 = events_now()
+    barrier(pg)
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        eng.advance(args.steps)
+        wall = time.perf_counter() - t0
+    prof = eng.profile()
+    e1 = events_now()
+    res = eng.finish()
+    events = e1 - e0
+    dev_s = max_over_ranks(pg, prof["total_ms"] / 1e3)
+    total_events = sum_over_ranks(pg, float(events))
+    value = total_events / dev_s
+    # reaction / diffusion split over the whole run -> bytes per timed event
+    ev = res["events"].sum(axis=0).astype(np.float64)
+    frac_rxn = ev[0] / max(1.0, ev.sum())
+    bytes_per_event = frac_rxn * B_RXN + (1 - frac_rxn) * B_DIFF
+    peak, peak_src = measured_peak()
+    achieved = events * bytes_per_event / (prof["kernel_ms"] / 1e3) / 1e9
+    eng.close()
+
+    # e2e: sp_run through the C ABI with host buffers, K intervals
+    sc_e2e = workload(args.steps)
+    with Engine(sc_e2e, device=0) as e2:
+        barrier(pg)
+        t0 = time.perf_counter()
+        r2 = e2.run(seeds, want_counts=False, want_moments=True)
+        e2e_s = max_over_ranks(pg, time.perf_counter() - t0)
+    e2e_events = sum_over_ranks(pg, float(r2["events"].sum()))
+    h2d = sc_e2e.u0.nbytes + seeds.nbytes
+    d2h = r2["moments"][0].nbytes + r2["events"].nbytes
+
+    sdpd = run_sdpd(args) if not args.skip_sdpd else None
+
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int32 counts, f32 propensities, f64 clock", "data": "synthetic",
+        "config": config_dict(sc),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": args.traffic,
+                     "kernel": "nsm_advance_small", "peak_source": peak_src,
+                     "bytes_per_event": bytes_per_event},
+        "e2e": {"value": e2e_events / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps},
+        "gpu_launches": int(prof["launches"]),
+        "clocks": clk.summary(),
+        "wall_s": wall,
+    }
+    if sdpd is not None:
+        out["secondary"] = sdpd
+    if rank == 0 and not args.skip_cpu:
+        out["cpu_baseline"] = cpu_baseline()
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-sdpd", action="store_true")
+    ap.add_argument("--sdpd-steps", type=int, default=200)
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="DRAM bytes per event of the event-loop kernel from an ncu capture")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="small case for ncu: the bench workload over two 0.05 intervals")
+    args = ap.parse_args()
+    if args.profile_case:
+        import __graft_entry__ as g
+        g.build()
+        from spatialpy_gb300 import scenario as S
+        from spatialpy_gb300.engine import Engine
+        sc = S.config_rdme_3d(t_end=0.1, num_points=3, dt=0.05)
+        with Engine(sc) as eng:
+            r = eng.run(np.arange(SEED0, SEED0 + NTRAJ, dtype=np.uint64), want_counts=False)
+            print("profile case events", int(r["events"].sum()), eng.profile())
+        return
+    world, rank, local, pg = dist_setup()
+    if args.impl == "reference":
+        out = run_reference(args, rank, pg)
+    else:
+        out = run_ours(args, world, rank, local, pg)
+    if rank == 0 and out is not None:
+        print(json.dumps(out), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

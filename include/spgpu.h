@@ -120,7 +120,8 @@ typedef struct sp_scenario {
 typedef struct sp_options {
     int32_t device;               /* CUDA device ordinal */
     int32_t sdpd_precision;       /* SP_PREC_F32 (default) or SP_PREC_F64 */
-    int32_t nsm_variant;          /* 0 = autotuned, 1 = sequential warp, 2 = speculative batch warp */
+    int32_t nsm_variant;          /* 0 = chosen per run (register-resident network when
+                                     S <= 8 and R <= 16), 1 = generic warp kernel */
     int32_t reserved;
     int64_t event_budget;         /* max events per trajectory per launch (0 = default) */
 } sp_options;
@@ -171,6 +172,18 @@ int         sp_abi_version(void);
 int         sp_create(const sp_scenario* scenarios, int32_t num_scenarios,
                       const sp_options* opts, sp_handle** out);
 int         sp_run(sp_handle* h, const sp_run_args* args, sp_outputs* out);
+/*
+ * sp_run in three parts, for callers that advance an ensemble output by
+ * output (progress reporting, timing): sp_run_start uploads u0, builds the
+ * event queues and writes the outputs at step 0; sp_run_continue advances
+ * through the next `num_outputs` outputs that need events; sp_run_finish
+ * copies results to host buffers and fills out->event_counts.  sp_run =
+ * start + continue(all) + finish.  Same replacement as sp_run
+ * (solver.py:547-605, simulate_threads.cpp:232-281).
+ */
+int         sp_run_start(sp_handle* h, const sp_run_args* args, sp_outputs* out);
+int         sp_run_continue(sp_handle* h, int32_t num_outputs);
+int         sp_run_finish(sp_handle* h);
 int         sp_status(sp_handle* h, int32_t trajectory, sp_traj_status* st);
 const char* sp_last_error(sp_handle* h);
 void        sp_destroy(sp_handle* h);
@@ -193,9 +206,20 @@ int sp_get_particles(sp_handle* h, int32_t inst, double* x, double* v, double* r
 /* Advance the SDPD flow of instance inst by nsteps without species
    (take_step substeps 0-2, simulate.cpp:33-48), from its current state. */
 int sp_sdpd_advance(sp_handle* h, int32_t inst, int32_t nsteps);
-/* Device time in milliseconds of the last sp_run / sp_sdpd_advance
-   (CUDA events on the handle's stream) and kernel launches issued by it. */
+/* Device time in milliseconds of the last sp_run / sp_run_continue /
+   sp_sdpd_advance (CUDA events on the handle's stream) and kernel launches
+   issued by it. */
 int sp_last_timing(sp_handle* h, double* ms, int64_t* launches);
+
+/* Same, split by kernel: kernel_ms = the NSM event-loop (or SDPD step)
+   kernels alone, timed by CUDA events around each launch. */
+typedef struct sp_profile {
+    double total_ms;
+    double kernel_ms;
+    int64_t launches;
+    int64_t reserved;
+} sp_profile;
+int sp_last_profile(sp_handle* h, sp_profile* p);
 
 #ifdef __cplusplus
 }

@@ -56,8 +56,10 @@ def lib():
                                     _p(C.c_int32), _p(C.c_int32), _p(C.c_double),
                                     _p(C.c_double), _p(C.c_double)]
         L.spo_diffusion_tables.argtypes = [_p(SpScenario), C.c_int32, _p(C.c_int32),
-                                           _p(C.c_int32), _p(C.c_double), _p(C.c_double),
-                                           _p(C.c_double)]
+                                           _p(C.c_int32), _p(C.c_double), _p(C.c_float),
+                                           _p(C.c_float)]
+        L.spo_neglog_f.argtypes = [C.c_float]
+        L.spo_neglog_f.restype = C.c_float
         L.spo_nsm_trajectory.argtypes = [_p(SpScenario), _p(C.c_uint32), C.c_uint64, C.c_int32,
                                          _p(C.c_int32), _p(C.c_int64)]
         L.spo_nsm_ensemble.argtypes = [_p(SpScenario), _p(C.c_uint32), _p(C.c_uint64),
@@ -86,6 +88,10 @@ def neglog(u: float) -> float:
     return lib().spo_neglog(float(u))
 
 
+def neglog_f(u: float) -> float:
+    return lib().spo_neglog_f(float(u))
+
+
 def neighbors(sc, kmax: int = 64, xq=None, xt=None):
     """(count, idx, dist, dWdr, Dij) with the reference predicate and order."""
     n = sc.num_particles
@@ -108,11 +114,11 @@ def neighbors(sc, kmax: int = 64, xq=None, xt=None):
 def diffusion_tables(sc, cnt, idx, dij):
     kmax = idx.shape[1]
     s = scenario_struct(sc)
-    dd = np.zeros((sc.num_particles, sc.num_species))
-    cdf = np.zeros((sc.num_particles, sc.num_species, kmax))
+    dd = np.zeros((sc.num_particles, sc.num_species), np.float32)
+    cdf = np.zeros((sc.num_particles, sc.num_species, kmax), np.float32)
     lib().spo_diffusion_tables(C.byref(s), kmax, _ptr(cnt, C.c_int32), _ptr(idx, C.c_int32),
-                               _ptr(np.ascontiguousarray(dij), C.c_double), _ptr(dd, C.c_double),
-                               _ptr(cdf, C.c_double))
+                               _ptr(np.ascontiguousarray(dij), C.c_double), _ptr(dd, C.c_float),
+                               _ptr(cdf, C.c_float))
     return dd, cdf
 
 

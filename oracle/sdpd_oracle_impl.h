@@ -10,7 +10,7 @@
 
 static int SPO_NB(int n, int dim, const REAL *xq, const REAL *xt, REAL h, const REAL *mass,
                   const REAL *rho, int kmax, int32_t *count, int32_t *idx, REAL *dist,
-                  REAL *dwdr) {
+                  REAL *dwdr, const REAL *self_d2) {
     /* same predicate and order as spo_neighbors, in REAL arithmetic */
     REAL lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
     for (int d = 0; d < dim; d++) {
@@ -69,6 +69,8 @@ static int SPO_NB(int n, int dim, const REAL *xq, const REAL *xt, REAL h, const 
                             d2 = d2 + tt * tt;
                             if (d2 > sq) break;
                         }
+                        if (self_d2 && j == i) { d2 = self_d2[i]; d = dim; }
+                        if (d2 > sq) continue;
                         if (d < dim || d2 == 0) continue;
                         if (SQRT(d2) > h) continue;
                         if (m >= kmax) { rc = -1; break; }
@@ -113,6 +115,7 @@ int SPO_FN(const sp_scenario *sc, int32_t step0, int32_t nsteps, int32_t mode, i
     REAL *rho = (REAL *)malloc(sizeof(REAL) * n), *orho = (REAL *)malloc(sizeof(REAL) * n);
     REAL *Frho = (REAL *)malloc(sizeof(REAL) * n), *m = (REAL *)malloc(sizeof(REAL) * n);
     REAL *nu = (REAL *)malloc(sizeof(REAL) * n), *nrm = (REAL *)malloc(sizeof(REAL) * 3 * n);
+    REAL *sd2 = (REAL *)malloc(sizeof(REAL) * n);
     REAL *ndist = (REAL *)malloc(sizeof(REAL) * (size_t)n * kmax);
     REAL *ndw = (REAL *)malloc(sizeof(REAL) * (size_t)n * kmax);
     int32_t *nidx = (int32_t *)malloc(sizeof(int32_t) * (size_t)n * kmax);
@@ -152,7 +155,25 @@ int SPO_FN(const sp_scenario *sc, int32_t step0, int32_t nsteps, int32_t mode, i
            start-of-step points (mode 2) or against moved points */
         const REAL *q = (step == 0) ? xt : x;
         const REAL *tp = (step == 0 || (mode & 2)) ? xt : x;
-        if (SPO_NB(n, dim, q, tp, h, m, rho, kmax, ncnt, nidx, ndist, ndw)) { rc = -1; break; }
+        /* mode 4: a moved particle meets its own start-of-step point at the
+           predictor displacement |dt vt| (resolved even where positions
+           round to the same value) */
+        const int selfmode = (mode & 4) && (mode & 2) && step != 0;
+        if (selfmode)
+            for (int i = 0; i < n; i++) {
+                REAL s2 = 0;
+                if (!sc->fixed[i] && !sc->static_domain) {
+                    const REAL a = dt * vt[3 * i], b = dt * vt[3 * i + 1], c = dt * vt[3 * i + 2];
+                    s2 = a * a;
+                    if (dim > 1) s2 = s2 + b * b;
+                    if (dim > 2) s2 = s2 + c * c;
+                }
+                sd2[i] = s2;
+            }
+        if (SPO_NB(n, dim, q, tp, h, m, rho, kmax, ncnt, nidx, ndist, ndw, selfmode ? sd2 : NULL)) {
+            rc = -1;
+            break;
+        }
         /* substep 1: pairwiseForce (model.cpp:39-191) */
         for (int i = 0; i < n; i++) {
             const REAL Pi = P0 * (rho[i] / rho0 - K_(1.0));
@@ -269,7 +290,7 @@ int SPO_FN(const sp_scenario *sc, int32_t step0, int32_t nsteps, int32_t mode, i
     for (int i = 0; i < n; i++) { rho_io[i] = rho[i]; Frho_io[i] = Frho[i]; }
     if (nbr_count) memcpy(nbr_count, ncnt, sizeof(int32_t) * n);
     free(x); free(xt); free(v); free(vt); free(F); free(Fbp); free(rho); free(orho); free(Frho);
-    free(m); free(nu); free(nrm); free(ndist); free(ndw); free(nidx); free(ncnt);
+    free(m); free(nu); free(nrm); free(ndist); free(ndw); free(nidx); free(ncnt); free(sd2);
     return rc;
 }
 #undef K_

@@ -76,6 +76,41 @@ double spo_neglog(double u) {
 }
 
 /* ------------------------------------------------------------------------
+ * Single-precision variate helpers used by the NSM event loop.
+ *   u24(r):  (r >> 8) 2^-24 + 2^-25, exact, in (0,1)      (selection uniforms)
+ *   u32f(r): ((float)r + 0.5f) 2^-32, in (0,1]              (exponential draws)
+ *   neglog_f: the construction of spo_neglog in float, series to w^5 and a
+ *   ln 2 head with the low 9 mantissa bits cleared.
+ * ------------------------------------------------------------------------ */
+static inline float u24(uint32_t r) {
+    return (float)(r >> 8) * (1.0f / 16777216.0f) + (1.0f / 33554432.0f);
+}
+static inline float u32f(uint32_t r) { return ((float)r + 0.5f) * (1.0f / 4294967296.0f); }
+
+float spo_neglog_f(float u) {
+    uint32_t b;
+    memcpy(&b, &u, 4);
+    int e = (int)((b >> 23) & 0xff) - 127;
+    b = (b & 0x007fffffu) | 0x3f800000u;
+    float m;
+    memcpy(&m, &b, 4);
+    if (m > 1.41421356f) { m = m * 0.5f; e = e + 1; }
+    const float z = (m - 1.0f) / (m + 1.0f);
+    const float w = z * z;
+    float p = 1.0f / 11.0f;
+    p = p * w + 1.0f / 9.0f;
+    p = p * w + 1.0f / 7.0f;
+    p = p * w + 1.0f / 5.0f;
+    p = p * w + 1.0f / 3.0f;
+    p = p * w + 1.0f;
+    const float logm = (2.0f * z) * p;
+    const float ln2_hi = 0.693145751953125f;     /* 0x3f317200 */
+    const float ln2_lo = 1.428606765330187e-06f; /* 0x35bfbe8e */
+    const float ed = (float)e;
+    return -(ed * ln2_hi + (ed * ln2_lo + logm));
+}
+
+/* ------------------------------------------------------------------------
  * Neighbour search with the ANN fixed-radius predicate.
  * ------------------------------------------------------------------------ */
 typedef struct { double d2; int32_t j; } cand_t;
@@ -193,7 +228,10 @@ int spo_neighbors(int32_t n, int32_t dim, const double *xq, const double *xt, do
 }
 
 void spo_diffusion_tables(const sp_scenario *sc, int32_t kmax, const int32_t *count,
-                          const int32_t *idx, const double *dij, double *ddiag, double *cdf) {
+                          const int32_t *idx, const double *dij, float *ddiag, float *cdf) {
+    /* Ddiag[s] = sum_k D(s,type_j) D_ij in list order (simulate_rdme.cpp:142-148),
+       accumulated in double and rounded to float; cdf holds the rounded
+       running sums scanned by the destination choice (:359-367). */
     const int S = sc->num_species, T = sc->num_types;
     for (int i = 0; i < sc->num_particles; i++) {
         for (int s = 0; s < S; s++) {
@@ -201,22 +239,23 @@ void spo_diffusion_tables(const sp_scenario *sc, int32_t kmax, const int32_t *co
             for (int k = 0; k < count[i]; k++) {
                 const int j = idx[(size_t)i * kmax + k];
                 const double dc = sc->diffusion[s * T + (sc->type[j] - 1)];
-                acc = acc + dc * dij[(size_t)i * kmax + k];     /* simulate_rdme.cpp:146-147 */
-                if (cdf) cdf[((size_t)i * S + s) * kmax + k] = acc;
+                acc = acc + dc * dij[(size_t)i * kmax + k];
+                if (cdf) cdf[((size_t)i * S + s) * kmax + k] = (float)acc;
             }
-            ddiag[(size_t)i * S + s] = acc;
+            ddiag[(size_t)i * S + s] = (float)acc;
         }
     }
 }
 
 /* ------------------------------------------------------------------------
- * NSM
+ * NSM.  Propensities, selection scans and exponential variates in single
+ * precision; event times (the clock) in double.
  * ------------------------------------------------------------------------ */
 typedef struct {
     const sp_scenario *sc;
     int N, S, R, T, K;
     int32_t *cnt, *idx;
-    double *cdf, *ddiag, *vol;
+    float *cdf, *ddiag, *vol, *ivol, *rate;
 } nsm_tables_t;
 
 static int tables_build(const sp_scenario *sc, nsm_tables_t *t) {
@@ -236,8 +275,8 @@ static int tables_build(const sp_scenario *sc, nsm_tables_t *t) {
                                t->cnt, t->idx, NULL, NULL, dij);
         if (rc == 0) {
             t->K = K;
-            t->cdf = (double *)malloc(sizeof(double) * (size_t)N * t->S * K);
-            t->ddiag = (double *)malloc(sizeof(double) * (size_t)N * t->S);
+            t->cdf = (float *)malloc(sizeof(float) * (size_t)N * t->S * K);
+            t->ddiag = (float *)malloc(sizeof(float) * (size_t)N * t->S);
             spo_diffusion_tables(sc, K, t->cnt, t->idx, dij, t->ddiag, t->cdf);
             free(dij);
             break;
@@ -247,34 +286,48 @@ static int tables_build(const sp_scenario *sc, nsm_tables_t *t) {
         free(dij);
         K *= 2;
     }
-    t->vol = (double *)malloc(sizeof(double) * N);
-    for (int i = 0; i < N; i++) t->vol[i] = sc->mass[i] / sc->rho[i];
+    t->vol = (float *)malloc(sizeof(float) * N);
+    t->ivol = (float *)malloc(sizeof(float) * N);
+    for (int i = 0; i < N; i++) {
+        t->vol[i] = (float)(sc->mass[i] / sc->rho[i]);
+        t->ivol[i] = (float)(sc->rho[i] / sc->mass[i]);
+    }
+    t->rate = (float *)malloc(sizeof(float) * (t->R > 0 ? t->R : 1));
+    for (int r = 0; r < t->R; r++) t->rate[r] = (float)sc->rxn_rate[r];
     return 0;
 }
 
 static void tables_free(nsm_tables_t *t) {
-    free(t->cnt); free(t->idx); free(t->cdf); free(t->ddiag); free(t->vol);
+    free(t->cnt); free(t->idx); free(t->cdf); free(t->ddiag); free(t->vol); free(t->ivol);
+    free(t->rate);
 }
 
-/* mass-action propensity, operator order of the generated code */
-static inline double prop(const sp_scenario *sc, int r, const int32_t *x, double vol, int type) {
-    if (sc->rxn_allowed && !sc->rxn_allowed[(size_t)r * (sc->num_types + 1) + type]) return 0.0;
-    const double k = sc->rxn_rate[r];
+/* mass-action propensity in float, the generated code's operator order with
+   the second-order division by vol replaced by a product with 1/vol
+   (rounded from double): k*vol, k*A, (k*A*B)*(1/vol), (k*A*(A-1))*(1/vol) */
+static inline float prop(const nsm_tables_t *t, int r, const int32_t *x, float vol, float ivol,
+                         int type) {
+    const sp_scenario *sc = t->sc;
+    if (sc->rxn_allowed && !sc->rxn_allowed[(size_t)r * (sc->num_types + 1) + type]) return 0.0f;
+    const float k = t->rate[r];
     const int a = sc->rxn_reactants[2 * r], b = sc->rxn_reactants[2 * r + 1];
     switch (sc->rxn_kind[r]) {
         case SP_RXN_ZERO: return k * vol;
-        case SP_RXN_FIRST: return k * (double)x[a];
-        case SP_RXN_SECOND: return k * (double)x[a] * (double)x[b] / vol;
-        default: return k * (double)x[a] * (double)(x[a] - 1) / vol;
+        case SP_RXN_FIRST: return k * (float)x[a];
+        case SP_RXN_SECOND: return k * (float)x[a] * (float)x[b] * ivol;
+        default: return k * (float)x[a] * (float)(x[a] - 1) * ivol;
     }
 }
 
-static inline void voxel_rates(const nsm_tables_t *t, int v, const int32_t *x, double vol,
-                               double *srr, double *sdr) {
-    double a = 0.0;
-    for (int r = 0; r < t->R; r++) a = a + prop(t->sc, r, x, vol, t->sc->type[v]);
-    double d = 0.0;
-    for (int s = 0; s < t->S; s++) d = d + t->ddiag[(size_t)v * t->S + s] * (double)x[s];
+/* the voxel whose volume a rate uses: its own, or (reference selection, for
+   a diffusion destination) the source voxel's */
+static inline void voxel_rates(const nsm_tables_t *t, int v, const int32_t *x, int volv,
+                               float *srr, float *sdr) {
+    const float vol = t->vol[volv], ivol = t->ivol[volv];
+    float a = 0.0f;
+    for (int r = 0; r < t->R; r++) a = a + prop(t, r, x, vol, ivol, t->sc->type[v]);
+    float d = 0.0f;
+    for (int s = 0; s < t->S; s++) d = d + t->ddiag[(size_t)v * t->S + s] * (float)x[s];
     *srr = a;
     *sdr = d;
 }
@@ -308,8 +361,10 @@ static void hfix(heap_t *h, int v) {
     }
 }
 
-static inline double draw_time(double t, double e, double a) {
-    return a > 0.0 ? t + e / a : HUGE_VAL;
+/* next firing time t + E/a (NRMConstant_v5.cpp:57, :98): the waiting time in
+   float, the clock in double */
+static inline double draw_time(double t, float e, float a) {
+    return a > 0.0f ? t + (double)(e / a) : HUGE_VAL;
 }
 
 static int nsm_run(const nsm_tables_t *t, const uint32_t *u0, uint64_t seed, int selection,
@@ -326,11 +381,11 @@ static int nsm_run(const nsm_tables_t *t, const uint32_t *u0, uint64_t seed, int
     const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
     /* queue build at t0 = 0 (NRMConstant_v5::build, :52-71): stream 1 */
     for (int v = 0; v < N; v++) {
-        double srr, sdr;
-        voxel_rates(t, v, x + (size_t)v * S, t->vol[v], &srr, &sdr);
+        float srr, sdr;
+        voxel_rates(t, v, x + (size_t)v * S, v, &srr, &sdr);
         uint32_t ctr[4] = {(uint32_t)v, 0u, 1u, 0u}, r[4];
         spo_philox4x32_10(ctr, key, r);
-        h.tau[v] = draw_time(0.0, spo_neglog(u01(r[0])), srr + sdr);
+        h.tau[v] = draw_time(0.0, spo_neglog_f(u32f(r[0])), srr + sdr);
         h.heap[v] = v;
         h.pos[v] = v;
     }
@@ -364,20 +419,20 @@ static int nsm_run(const nsm_tables_t *t, const uint32_t *u0, uint64_t seed, int
             uint32_t ctr[4] = {(uint32_t)evn, (uint32_t)(evn >> 32), 0u, 0u}, r[4];
             spo_philox4x32_10(ctr, key, r);
             evn++;
-            const double ua = u01(r[0]), ub = u01(r[1]);
-            const double e0 = spo_neglog(u01(r[2])), e1 = spo_neglog(u01(r[3]));
+            const float ua = u24(r[0]), ub = u24(r[1]);
+            const float e0 = spo_neglog_f(u32f(r[2])), e1 = spo_neglog_f(u32f(r[3]));
             int32_t *xv = x + (size_t)v * S;
-            double srr, sdr;
-            voxel_rates(t, v, xv, t->vol[v], &srr, &sdr);
-            const double tot = srr + sdr;
-            if (ua <= srr / tot) {                               /* :255 */
-                const double target = selection == SP_SELECT_EXACT ? ua * tot : ua * srr;
-                double cum = 0.0;
+            float srr, sdr;
+            voxel_rates(t, v, xv, v, &srr, &sdr);
+            const float tot = srr + sdr;
+            if (ua * tot <= srr) {                               /* :255 rand1 <= srrate/totrate */
+                const float target = selection == SP_SELECT_EXACT ? ua * tot : ua * srr;
+                float cum = 0.0f;
                 int re = -1, last = -1;
                 for (int q = 0; q < t->R; q++) {
-                    const double a = prop(sc, q, xv, t->vol[v], sc->type[v]);
+                    const float a = prop(t, q, xv, t->vol[v], t->ivol[v], sc->type[v]);
                     cum = cum + a;
-                    if (a > 0.0) {
+                    if (a > 0.0f) {
                         last = q;
                         if (target <= cum) { re = q; break; }
                     }
@@ -389,28 +444,28 @@ static int nsm_run(const nsm_tables_t *t, const uint32_t *u0, uint64_t seed, int
                     if (xv[sc->irN[i]] < 0) status = SP_TRAJ_NEG_COUNT;
                 }
                 if (status) break;
-                voxel_rates(t, v, xv, t->vol[v], &srr, &sdr);
+                voxel_rates(t, v, xv, v, &srr, &sdr);
                 h.tau[v] = draw_time(tt, e0, srr + sdr);
                 hfix(&h, v);
                 nrx++;
             } else {
-                const double target = selection == SP_SELECT_EXACT ? ua * tot - srr : ua * sdr;
-                double cum = 0.0;
+                const float target = selection == SP_SELECT_EXACT ? ua * tot - srr : ua * sdr;
+                float cum = 0.0f;
                 int sp = -1, last = -1;
                 for (int s = 0; s < S; s++) {                      /* :319-321 */
-                    const double wgt = t->ddiag[(size_t)v * S + s] * (double)xv[s];
+                    const float wgt = t->ddiag[(size_t)v * S + s] * (float)xv[s];
                     cum = cum + wgt;
-                    if (wgt > 0.0) {
+                    if (wgt > 0.0f) {
                         last = s;
                         if (target <= cum) { sp = s; break; }
                     }
                 }
                 if (sp < 0) sp = last;
                 if (sp < 0) { status = SP_TRAJ_SELECT_OVERFLOW; break; }
-                const double target2 = ub * t->ddiag[(size_t)v * S + sp];   /* :353-354 */
-                const double *c = t->cdf + ((size_t)v * S + sp) * K;
+                const float target2 = ub * t->ddiag[(size_t)v * S + sp];   /* :353-354 */
+                const float *c = t->cdf + ((size_t)v * S + sp) * K;
                 int k = -1, lastk = -1;
-                double prev = 0.0;
+                float prev = 0.0f;
                 for (int q = 0; q < t->cnt[v]; q++) {             /* :359-367 */
                     if (c[q] > prev) {
                         lastk = q;
@@ -424,13 +479,12 @@ static int nsm_run(const nsm_tables_t *t, const uint32_t *u0, uint64_t seed, int
                 int32_t *xw = x + (size_t)w * S;
                 xv[sp] -= 1;                                          /* :394-402 */
                 xw[sp] += 1;
-                voxel_rates(t, v, xv, t->vol[v], &srr, &sdr);
+                voxel_rates(t, v, xv, v, &srr, &sdr);
                 h.tau[v] = draw_time(tt, e0, srr + sdr);
                 hfix(&h, v);
                 /* the engine evaluates the destination's reactions with the
                    source voxel's volume (simulate_rdme.cpp:431-433) */
-                const double volw = selection == SP_SELECT_REFERENCE ? t->vol[v] : t->vol[w];
-                voxel_rates(t, w, xw, volw, &srr, &sdr);
+                voxel_rates(t, w, xw, selection == SP_SELECT_REFERENCE ? v : w, &srr, &sdr);
                 h.tau[w] = draw_time(tt, e1, srr + sdr);
                 hfix(&h, w);
                 ndf++;

@@ -6,7 +6,8 @@
  * NSM semantics follow nsm_core__take_step (src/simulate_rdme.cpp:211-472)
  * and the NRM queue contract (src/NRMConstant_v5.cpp): per-voxel next-event
  * times, fresh exponential draws for every voxel an event touches, events
- * in increasing time.  The random streams are Philox4x32-10 (Salmon et al.,
+ * in increasing time.  Propensities, selection scans and waiting times are
+ * single precision with a fixed operation order; the clock is double.  The random streams are Philox4x32-10 (Salmon et al.,
  * SC'11) keyed by the trajectory seed, so the GPU engine can be checked
  * against this file event for event; against the reference's own
  * mt19937_64 streams the comparison is statistical.
@@ -38,9 +39,12 @@ int spo_neighbors(int32_t n, int32_t dim, const double *xq, const double *xt, do
                   int32_t *idx, double *dist, double *dwdr, double *dij);
 
 /* Ddiag[i*S+s] and cumulative weights cdf[(i*S+s)*kmax + k] from the lists
- * (simulate_rdme.cpp:131-152 and the destination scan :353-367). */
+ * (simulate_rdme.cpp:131-152 and the destination scan :353-367), summed in
+ * double and rounded to float. */
 void spo_diffusion_tables(const sp_scenario *sc, int32_t kmax, const int32_t *count,
-                          const int32_t *idx, const double *dij, double *ddiag, double *cdf);
+                          const int32_t *idx, const double *dij, float *ddiag, float *cdf);
+/* single-precision -log(u), the variate of the NSM waiting times */
+float spo_neglog_f(float u);
 
 /*
  * Run one NSM trajectory on a static domain.
@@ -67,6 +71,8 @@ int spo_nsm_ensemble(const sp_scenario *sc, const uint32_t *u0, const uint64_t *
  *       order a single engine thread produces, model.cpp:284-288)
  *   2 = neighbour distances between moved query and start-of-step points (the
  *       kd-tree is built once per step, simulate_threads.cpp:80-108)
+ *   4 = with 2: a particle's distance to its own start-of-step point is the
+ *       predictor displacement |dt vt| (the FP32 engine's rule)
  * State arrays are [N*3] / [N] in double; nsteps engine steps from step0. */
 int spo_sdpd_f64(const sp_scenario *sc, int32_t step0, int32_t nsteps, int32_t mode, int32_t kmax,
                  double *x, double *v, double *vt, double *rho, double *F, double *Fbp,

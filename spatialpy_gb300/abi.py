@@ -105,6 +105,15 @@ class SpOutputs(C.Structure):
     ]
 
 
+class SpProfile(C.Structure):
+    _fields_ = [
+        ("total_ms", C.c_double),
+        ("kernel_ms", C.c_double),
+        ("launches", C.c_int64),
+        ("reserved", C.c_int64),
+    ]
+
+
 class SpTrajStatus(C.Structure):
     _fields_ = [
         ("code", C.c_int32),
@@ -116,9 +125,10 @@ class SpTrajStatus(C.Structure):
 
 #: every entry point declared in include/spgpu.h
 EXPORTED_SYMBOLS = (
-    "sp_abi_version", "sp_create", "sp_run", "sp_status", "sp_last_error",
-    "sp_destroy", "sp_get_neighbors", "sp_get_ddiag", "sp_get_particles",
-    "sp_sdpd_advance", "sp_last_timing",
+    "sp_abi_version", "sp_create", "sp_run", "sp_run_start", "sp_run_continue",
+    "sp_run_finish", "sp_status", "sp_last_error", "sp_destroy", "sp_get_neighbors",
+    "sp_get_ddiag", "sp_get_particles", "sp_sdpd_advance", "sp_last_timing",
+    "sp_last_profile",
 )
 
 
@@ -196,6 +206,14 @@ def load_library(path: str | None = None):
     lib.sp_create.restype = C.c_int
     lib.sp_run.argtypes = [C.c_void_p, _p(SpRunArgs), _p(SpOutputs)]
     lib.sp_run.restype = C.c_int
+    lib.sp_run_start.argtypes = [C.c_void_p, _p(SpRunArgs), _p(SpOutputs)]
+    lib.sp_run_start.restype = C.c_int
+    lib.sp_run_continue.argtypes = [C.c_void_p, C.c_int32]
+    lib.sp_run_continue.restype = C.c_int
+    lib.sp_run_finish.argtypes = [C.c_void_p]
+    lib.sp_run_finish.restype = C.c_int
+    lib.sp_last_profile.argtypes = [C.c_void_p, _p(SpProfile)]
+    lib.sp_last_profile.restype = C.c_int
     lib.sp_status.argtypes = [C.c_void_p, C.c_int32, _p(SpTrajStatus)]
     lib.sp_status.restype = C.c_int
     lib.sp_last_error.argtypes = [C.c_void_p]

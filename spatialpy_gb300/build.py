@@ -3,7 +3,8 @@
 ``python -m spatialpy_gb300.build`` compiles every translation unit of
 ``csrc/`` in parallel and links ``_build/libspgpu.so``.  The NSM and
 neighbour-search units are compiled with ``-fmad=false`` so their double
-precision arithmetic rounds exactly as written.
+precision arithmetic rounds exactly as written; the SDPD unit likewise, in
+both precisions, so it rounds like the CPU oracle.
 """
 from __future__ import annotations
 
@@ -22,7 +23,7 @@ UNITS = {
     "engine.cu": [],
     "nsm.cu": ["-fmad=false"],
     "neighbors.cu": ["-fmad=false"],
-    "sdpd.cu": [],
+    "sdpd.cu": ["-fmad=false"],
 }
 
 

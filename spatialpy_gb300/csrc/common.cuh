@@ -88,21 +88,64 @@ __host__ __device__ __forceinline__ double neglog(double u) {
     return -(ed * ln2_hi + (ed * ln2_lo + logm));
 }
 
+// Selection uniform in (0,1) from the top 24 bits, exact in float.
+__host__ __device__ __forceinline__ float u24(uint32_t r) {
+    return (float)(r >> 8) * (1.0f / 16777216.0f) + (1.0f / 33554432.0f);
+}
+// Uniform in (0,1] for exponential draws, full 32-bit resolution near 0.
+__host__ __device__ __forceinline__ float u32f(uint32_t r) {
+    return ((float)r + 0.5f) * (1.0f / 4294967296.0f);
+}
+
+// Single-precision -log(u): the construction of neglog() in float (series to
+// w^5, ln 2 head with 9 low mantissa bits cleared).  The NSM waiting times use
+// it; the CPU oracle evaluates the same operations in the same order.
+__host__ __device__ __forceinline__ float neglog_f(float u) {
+#ifdef __CUDA_ARCH__
+    unsigned b = __float_as_uint(u);
+#else
+    unsigned b;
+    __builtin_memcpy(&b, &u, 4);
+#endif
+    int e = (int)((b >> 23) & 0xff) - 127;
+    b = (b & 0x007fffffu) | 0x3f800000u;
+#ifdef __CUDA_ARCH__
+    float m = __uint_as_float(b);
+#else
+    float m;
+    __builtin_memcpy(&m, &b, 4);
+#endif
+    if (m > 1.41421356f) { m = m * 0.5f; e = e + 1; }
+    const float z = (m - 1.0f) / (m + 1.0f);
+    const float w = z * z;
+    float p = 1.0f / 11.0f;
+    p = p * w + 1.0f / 9.0f;
+    p = p * w + 1.0f / 7.0f;
+    p = p * w + 1.0f / 5.0f;
+    p = p * w + 1.0f / 3.0f;
+    p = p * w + 1.0f;
+    const float logm = (2.0f * z) * p;
+    const float ed = (float)e;
+    return -(ed * 0.693145751953125f + (ed * 1.428606765330187e-06f + logm));
+}
+
+// Event times are non-negative doubles or +inf; their IEEE bit patterns order
+// like the values, so the queue compares them as 64-bit integers.
+#define SP_INF_BITS 0x7ff0000000000000ll
+
 // (time, index) lexicographic order of the event queue
-__device__ __forceinline__ bool tless(double ta, int ia, double tb, int ib) {
+__device__ __forceinline__ bool kless(long long ta, int ia, long long tb, int ib) {
     return ta < tb || (ta == tb && ia < ib);
 }
 
-__device__ __forceinline__ void warp_argmin(double &t, int &i) {
+__device__ __forceinline__ void warp_argmin(long long& t, int& i) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        const double t2 = __shfl_xor_sync(SP_FULL, t, o);
+        const long long t2 = __shfl_xor_sync(SP_FULL, t, o);
         const int i2 = __shfl_xor_sync(SP_FULL, i, o);
-        if (tless(t2, i2, t, i)) { t = t2; i = i2; }
+        if (kless(t2, i2, t, i)) { t = t2; i = i2; }
     }
 }
-
-struct TreeNode { double t; int32_t i; int32_t pad; };
 
 constexpr int kMaxLevels = 8;
 
@@ -111,16 +154,17 @@ struct NsmInstance {
     int32_t N, S, R, T, K;            // voxels, species, reactions, types, neighbour stride
     int32_t levels;                   // tree levels above the leaves (root = level `levels`)
     int32_t level_size[kMaxLevels + 1];
-    int32_t level_off[kMaxLevels + 1];  // node offset of level l (l >= 1) in the node array
+    int32_t level_off[kMaxLevels + 1];  // node offset of level l (l >= 1) in the node arrays
     int32_t num_nodes;
     int32_t leaf_stride;              // padded leaf count (multiple of 32)
     const int32_t* type;              // [N]
-    const double* vol;                // [N]
+    const float* vol;                 // [N] mass/rho rounded to float
+    const float* ivol;                // [N] rho/mass rounded to float
     const int32_t* nbr_cnt;           // [N]
     const int32_t* nbr_idx;           // [N*K]
-    const double* cdf;                // [N*S*K]
-    const double* ddiag;              // [N*S]
-    const double* rate;               // [R]
+    const float* cdf;                 // [N*S*K] running sums of D(s,type_j) D_ij
+    const float* ddiag;               // [N*S]
+    const float* rate;                // [R] rate constants rounded to float
     const int32_t* kind;              // [R]
     const int32_t* reac;              // [2R]
     const uint8_t* allowed;           // [R*(T+1)] or nullptr
@@ -140,8 +184,9 @@ struct NsmTraj {
     int64_t nrx, ndf;                 // reaction / diffusion events
     double t_last;                    // time of the last executed event
     int32_t* x;                       // [N*S] counts
-    double* leaf;                     // [leaf_stride] next-event times
-    TreeNode* node;                   // [num_nodes] tree levels >= 1
+    long long* leaf;                  // [leaf_stride] next-event times (double bits)
+    long long* node_t;                // [num_nodes] tree times, levels >= 1
+    int32_t* node_i;                  // [num_nodes] tree voxel indices
 };
 
 }  // namespace spg

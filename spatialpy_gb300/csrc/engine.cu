@@ -21,9 +21,11 @@
 namespace spg {
 void launch_nsm_init(NsmTraj* trajs, const NsmInstance* insts, int ntraj, int max_leaf,
                      int max_levels, const uint32_t* const* u0, cudaStream_t st);
-void launch_nsm_advance(bool ref, NsmTraj* trajs, const NsmInstance* insts, int ntraj,
-                        int step_end, double dt, long long budget, long long max_ns, int* work,
-                        int num_sms, cudaStream_t st);
+int nsm_warp_smem(const NsmInstance& d, bool with_state);
+void launch_nsm_advance(bool ref, bool smem_state, int variant, int warp_smem, int wpb,
+                        NsmTraj* trajs, const NsmInstance* insts, int ntraj, int step_end,
+                        double dt, long long budget, long long max_ns, int* work, int num_sms,
+                        cudaStream_t st);
 void launch_nsm_snapshot(const NsmTraj* trajs, const NsmInstance* insts, int ntraj,
                          int32_t* counts, const long long* count_off, long long* moments,
                          const long long* mom_off, int out_index, cudaStream_t st);
@@ -44,13 +46,14 @@ struct Instance {
     double h = 0, rho0 = 0, c0 = 0, P0 = 0, g[3] = {0, 0, 0};
     std::vector<double> x_host;
     // device arrays
-    double *x = nullptr, *mass = nullptr, *rho = nullptr, *nu = nullptr, *vol = nullptr;
+    double *x = nullptr, *mass = nullptr, *rho = nullptr, *nu = nullptr;
+    float *vol = nullptr, *ivol = nullptr;
     int *type = nullptr;
     uint8_t* fixed = nullptr;
     int *nbr_cnt = nullptr, *nbr_idx = nullptr;
     double *nbr_dist = nullptr, *nbr_dwdr = nullptr, *nbr_dij = nullptr;
-    double *cdf = nullptr, *ddiag = nullptr;
-    double *rate = nullptr, *diffusion = nullptr;
+    float *cdf = nullptr, *ddiag = nullptr, *rate = nullptr;
+    double* diffusion = nullptr;
     int *kind = nullptr, *reac = nullptr, *jcN = nullptr, *irN = nullptr, *prN = nullptr;
     uint8_t* allowed = nullptr;
     uint32_t* u0 = nullptr;   // device copy for the current run
@@ -60,11 +63,25 @@ struct Instance {
 
 }  // namespace
 
+struct RunState {
+    bool active = false;
+    sp_run_args args{};
+    sp_outputs out{};
+    std::vector<int> inst;
+    std::vector<void*> tmp;
+    std::chrono::steady_clock::time_point wall0;
+    bool smem_state = false, want_counts = false, want_mom = false;
+    int warp_smem = 0, wpb = 1, variant = 0, next_out = 0, result = SP_OK;
+    long long ctot = 0, mtot = 0;
+    int32_t* d_counts = nullptr;
+    long long *d_mom = nullptr, *d_coff = nullptr, *d_moff = nullptr;
+};
+
 struct sp_handle {
     int device = 0;
     int num_sms = 0;
     cudaStream_t st = nullptr;
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr, ea = nullptr, eb = nullptr;
     sp_options opt{};
     std::vector<Instance> inst;
     std::vector<void*> allocs;
@@ -80,8 +97,9 @@ struct sp_handle {
     std::vector<NsmTraj> h_trajs;
     int* d_work = nullptr;
     std::string err;
-    double last_ms = 0;
-    long long last_launches = 0;
+    double last_ms = 0, adv_ms = 0;
+    long long last_launches = 0, launches = 0;
+    RunState run;
 };
 
 int spg_set_cuda_error(sp_handle* h, cudaError_t e, const char* what, const char* file, int line) {
@@ -197,9 +215,13 @@ static int setup_instance(sp_handle* h, const sp_scenario& s, Instance& I) {
     if ((rc = dev_upload(h, &I.rho, s.rho, N))) return rc;
     if ((rc = dev_upload(h, &I.nu, s.nu, N))) return rc;
     if ((rc = dev_upload(h, &I.fixed, s.fixed, N))) return rc;
-    std::vector<double> vol(N);
-    for (int p = 0; p < N; p++) vol[p] = s.mass[p] / s.rho[p];   // simulate_rdme.cpp:123
+    std::vector<float> vol(N), ivol(N);
+    for (int p = 0; p < N; p++) {
+        vol[p] = (float)(s.mass[p] / s.rho[p]);   // simulate_rdme.cpp:123
+        ivol[p] = (float)(s.rho[p] / s.mass[p]);
+    }
     if ((rc = dev_upload(h, &I.vol, vol.data(), N))) return rc;
+    if ((rc = dev_upload(h, &I.ivol, ivol.data(), N))) return rc;
     // reaction tables
     const int R = I.R, S = I.S, T = I.T;
     std::vector<int> jc(R + 1, 0), ir, pr;
@@ -207,7 +229,9 @@ static int setup_instance(sp_handle* h, const sp_scenario& s, Instance& I) {
         for (int r = 0; r <= R; r++) jc[r] = (int)s.jcN[r];
         ir.assign(s.irN, s.irN + s.jcN[R]);
         pr.assign(s.prN, s.prN + s.jcN[R]);
-        if ((rc = dev_upload(h, &I.rate, s.rxn_rate, R))) return rc;
+        std::vector<float> rate(R);
+        for (int r = 0; r < R; r++) rate[r] = (float)s.rxn_rate[r];
+        if ((rc = dev_upload(h, &I.rate, rate.data(), R))) return rc;
         if ((rc = dev_upload(h, &I.kind, s.rxn_kind, R))) return rc;
         if ((rc = dev_upload(h, &I.reac, s.rxn_reactants, 2 * (size_t)R))) return rc;
         if (s.rxn_allowed && (rc = dev_upload(h, &I.allowed, s.rxn_allowed, (size_t)R * (T + 1))))
@@ -275,6 +299,7 @@ static int setup_instance(sp_handle* h, const sp_scenario& s, Instance& I) {
     tree_layout(d, N);
     d.type = I.type;
     d.vol = I.vol;
+    d.ivol = I.ivol;
     d.nbr_cnt = I.nbr_cnt;
     d.nbr_idx = I.nbr_idx;
     d.cdf = I.cdf;
@@ -302,25 +327,28 @@ int sp_create(const sp_scenario* scenarios, int32_t num_scenarios, const sp_opti
     if (opts) h->opt = *opts;
     *out = h;
     h->device = h->opt.device;
-    SP_CUDA_TRY(cudaSetDevice(h->device));
-    SP_CUDA_TRY(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device));
-    SP_CUDA_TRY(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
-    SP_CUDA_TRY(cudaEventCreate(&h->e0));
-    SP_CUDA_TRY(cudaEventCreate(&h->e1));
+    // arguments are checked before any device call
     for (int i = 0; i < num_scenarios; i++) {
         int rc = validate(h, scenarios[i], i);
         if (rc) return rc;
     }
     const sp_scenario& s0 = scenarios[0];
-    h->dt = s0.dt;
-    h->num_steps = s0.num_steps;
-    h->output_steps.assign(s0.output_steps, s0.output_steps + s0.num_outputs);
     for (int i = 1; i < num_scenarios; i++) {
         const sp_scenario& s = scenarios[i];
         if (s.dt != s0.dt || s.num_steps != s0.num_steps || s.num_outputs != s0.num_outputs ||
             !std::equal(s.output_steps, s.output_steps + s.num_outputs, s0.output_steps))
             return fail(h, SP_E_INVALID, "all instances of one handle need the same time span");
     }
+    SP_CUDA_TRY(cudaSetDevice(h->device));
+    SP_CUDA_TRY(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device));
+    SP_CUDA_TRY(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+    SP_CUDA_TRY(cudaEventCreate(&h->e0));
+    SP_CUDA_TRY(cudaEventCreate(&h->e1));
+    SP_CUDA_TRY(cudaEventCreate(&h->ea));
+    SP_CUDA_TRY(cudaEventCreate(&h->eb));
+    h->dt = s0.dt;
+    h->num_steps = s0.num_steps;
+    h->output_steps.assign(s0.output_steps, s0.output_steps + s0.num_outputs);
     h->inst.resize(num_scenarios);
     std::vector<NsmInstance> descs(num_scenarios);
     for (int i = 0; i < num_scenarios; i++) {
@@ -344,8 +372,9 @@ static int ensure_traj(sp_handle* h, int ntraj, const int* inst) {
         const NsmInstance& d = h->inst[inst[j]].desc;
         off[j] = bytes;
         bytes += align(sizeof(int32_t) * (size_t)d.N * d.S);
-        bytes += align(sizeof(double) * (size_t)d.leaf_stride);
-        bytes += align(sizeof(TreeNode) * (size_t)d.num_nodes);
+        bytes += align(sizeof(long long) * (size_t)d.leaf_stride);
+        bytes += align(sizeof(long long) * (size_t)d.num_nodes);
+        bytes += align(sizeof(int32_t) * (size_t)d.num_nodes);
     }
     if (bytes > h->traj_bytes) {
         if (h->traj_mem) cudaFree(h->traj_mem);
@@ -364,32 +393,50 @@ static int ensure_traj(sp_handle* h, int ntraj, const int* inst) {
         char* p = base + off[j];
         T.x = (int32_t*)p;
         p += align(sizeof(int32_t) * (size_t)d.N * d.S);
-        T.leaf = (double*)p;
-        p += align(sizeof(double) * (size_t)d.leaf_stride);
-        T.node = (TreeNode*)p;
+        T.leaf = (long long*)p;
+        p += align(sizeof(long long) * (size_t)d.leaf_stride);
+        T.node_t = (long long*)p;
+        p += align(sizeof(long long) * (size_t)d.num_nodes);
+        T.node_i = (int32_t*)p;
     }
     return SP_OK;
 }
 
-int sp_run(sp_handle* h, const sp_run_args* a, sp_outputs* out) {
+// ---------------------------------------------------------------------------
+// ensemble runs: start (upload, queue build, output 0), continue (advance
+// through further outputs), finish (copy results to the caller)
+// ---------------------------------------------------------------------------
+static void run_release(sp_handle* h) {
+    RunState& R = h->run;
+    for (void* p : R.tmp) cudaFree(p);
+    R.tmp.clear();
+    R.active = false;
+}
+
+int sp_run_start(sp_handle* h, const sp_run_args* a, sp_outputs* out) {
     if (!h) return SP_E_INVALID;
     if (!a || a->num_trajectories < 1 || !a->seeds || !a->u0)
         return fail(h, SP_E_INVALID, "sp_run: num_trajectories, seeds and u0 are required");
     if (a->selection != SP_SELECT_EXACT && a->selection != SP_SELECT_REFERENCE)
         return fail(h, SP_E_INVALID, "sp_run: unknown selection mode");
     SP_CUDA_TRY(cudaSetDevice(h->device));
-    const auto wall0 = std::chrono::steady_clock::now();
+    if (h->run.active) run_release(h);
+    RunState& R = h->run;
+    R = RunState{};
+    R.wall0 = std::chrono::steady_clock::now();
+    R.args = *a;
+    R.out = out ? *out : sp_outputs{};
     const int ntraj = a->num_trajectories;
     const int ninst = (int)h->inst.size();
-    std::vector<int> inst(ntraj, 0);
+    R.inst.assign(ntraj, 0);
     for (int j = 0; j < ntraj; j++) {
-        inst[j] = a->instance ? a->instance[j] : 0;
-        if (inst[j] < 0 || inst[j] >= ninst) return fail(h, SP_E_INVALID, "instance index out of range");
-        if (!h->inst[inst[j]].is_static)
+        R.inst[j] = a->instance ? a->instance[j] : 0;
+        if (R.inst[j] < 0 || R.inst[j] >= ninst) return fail(h, SP_E_INVALID, "instance index out of range");
+        if (!h->inst[R.inst[j]].is_static)
             return fail(h, SP_E_UNSUPPORTED, "sp_run: moving (non-static) domains are run by sp_sdpd_advance");
-        if (h->inst[inst[j]].S == 0) return fail(h, SP_E_INVALID, "sp_run: model has no species");
+        if (h->inst[R.inst[j]].S == 0) return fail(h, SP_E_INVALID, "sp_run: model has no species");
     }
-    int rc = ensure_traj(h, ntraj, inst.data());
+    int rc = ensure_traj(h, ntraj, R.inst.data());
     if (rc) return rc;
     for (int j = 0; j < ntraj; j++) {
         NsmTraj& T = h->h_trajs[j];
@@ -403,16 +450,20 @@ int sp_run(sp_handle* h, const sp_run_args* a, sp_outputs* out) {
         T.t_last = 0.0;
     }
     cudaStream_t st = h->st;
-    long long launches = 0;
+    R.active = true;
+    h->launches = 0;
+    h->adv_ms = 0;
     SP_CUDA_TRY(cudaEventRecord(h->e0, st));
     SP_CUDA_TRY(cudaMemcpyAsync(h->d_trajs, h->h_trajs.data(), sizeof(NsmTraj) * ntraj,
                                 cudaMemcpyHostToDevice, st));
+    auto dmalloc = [&](void** p, size_t bytes) -> int {
+        cudaError_t e = cudaMalloc(p, bytes);
+        if (e != cudaSuccess) { run_release(h); return spg_set_cuda_error(h, e, "cudaMalloc", __FILE__, __LINE__); }
+        R.tmp.push_back(*p);
+        return SP_OK;
+    };
     // initial counts (u0 per instance)
     std::vector<const uint32_t*> u0ptr(ninst, nullptr);
-    std::vector<void*> tmp;
-    auto cleanup = [&]() {
-        for (void* p : tmp) cudaFree(p);
-    };
     for (int i = 0; i < ninst; i++) {
         const Instance& I = h->inst[i];
         if (!a->u0[i]) continue;
@@ -420,84 +471,124 @@ int sp_run(sp_handle* h, const sp_run_args* a, sp_outputs* out) {
             u0ptr[i] = a->u0[i];
         } else {
             void* d = nullptr;
-            cudaError_t e = cudaMalloc(&d, sizeof(uint32_t) * (size_t)I.N * I.S);
-            if (e != cudaSuccess) { cleanup(); return spg_set_cuda_error(h, e, "cudaMalloc u0", __FILE__, __LINE__); }
-            tmp.push_back(d);
-            cudaMemcpyAsync(d, a->u0[i], sizeof(uint32_t) * (size_t)I.N * I.S,
-                            cudaMemcpyHostToDevice, st);
+            if ((rc = dmalloc(&d, sizeof(uint32_t) * (size_t)I.N * I.S))) return rc;
+            cudaMemcpyAsync(d, a->u0[i], sizeof(uint32_t) * (size_t)I.N * I.S, cudaMemcpyHostToDevice, st);
             u0ptr[i] = (const uint32_t*)d;
         }
     }
     for (int j = 0; j < ntraj; j++)
-        if (!u0ptr[inst[j]]) { cleanup(); return fail(h, SP_E_INVALID, "u0 missing for an instance in use"); }
+        if (!u0ptr[R.inst[j]]) { run_release(h); return fail(h, SP_E_INVALID, "u0 missing for an instance in use"); }
     const uint32_t** d_u0 = nullptr;
-    {
-        cudaError_t e = cudaMalloc(&d_u0, sizeof(void*) * ninst);
-        if (e != cudaSuccess) { cleanup(); return spg_set_cuda_error(h, e, "cudaMalloc", __FILE__, __LINE__); }
-        tmp.push_back(d_u0);
-        cudaMemcpyAsync(d_u0, u0ptr.data(), sizeof(void*) * ninst, cudaMemcpyHostToDevice, st);
-    }
-    int max_leaf = 0, max_levels = 0;
+    if ((rc = dmalloc((void**)&d_u0, sizeof(void*) * ninst))) return rc;
+    cudaMemcpyAsync(d_u0, u0ptr.data(), sizeof(void*) * ninst, cudaMemcpyHostToDevice, st);
+    int max_leaf = 0, max_levels = 0, smem_state_bytes = 0, smem_tree_bytes = 0;
+    int maxS = 0, maxR = 0, maxT = 0;
     for (int j = 0; j < ntraj; j++) {
-        const NsmInstance& d = h->inst[inst[j]].desc;
+        const Instance& I = h->inst[R.inst[j]];
+        const NsmInstance& d = I.desc;
         max_leaf = std::max(max_leaf, d.leaf_stride);
         max_levels = std::max(max_levels, d.levels);
+        smem_state_bytes = std::max(smem_state_bytes, nsm_warp_smem(d, true));
+        smem_tree_bytes = std::max(smem_tree_bytes, nsm_warp_smem(d, false));
+        maxS = std::max(maxS, I.S);
+        maxR = std::max(maxR, I.R);
+        maxT = std::max(maxT, I.T);
     }
+    // shared-memory policy: whole trajectory state when it fits in 48 KB per
+    // warp, else the tree only (levels >= 1, 12 bytes per node)
+    R.smem_state = smem_state_bytes <= 48 * 1024;
+    R.warp_smem = R.smem_state ? smem_state_bytes : smem_tree_bytes;
+    if (R.warp_smem > 200 * 1024) {
+        run_release(h);
+        return fail(h, SP_E_UNSUPPORTED, "domain too large for the shared-memory event queue");
+    }
+    R.wpb = R.warp_smem <= 24 * 1024 ? 4 : R.warp_smem <= 48 * 1024 ? 2 : 1;
+    // kernel variant: register-resident networks when small enough
+    int minS = 1 << 30, minR = 1 << 30;
+    for (int j = 0; j < ntraj; j++) {
+        minS = std::min(minS, h->inst[R.inst[j]].S);
+        minR = std::min(minR, h->inst[R.inst[j]].R);
+    }
+    R.variant = 0;
+    if (maxT < 64 && minS == maxS && minR == maxR && maxS == 1 && maxR == 2) R.variant = 3;
+    else if (maxT < 64 && minS == maxS && minR == maxR && maxS == 3 && maxR == 4) R.variant = 4;
+    else if (maxT < 64 && maxS <= 4 && maxR <= 8) R.variant = 1;
+    else if (maxT < 64 && maxS <= 8 && maxR <= 16) R.variant = 2;
+    if (h->opt.nsm_variant == 1) R.variant = 0;   // force the generic warp kernel
     launch_nsm_init(h->d_trajs, h->d_insts, ntraj, max_leaf, max_levels, d_u0, st);
-    launches += 2 + max_levels;
+    h->launches += 2 + max_levels;
     // output buffers
     const int nout = (int)h->output_steps.size();
     std::vector<long long> count_off(ntraj), mom_off(ninst);
-    long long ctot = 0, mtot = 0;
+    R.ctot = 0;
+    R.mtot = 0;
     for (int j = 0; j < ntraj; j++) {
-        count_off[j] = ctot;
-        ctot += (long long)nout * h->inst[inst[j]].N * h->inst[inst[j]].S;
+        count_off[j] = R.ctot;
+        R.ctot += (long long)nout * h->inst[R.inst[j]].N * h->inst[R.inst[j]].S;
     }
     for (int i = 0; i < ninst; i++) {
-        mom_off[i] = mtot;
-        mtot += (long long)nout * h->inst[i].N * h->inst[i].S;
+        mom_off[i] = R.mtot;
+        R.mtot += (long long)nout * h->inst[i].N * h->inst[i].S;
     }
-    int32_t* d_counts = nullptr;
-    long long* d_mom = nullptr;
-    long long *d_coff = nullptr, *d_moff = nullptr;
-    auto dmalloc = [&](void** p, size_t b) -> int {
-        cudaError_t e = cudaMalloc(p, b);
-        if (e != cudaSuccess) return spg_set_cuda_error(h, e, "cudaMalloc outputs", __FILE__, __LINE__);
-        tmp.push_back(*p);
-        return SP_OK;
-    };
-    const bool want_counts = a->want_counts && out && out->counts;
-    const bool want_mom = a->want_moments && out && out->moments;
-    if (want_counts) {
-        if (a->buffers_on_device) d_counts = out->counts;
-        else if ((rc = dmalloc((void**)&d_counts, sizeof(int32_t) * ctot))) { cleanup(); return rc; }
-        if ((rc = dmalloc((void**)&d_coff, sizeof(long long) * ntraj))) { cleanup(); return rc; }
-        cudaMemcpyAsync(d_coff, count_off.data(), sizeof(long long) * ntraj, cudaMemcpyHostToDevice, st);
+    R.want_counts = a->want_counts && out && out->counts;
+    R.want_mom = a->want_moments && out && out->moments;
+    if (R.want_counts) {
+        if (a->buffers_on_device) R.d_counts = out->counts;
+        else if ((rc = dmalloc((void**)&R.d_counts, sizeof(int32_t) * R.ctot))) return rc;
+        if ((rc = dmalloc((void**)&R.d_coff, sizeof(long long) * ntraj))) return rc;
+        cudaMemcpyAsync(R.d_coff, count_off.data(), sizeof(long long) * ntraj, cudaMemcpyHostToDevice, st);
     }
-    if (want_mom) {
-        if (a->buffers_on_device) d_mom = (long long*)out->moments;
-        else if ((rc = dmalloc((void**)&d_mom, sizeof(long long) * 2 * mtot))) { cleanup(); return rc; }
-        if ((rc = dmalloc((void**)&d_moff, sizeof(long long) * ninst))) { cleanup(); return rc; }
-        cudaMemcpyAsync(d_moff, mom_off.data(), sizeof(long long) * ninst, cudaMemcpyHostToDevice, st);
-        cudaMemsetAsync(d_mom, 0, sizeof(long long) * 2 * mtot, st);
+    if (R.want_mom) {
+        if (a->buffers_on_device) R.d_mom = (long long*)out->moments;
+        else if ((rc = dmalloc((void**)&R.d_mom, sizeof(long long) * 2 * R.mtot))) return rc;
+        if ((rc = dmalloc((void**)&R.d_moff, sizeof(long long) * ninst))) return rc;
+        cudaMemcpyAsync(R.d_moff, mom_off.data(), sizeof(long long) * ninst, cudaMemcpyHostToDevice, st);
+        cudaMemsetAsync(R.d_mom, 0, sizeof(long long) * 2 * R.mtot, st);
     }
-    const bool ref = a->selection == SP_SELECT_REFERENCE;
+    R.next_out = 0;
+    R.result = SP_OK;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) { run_release(h); return spg_set_cuda_error(h, e, "sp_run_start", __FILE__, __LINE__); }
+    // outputs at step 0 need no events
+    return sp_run_continue(h, 0);
+}
+
+int sp_run_continue(sp_handle* h, int32_t num_outputs) {
+    if (!h) return SP_E_INVALID;
+    RunState& R = h->run;
+    if (!R.active) return fail(h, SP_E_INVALID, "sp_run_continue: no run in progress");
+    if (num_outputs < 0) return fail(h, SP_E_INVALID, "sp_run_continue: negative output count");
+    SP_CUDA_TRY(cudaSetDevice(h->device));
+    cudaStream_t st = h->st;
+    const int ntraj = R.args.num_trajectories;
+    const int nout = (int)h->output_steps.size();
+    const bool ref = R.args.selection == SP_SELECT_REFERENCE;
     const long long budget = h->opt.event_budget > 0 ? h->opt.event_budget : (1ll << 62);
     const long long max_ns = 2000000000ll;
-    int result = SP_OK;
-    for (int k = 0; k < nout && result == SP_OK; k++) {
-        const int target = h->output_steps[k];
+    int done = 0;
+    h->launches = 0;
+    h->adv_ms = 0;
+    SP_CUDA_TRY(cudaEventRecord(h->e0, st));
+    while (R.next_out < nout && R.result == SP_OK) {
+        const int target = h->output_steps[R.next_out];
         if (target > 0) {
-            for (int attempt = 0;; attempt++) {
-                launch_nsm_advance(ref, h->d_trajs, h->d_insts, ntraj, target, h->dt, budget, max_ns,
-                                   h->d_work, h->num_sms, st);
-                launches++;
+            if (done >= num_outputs) break;
+            for (;;) {
+                cudaEventRecord(h->ea, st);
+                launch_nsm_advance(ref, R.smem_state, R.variant, R.warp_smem, R.wpb, h->d_trajs,
+                                   h->d_insts, ntraj, target, h->dt, budget, max_ns, h->d_work,
+                                   h->num_sms, st);
+                cudaEventRecord(h->eb, st);
+                h->launches++;
                 cudaError_t e = cudaGetLastError();
-                if (e != cudaSuccess) { cleanup(); return spg_set_cuda_error(h, e, "nsm_advance", __FILE__, __LINE__); }
+                if (e != cudaSuccess) { run_release(h); return spg_set_cuda_error(h, e, "nsm_advance", __FILE__, __LINE__); }
                 e = cudaMemcpyAsync(h->h_trajs.data(), h->d_trajs, sizeof(NsmTraj) * ntraj,
                                     cudaMemcpyDeviceToHost, st);
                 if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-                if (e != cudaSuccess) { cleanup(); return spg_set_cuda_error(h, e, "nsm_advance sync", __FILE__, __LINE__); }
+                if (e != cudaSuccess) { run_release(h); return spg_set_cuda_error(h, e, "nsm_advance sync", __FILE__, __LINE__); }
+                float ms = 0;
+                cudaEventElapsedTime(&ms, h->ea, h->eb);
+                h->adv_ms += ms;
                 bool again = false;
                 for (int j = 0; j < ntraj; j++) {
                     NsmTraj& T = h->h_trajs[j];
@@ -505,48 +596,37 @@ int sp_run(sp_handle* h, const sp_run_args* a, sp_outputs* out) {
                         T.status = SP_TRAJ_OK;
                         again = true;
                     } else if (T.status != SP_TRAJ_OK) {
-                        result = SP_E_TRAJECTORY;
+                        R.result = SP_E_TRAJECTORY;
                     }
                 }
-                if (result != SP_OK) break;
-                if (a->timeout_s > 0) {
-                    const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - wall0).count();
-                    if (el > a->timeout_s) { result = SP_E_TIMEOUT; break; }
+                if (R.result != SP_OK) break;
+                if (R.args.timeout_s > 0) {
+                    const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - R.wall0).count();
+                    if (el > R.args.timeout_s) { R.result = SP_E_TIMEOUT; break; }
                 }
                 if (!again) break;
                 // resume: statuses were reset on the host copy
                 cudaMemcpyAsync(h->d_trajs, h->h_trajs.data(), sizeof(NsmTraj) * ntraj,
                                 cudaMemcpyHostToDevice, st);
             }
+            done++;
         }
-        if (result != SP_OK) break;
-        if (want_counts || want_mom) {
-            launch_nsm_snapshot(h->d_trajs, h->d_insts, ntraj, want_counts ? d_counts : nullptr,
-                                d_coff, want_mom ? d_mom : nullptr, d_moff, k, st);
-            launches++;
+        if (R.result != SP_OK) break;
+        if (R.want_counts || R.want_mom) {
+            launch_nsm_snapshot(h->d_trajs, h->d_insts, ntraj, R.want_counts ? R.d_counts : nullptr,
+                                R.d_coff, R.want_mom ? R.d_mom : nullptr, R.d_moff, R.next_out, st);
+            h->launches++;
         }
+        R.next_out++;
     }
     cudaEventRecord(h->e1, st);
-    if (result == SP_OK || result == SP_E_TRAJECTORY) {
-        if (want_counts && !a->buffers_on_device)
-            cudaMemcpyAsync(out->counts, d_counts, sizeof(int32_t) * ctot, cudaMemcpyDeviceToHost, st);
-        if (want_mom && !a->buffers_on_device)
-            cudaMemcpyAsync(out->moments, d_mom, sizeof(long long) * 2 * mtot, cudaMemcpyDeviceToHost, st);
-    }
-    cudaMemcpyAsync(h->h_trajs.data(), h->d_trajs, sizeof(NsmTraj) * ntraj, cudaMemcpyDeviceToHost, st);
     cudaError_t e = cudaStreamSynchronize(st);
-    cleanup();
-    if (e != cudaSuccess) return spg_set_cuda_error(h, e, "sp_run", __FILE__, __LINE__);
+    if (e != cudaSuccess) { run_release(h); return spg_set_cuda_error(h, e, "sp_run_continue", __FILE__, __LINE__); }
     float ms = 0;
     cudaEventElapsedTime(&ms, h->e0, h->e1);
     h->last_ms = ms;
-    h->last_launches = launches;
-    if (out && out->event_counts)
-        for (int j = 0; j < ntraj; j++) {
-            out->event_counts[2 * j] = h->h_trajs[j].nrx;
-            out->event_counts[2 * j + 1] = h->h_trajs[j].ndf;
-        }
-    if (result == SP_E_TRAJECTORY) {
+    h->last_launches = h->launches;
+    if (R.result == SP_E_TRAJECTORY) {
         for (int j = 0; j < ntraj; j++)
             if (h->h_trajs[j].status != SP_TRAJ_OK) {
                 char b[256];
@@ -555,10 +635,62 @@ int sp_run(sp_handle* h, const sp_run_args* a, sp_outputs* out) {
                 h->err = b;
                 break;
             }
-    } else if (result == SP_E_TIMEOUT) {
+    } else if (R.result == SP_E_TIMEOUT) {
         h->err = "sp_run: timeout";
     }
+    return R.result;
+}
+
+int sp_run_finish(sp_handle* h) {
+    if (!h) return SP_E_INVALID;
+    RunState& R = h->run;
+    if (!R.active) return fail(h, SP_E_INVALID, "sp_run_finish: no run in progress");
+    SP_CUDA_TRY(cudaSetDevice(h->device));
+    cudaStream_t st = h->st;
+    const int ntraj = R.args.num_trajectories;
+    if (!R.args.buffers_on_device) {
+        if (R.want_counts)
+            cudaMemcpyAsync(R.out.counts, R.d_counts, sizeof(int32_t) * R.ctot, cudaMemcpyDeviceToHost, st);
+        if (R.want_mom)
+            cudaMemcpyAsync(R.out.moments, R.d_mom, sizeof(long long) * 2 * R.mtot, cudaMemcpyDeviceToHost, st);
+    }
+    cudaMemcpyAsync(h->h_trajs.data(), h->d_trajs, sizeof(NsmTraj) * ntraj, cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    const int result = R.result;
+    if (R.out.event_counts)
+        for (int j = 0; j < ntraj; j++) {
+            R.out.event_counts[2 * j] = h->h_trajs[j].nrx;
+            R.out.event_counts[2 * j + 1] = h->h_trajs[j].ndf;
+        }
+    run_release(h);
+    if (e != cudaSuccess) return spg_set_cuda_error(h, e, "sp_run_finish", __FILE__, __LINE__);
     return result;
+}
+
+int sp_run(sp_handle* h, const sp_run_args* a, sp_outputs* out) {
+    int rc = sp_run_start(h, a, out);
+    if (rc != SP_OK) {
+        if (h && h->run.active) sp_run_finish(h);
+        return rc;
+    }
+    double ms0 = h->last_ms;
+    long long l0 = h->last_launches;
+    const int rc2 = sp_run_continue(h, 1 << 30);
+    const double adv = h->adv_ms;
+    h->last_ms += ms0;
+    h->last_launches += l0;
+    const int rc3 = sp_run_finish(h);
+    h->adv_ms = adv;
+    return rc2 != SP_OK ? rc2 : rc3;
+}
+
+int sp_last_profile(sp_handle* h, sp_profile* p) {
+    if (!h || !p) return SP_E_INVALID;
+    p->total_ms = h->last_ms;
+    p->kernel_ms = h->adv_ms;
+    p->launches = h->last_launches;
+    p->reserved = 0;
+    return SP_OK;
 }
 
 int sp_status(sp_handle* h, int32_t traj, sp_traj_status* st) {
@@ -576,14 +708,21 @@ const char* sp_last_error(sp_handle* h) { return h ? h->err.c_str() : "null hand
 
 void sp_destroy(sp_handle* h) {
     if (!h) return;
+    if (!h->st) {   // never reached the device (argument errors)
+        delete h;
+        return;
+    }
     cudaSetDevice(h->device);
     if (h->st) cudaStreamSynchronize(h->st);
+    if (h->run.active) run_release(h);
     for (Instance& I : h->inst)
         if (I.sdpd) sdpd_destroy(I.sdpd);
     for (void* p : h->allocs) cudaFree(p);
     if (h->traj_mem) cudaFree(h->traj_mem);
     if (h->e0) cudaEventDestroy(h->e0);
     if (h->e1) cudaEventDestroy(h->e1);
+    if (h->ea) cudaEventDestroy(h->ea);
+    if (h->eb) cudaEventDestroy(h->eb);
     if (h->st) cudaStreamDestroy(h->st);
     delete h;
 }
@@ -623,7 +762,9 @@ int sp_get_ddiag(sp_handle* h, int32_t inst, double* ddiag) {
     if (!h || inst < 0 || inst >= (int)h->inst.size() || !ddiag) return SP_E_INVALID;
     Instance& I = h->inst[inst];
     if (!I.ddiag) return fail(h, SP_E_INVALID, "instance has no diffusion tables");
-    SP_CUDA_TRY(cudaMemcpy(ddiag, I.ddiag, sizeof(double) * (size_t)I.N * I.S, cudaMemcpyDeviceToHost));
+    std::vector<float> f((size_t)I.N * I.S);
+    SP_CUDA_TRY(cudaMemcpy(f.data(), I.ddiag, sizeof(float) * f.size(), cudaMemcpyDeviceToHost));
+    for (size_t e = 0; e < f.size(); e++) ddiag[e] = f[e];
     return SP_OK;
 }
 

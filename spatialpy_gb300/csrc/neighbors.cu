@@ -157,10 +157,11 @@ __global__ void neighbor_search_f64(const double* xq, const double* xt, int n, C
 }
 
 // Ddiag[i,s] = sum_k D(s, type_j) D_ij (simulate_rdme.cpp:142-148) and the
-// running sums over the list, the destination scan of :359-367.
+// running sums over the list scanned by the destination choice (:359-367),
+// accumulated in double in list order and rounded to float.
 __global__ void diffusion_tables(int n, int S, int T, int kmax, const int* type, const int* count,
                                  const int* idx, const double* dij, const double* diffusion,
-                                 double* ddiag, double* cdf) {
+                                 float* ddiag, float* cdf) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n * S) return;
     const int i = e / S, s = e % S;
@@ -169,9 +170,9 @@ __global__ void diffusion_tables(int n, int S, int T, int kmax, const int* type,
         const int j = idx[(size_t)i * kmax + k];
         const double dc = diffusion[s * T + (type[j] - 1)];
         acc = acc + dc * dij[(size_t)i * kmax + k];
-        cdf[((size_t)i * S + s) * kmax + k] = acc;
+        cdf[((size_t)i * S + s) * kmax + k] = (float)acc;
     }
-    ddiag[e] = acc;
+    ddiag[e] = (float)acc;
 }
 
 // ---------------------------------------------------------------------------
@@ -236,7 +237,7 @@ int run_neighbor_search(const double* d_xq, const double* d_xt, int n, const Cel
 
 void launch_diffusion_tables(int n, int S, int T, int kmax, const int* d_type, const int* d_count,
                              const int* d_idx, const double* d_dij, const double* d_diffusion,
-                             double* d_ddiag, double* d_cdf, cudaStream_t st) {
+                             float* d_ddiag, float* d_cdf, cudaStream_t st) {
     const int e = n * S;
     diffusion_tables<<<(e + 255) / 256, 256, 0, st>>>(n, S, T, kmax, d_type, d_count, d_idx, d_dij,
                                                       d_diffusion, d_ddiag, d_cdf);

@@ -1,23 +1,628 @@
-// sdpd.cu — SDPD particle step (placeholder until the flow kernels land).
+// sdpd.cu — SDPD particle step on the GPU (FP32 or FP64).
+//
+// Restates one engine step of a moving domain (src/simulate_threads.cpp:232-281
+// with the kd-tree of :80-108): take_step1 (src/simulate.cpp:56-109),
+// find_neighbors + pairwiseForce (particle.cpp:240-294, model.cpp:39-191),
+// take_step2 with filterDensity and the boundary volume fraction
+// (simulate.cpp:132-173, model.cpp:194-329).  Per step, five launches:
+//
+//   begin     cell key of each particle at its start-of-step position (the
+//             kd-tree points of the step), copy of that position, predictor
+//   scan      exclusive scan of the cell histogram (one block)
+//   scatter   counting-sort scatter: tree points in cell order
+//   pairs     per particle: neighbour list of the moved position against the
+//             tree points, sorted by (r^2, j); pressure, viscous,
+//             background-pressure and transport forces and the density rate
+//             summed in list order
+//   corrector corrector, Shepard filter every 20 steps, boundary volume
+//             fraction and bounce-back
+//
+// Layout (HBM, structure of arrays): position, velocity, transport velocity,
+// force (+density rate in .w) and background force as 4-vectors of REAL;
+// rho, old_rho, mass, nu as REAL arrays; neighbour lists [N][KCAP].
+//
+// The reference builds its kd-tree once per step, so in the force pass a
+// moved particle is searched against start-of-step points and finds its own
+// start-of-step point at distance |dt vt|; that self pair enters the Shepard
+// filter and the boundary volume fraction.  The FP32 path takes that distance
+// from the predictor displacement dt*vt, which FP32 positions cannot resolve.
+// Densities read from neighbours in the corrector are their post-predictor
+// values (old_rho), the order a parallel engine reads them in.
+//
+// Compiled with -fmad=false: the arithmetic rounds like the CPU oracle.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include "common.cuh"
+#include "neighbors.cuh"
 #include "sdpd.cuh"
 
 namespace spg {
-struct SdpdState { int dummy; };
-SdpdState* sdpd_create(const sp_scenario&, int, cudaStream_t, std::string* err) {
-    *err = "moving domains are not supported yet";
-    return nullptr;
+
+template <typename R> struct Vec4;
+template <> struct Vec4<float> { using T = float4; };
+template <> struct Vec4<double> { using T = double4; };
+
+template <typename R>
+struct SdpdDev {
+    int N, dim, step, stat;
+    R h, dt, rho0, P0, alpha, g0, g1, g2;
+    typename Vec4<R>::T *pos, *vel, *vt, *F, *Fbp, *pold, *xs;
+    R *rho, *orho, *mass, *nu;
+    const uint8_t* fixed;
+    int *cell, *order, *start, *hist, *fill;
+    int *ncnt, *nidx;
+    R *ndist, *ndw;
+    int kcap;
+    CellGrid g;
+    int* flag;   // bit 1: list overflow, bit 2: NaN state
+};
+
+template <typename R>
+__device__ __forceinline__ int cellc(R p, const CellGrid& g, int d) {
+    if (d >= g.dim) return 0;
+    int c = (int)floor(((double)p - g.lo[d]) / g.cs);
+    c = c < 0 ? 0 : c;
+    return c >= g.nc[d] ? g.nc[d] - 1 : c;
 }
-void sdpd_destroy(SdpdState* s) { delete s; }
-int sdpd_advance(SdpdState*, int, double*, long long*, std::string* err) {
-    *err = "moving domains are not supported yet";
-    return SP_E_UNSUPPORTED;
+
+// take_step1 (simulate.cpp:56-109) + the cell key of the start-of-step point
+template <typename R>
+__global__ void sdpd_begin(SdpdDev<R> D) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= D.N) return;
+    auto p = D.pos[i];
+    auto v = D.vel[i];
+    R rho = D.rho[i];
+    if (isnan((double)p.x) || isinf((double)p.x) || isnan((double)p.y) || isinf((double)p.y) ||
+        isnan((double)p.z) || isinf((double)p.z) || isnan((double)v.x) || isinf((double)v.x) ||
+        isnan((double)v.y) || isinf((double)v.y) || isnan((double)v.z) || isinf((double)v.z) ||
+        isnan((double)rho) || isinf((double)rho))
+        atomicOr(D.flag, 2);
+    const int c = (cellc<R>(p.x, D.g, 0) * D.g.nc[1] + cellc<R>(p.y, D.g, 1)) * D.g.nc[2] +
+                  cellc<R>(p.z, D.g, 2);
+    D.cell[i] = c;
+    atomicAdd(&D.hist[c], 1);
+    D.pold[i] = p;
+    if (!D.stat && !D.fixed[i]) {
+        const auto F = D.F[i];
+        const auto Fb = D.Fbp[i];
+        const R hdt = (R)0.5 * D.dt;
+        v.x = v.x + hdt * F.x;
+        v.y = v.y + hdt * F.y;
+        v.z = v.z + hdt * F.z;
+        auto t = v;
+        t.x = v.x + hdt * Fb.x;
+        t.y = v.y + hdt * Fb.y;
+        t.z = v.z + hdt * Fb.z;
+        p.x = p.x + D.dt * t.x;
+        p.y = p.y + D.dt * t.y;
+        p.z = p.z + D.dt * t.z;
+        rho = rho + hdt * F.w;
+        D.vel[i] = v;
+        D.vt[i] = t;
+        D.pos[i] = p;
+        D.rho[i] = rho;
+    }
+    auto F = D.F[i];
+    F.x = D.g0; F.y = D.g1; F.z = D.g2; F.w = 0;
+    D.F[i] = F;
+    auto Fb = D.Fbp[i];
+    Fb.x = 0; Fb.y = 0; Fb.z = 0; Fb.w = 0;
+    D.Fbp[i] = Fb;
+    D.orho[i] = rho;
 }
-int sdpd_get_state(SdpdState*, double*, double*, double*, std::string* err) {
-    *err = "moving domains are not supported yet";
-    return SP_E_UNSUPPORTED;
+
+template <typename R>
+__global__ void sdpd_scatter(SdpdDev<R> D) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= D.N) return;
+    const int c = D.cell[i];
+    const int slot = D.start[c] + atomicAdd(&D.fill[c], 1);
+    D.order[slot] = i;
+    D.xs[slot] = D.pold[i];
 }
-int sdpd_copy_neighbors(SdpdState*, int, int*, int*, double*, double*, double*, std::string* err) {
-    *err = "moving domains are not supported yet";
-    return SP_E_UNSUPPORTED;
+
+// find_neighbors against the step's tree points + pairwiseForce (model.cpp:39-191)
+template <typename R, int KCAP>
+__global__ void __launch_bounds__(128) sdpd_pairs(SdpdDev<R> D, int first_step) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= D.N) return;
+    R cd2[KCAP];
+    int cj[KCAP];
+    // at the first step of a run the lists come from the unmoved points (take_step1)
+    const auto q = first_step ? D.pold[i] : D.pos[i];
+    const R h = D.h, sq = h * h;
+    const int dim = D.dim;
+    const int c0 = cellc<R>(q.x, D.g, 0), c1 = cellc<R>(q.y, D.g, 1), c2 = cellc<R>(q.z, D.g, 2);
+    int m = 0;
+    bool over = false;
+    R self_d2 = 0;
+    if (sizeof(R) == 4 && !first_step) {
+        const auto t = D.vt[i];
+        const R a = D.dt * t.x, b = D.dt * t.y, c = D.dt * t.z;
+        self_d2 = a * a;
+        if (dim > 1) self_d2 = self_d2 + b * b;
+        if (dim > 2) self_d2 = self_d2 + c * c;
+        if (D.stat || D.fixed[i]) self_d2 = 0;
+    }
+    for (int a = c0 - 1; a <= c0 + 1; a++) {
+        if (a < 0 || a >= D.g.nc[0]) continue;
+        for (int b = c1 - 1; b <= c1 + 1; b++) {
+            if (b < 0 || b >= D.g.nc[1]) continue;
+            for (int c = c2 - 1; c <= c2 + 1; c++) {
+                if (c < 0 || c >= D.g.nc[2]) continue;
+                const int cid = (a * D.g.nc[1] + b) * D.g.nc[2] + c;
+                const int e = D.start[cid + 1];
+                for (int t = D.start[cid]; t < e; t++) {
+                    const int j = D.order[t];
+                    const auto p = D.xs[t];
+                    R d2 = 0;
+                    const R t0 = q.x - p.x;
+                    d2 = d2 + t0 * t0;
+                    if (dim > 1) { const R t1 = q.y - p.y; d2 = d2 + t1 * t1; }
+                    if (dim > 2) { const R t2 = q.z - p.z; d2 = d2 + t2 * t2; }
+                    if (sizeof(R) == 4 && j == i) d2 = self_d2;
+                    if (d2 > sq || d2 == (R)0) continue;     // kd_fix_rad_search.cpp:160-174
+                    if (sqrt(d2) > h) continue;              // particle.cpp:160-162
+                    if (m >= KCAP || m >= D.kcap) { over = true; continue; }
+                    int k = m++;
+                    while (k > 0 && (d2 < cd2[k - 1] || (d2 == cd2[k - 1] && j < cj[k - 1]))) {
+                        cd2[k] = cd2[k - 1];
+                        cj[k] = cj[k - 1];
+                        k--;
+                    }
+                    cd2[k] = d2;
+                    cj[k] = j;
+                }
+            }
+        }
+    }
+    if (over) atomicOr(D.flag, 1);
+    D.ncnt[i] = m;
+    const R alpha = D.alpha;
+    const auto xi = D.pos[i];
+    const auto vi = D.vel[i];
+    const auto ti = D.vt[i];
+    const R rhoi = D.rho[i], mi = D.mass[i], nui = D.nu[i];
+    const R P0 = D.P0, rho0 = D.rho0;
+    const R Pi = P0 * (rhoi / rho0 - (R)1.0);
+    R Fx = D.g0, Fy = D.g1, Fz = D.g2, Bx = 0, By = 0, Bz = 0, Fr = 0;
+    for (int k = 0; k < m; k++) {
+        const int j = cj[k];
+        const R r = sqrt(cd2[k]);
+        const R R_ = r / h;
+        const R dWdr = alpha * ((R)-12 * r / (h * h)) * (((R)1 - R_) * ((R)1 - R_));
+        const size_t o = (size_t)i * D.kcap + k;
+        D.nidx[o] = j;
+        D.ndist[o] = r;
+        D.ndw[o] = dWdr;
+        if (R_ > (R)1.0 || r == (R)0) continue;
+        const auto xj = D.pos[j];
+        const auto vj4 = D.vel[j];
+        const auto tj = D.vt[j];
+        R dx0 = 0, dx1 = 0, dx2 = 0, dv0 = 0, dv1 = 0, dv2 = 0, dvdx = 0;
+        dx0 = xi.x - xj.x; dv0 = vi.x - vj4.x; dvdx = dvdx + dv0 * dx0;
+        if (dim > 1) { dx1 = xi.y - xj.y; dv1 = vi.y - vj4.y; dvdx = dvdx + dv1 * dx1; }
+        if (dim > 2) { dx2 = xi.z - xj.z; dv2 = vi.z - vj4.z; dvdx = dvdx + dv2 * dx2; }
+        const R rhoj = D.rho[j], mj = D.mass[j], nuj = D.nu[j];
+        const R Pj = P0 * (rhoj / rho0 - (R)1.0);
+        R pg = Pi / (rhoi * rhoi) + Pj / (rhoj * rhoj);
+        if (pg < 0) pg = -Pi / (rhoi * rhoi) + Pj / (rhoj * rhoj);
+        const R rh = r + (R)0.001 * h;
+        const R fp = (R)-1.0 * mj * pg * dWdr / rh;
+        const R fv = mj * ((R)2.0 * (nui * nuj) / (nui + nuj)) * ((R)1 / rh) * dWdr / (rhoi * rhoj);
+        const R wi = mi / rhoi, wj = mj / rhoj;
+        const R ss = wi * wi + wj * wj;
+        const R fbp = (R)-10.0 * P0 * ((R)1.0 / mi) * ss * dWdr / rh;
+        const R a0 = ti.x - vi.x, a1 = ti.y - vi.y, a2 = ti.z - vi.z;
+        const R b0 = tj.x - vj4.x, b1 = tj.y - vj4.y, b2 = tj.z - vj4.z;
+        R ft[3];
+        const R via[3] = {vi.x, vi.y, vi.z}, vja[3] = {vj4.x, vj4.y, vj4.z};
+#pragma unroll
+        for (int q2 = 0; q2 < 3; q2++) {
+            const R T0 = (R)0.5 * ((rhoi * via[q2] * a0) + (rhoj * vja[q2] * b0));
+            const R T1 = (R)0.5 * ((rhoi * via[q2] * a1) + (rhoj * vja[q2] * b1));
+            const R T2 = (R)0.5 * ((rhoi * via[q2] * a2) + (rhoj * vja[q2] * b2));
+            ft[q2] = ((R)1.0 / mi) * ss * (T0 * dx0 + T1 * dx1 + T2 * dx2) * dWdr / rh;
+        }
+        Fx = Fx + (fp * dx0 + fv * dv0 + ft[0]);
+        Bx = Bx + fbp * dx0;
+        if (dim > 1) { Fy = Fy + (fp * dx1 + fv * dv1 + ft[1]); By = By + fbp * dx1; }
+        if (dim > 2) { Fz = Fz + (fp * dx2 + fv * dv2 + ft[2]); Bz = Bz + fbp * dx2; }
+        const R tvi = (vi.x - ti.x) * dx0 + (vi.y - ti.y) * dx1 + (vi.z - ti.z) * dx2;
+        const R tvj = (vj4.x - tj.x) * dx0 + (vj4.y - tj.y) * dx1 + (vj4.z - tj.z) * dx2;
+        Fr = Fr + rhoi * wj * dvdx * ((R)1 / rh) * dWdr -
+             wj * (rhoi * tvi + rhoj * tvj) * ((R)1.0 / rh) * dWdr;
+    }
+    auto F = D.F[i];
+    F.x = Fx; F.y = Fy; F.z = Fz; F.w = Fr;
+    D.F[i] = F;
+    auto B = D.Fbp[i];
+    B.x = Bx; B.y = By; B.z = Bz;
+    D.Fbp[i] = B;
 }
+
+// take_step2 (simulate.cpp:132-173), filterDensity and the boundary volume
+// fraction (model.cpp:194-329)
+template <typename R>
+__global__ void sdpd_corrector(SdpdDev<R> D) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= D.N) return;
+    const bool fluid = !D.fixed[i] && !D.stat, wall = D.fixed[i] && !D.stat;
+    const R h = D.h, alpha = D.alpha, hdt = (R)0.5 * D.dt;
+    auto v = D.vel[i];
+    const auto F = D.F[i];
+    R rho = D.rho[i];
+    const int m = D.ncnt[i];
+    const size_t base = (size_t)i * D.kcap;
+    if (fluid) {
+        v.x = v.x + hdt * F.x;
+        v.y = v.y + hdt * F.y;
+        v.z = v.z + hdt * F.z;
+    }
+    if ((fluid || wall) && D.step % 20 == 0) {
+        R num = 0, den = 0;
+        for (int k = 0; k < m; k++) {
+            const R r = D.ndist[base + k];
+            const R R_ = r / h;
+            if (R_ > (R)1.0 || r == (R)0) continue;
+            const R omr = (R)1 - R_;
+            const R W = alpha * (((R)1 + (R)3 * R_) * (omr * omr * omr));
+            num = num + D.orho[D.nidx[base + k]] * W;
+            den = den + W;
+        }
+        rho = num / den;
+    }
+    if (fluid) {
+        rho = rho + hdt * F.w;
+        const auto xi = D.pos[i];
+        R nw0 = 0, nw1 = 0, nw2 = 0, vos = 0, vtot = 0;
+        for (int k = 0; k < m; k++) {
+            const R r = D.ndist[base + k];
+            const R R_ = r / h;
+            if (R_ > (R)1.0 || r == (R)0) continue;
+            const int j = D.nidx[base + k];
+            const R omr = (R)1 - R_;
+            const R W = alpha * (((R)1 + (R)3 * R_) * (omr * omr * omr));
+            const R dWdr = D.ndw[base + k];
+            const auto xj = D.pos[j];
+            R dx0 = xi.x - xj.x, dx1 = 0, dx2 = 0;
+            if (D.dim > 1) dx1 = xi.y - xj.y;
+            if (D.dim > 2) dx2 = xi.z - xj.z;
+            const R vj = D.mass[j] / D.orho[j];
+            const R vv = vj * vj;
+            const bool solid = D.fixed[j];
+            if (solid) vos = vos + vv * W;
+            vtot = vtot + vv * W;
+            if (solid) {
+                const R rh = r + (R)0.001 * h;
+                nw0 = nw0 + vv * dx0 * dWdr / rh;
+                nw1 = nw1 + vv * dx1 * dWdr / rh;
+                nw2 = nw2 + vv * dx2 * dWdr / rh;
+            }
+        }
+        nw0 = nw0 / vtot;
+        nw1 = nw1 / vtot;
+        nw2 = nw2 / vtot;
+        const R nn = sqrt(nw0 * nw0 + nw1 * nw1 + nw2 * nw2);
+        const R n0 = -nw0 / nn, n1 = -nw1 / nn, n2 = -nw2 / nn;
+        const R phi = fabs(vos / vtot);
+        const R vdn = v.x * n0 + v.y * n1 + v.z * n2;
+        auto t = D.vt[i];
+        t.x = 0;
+        if (D.dim > 1) t.y = 0;
+        if (D.dim > 2) t.z = 0;
+        D.vt[i] = t;
+        if (phi >= (R)0.5) {                 // applyBoundaryVolumeFraction, model.cpp:316-329
+            const R mx = vdn > (R)0.0 ? vdn : (R)0.0;
+            v.x = -v.x + (R)2.0 * mx * n0;
+            if (D.dim > 1) v.y = -v.y + (R)2.0 * mx * n1;
+            if (D.dim > 2) v.z = -v.z + (R)2.0 * mx * n2;
+        }
+    }
+    D.vel[i] = v;
+    D.rho[i] = rho;
+}
+
+__global__ void sdpd_scan(const int* hist, int* start, int n) {
+    __shared__ int warp_sums[32];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int base = 0; base < n; base += blockDim.x) {
+        const int i = base + threadIdx.x;
+        const int v = i < n ? hist[i] : 0;
+        int incl = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(SP_FULL, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (lane == 31) warp_sums[wid] = incl;
+        __syncthreads();
+        if (wid == 0) {
+            int ws = lane < (int)(blockDim.x >> 5) ? warp_sums[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(SP_FULL, ws, o);
+                if (lane >= o) ws += t;
+            }
+            warp_sums[lane] = ws;
+        }
+        __syncthreads();
+        const int before = (wid > 0 ? warp_sums[wid - 1] : 0) + carry;
+        if (i < n) start[i] = before + incl - v;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry = before + incl;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) start[n] = carry;
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+struct SdpdState {
+    int prec = SP_PREC_F32;
+    int N = 0, dim = 0, step = 0, kcap = 48, stat = 0;
+    double h = 0, dt = 0, rho0 = 0, P0 = 0, g[3] = {0, 0, 0};
+    cudaStream_t st = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    std::vector<void*> allocs;
+    void *pos = nullptr, *vel = nullptr, *vt = nullptr, *F = nullptr, *Fbp = nullptr,
+         *pold = nullptr, *xs = nullptr, *rho = nullptr, *orho = nullptr, *mass = nullptr,
+         *nu = nullptr, *ndist = nullptr, *ndw = nullptr;
+    uint8_t* fixed = nullptr;
+    int *cell = nullptr, *order = nullptr, *start = nullptr, *hist = nullptr, *fill = nullptr,
+        *ncnt = nullptr, *nidx = nullptr, *flag = nullptr;
+    CellGrid grid{};
+};
+
+static bool sd_alloc(SdpdState* s, void** p, size_t bytes, std::string* err) {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *err = std::string("cudaMalloc (SDPD state): ") + cudaGetErrorString(e);
+        return false;
+    }
+    s->allocs.push_back(*p);
+    return true;
+}
+
+template <typename R>
+static SdpdDev<R> dev_view(SdpdState* s) {
+    using V = typename Vec4<R>::T;
+    SdpdDev<R> D{};
+    D.N = s->N;
+    D.dim = s->dim;
+    D.step = s->step;
+    D.stat = s->stat;
+    D.h = (R)s->h;
+    D.dt = (R)s->dt;
+    D.rho0 = (R)s->rho0;
+    D.P0 = (R)s->P0;
+    const R h = (R)s->h;
+    D.alpha = s->dim == 3 ? (R)105 / ((R)16 * (R)M_PI * h * h * h)
+            : s->dim == 2 ? (R)5 / ((R)M_PI * h * h) : h;
+    D.g0 = (R)s->g[0];
+    D.g1 = (R)s->g[1];
+    D.g2 = (R)s->g[2];
+    D.pos = (V*)s->pos; D.vel = (V*)s->vel; D.vt = (V*)s->vt; D.F = (V*)s->F; D.Fbp = (V*)s->Fbp;
+    D.pold = (V*)s->pold; D.xs = (V*)s->xs;
+    D.rho = (R*)s->rho; D.orho = (R*)s->orho; D.mass = (R*)s->mass; D.nu = (R*)s->nu;
+    D.fixed = s->fixed;
+    D.cell = s->cell; D.order = s->order; D.start = s->start; D.hist = s->hist; D.fill = s->fill;
+    D.ncnt = s->ncnt; D.nidx = s->nidx; D.ndist = (R*)s->ndist; D.ndw = (R*)s->ndw;
+    D.kcap = s->kcap;
+    D.g = s->grid;
+    D.flag = s->flag;
+    return D;
+}
+
+template <typename R>
+static bool upload(SdpdState* s, const sp_scenario& sc, std::string* err) {
+    using V = typename Vec4<R>::T;
+    const int N = sc.num_particles;
+    const size_t v4 = sizeof(V) * N, r1 = sizeof(R) * N;
+    void** four[] = {&s->pos, &s->vel, &s->vt, &s->F, &s->Fbp, &s->pold, &s->xs};
+    for (void** p : four)
+        if (!sd_alloc(s, p, v4, err)) return false;
+    void** ones[] = {&s->rho, &s->orho, &s->mass, &s->nu};
+    for (void** p : ones)
+        if (!sd_alloc(s, p, r1, err)) return false;
+    std::vector<V> pos(N), zero(N), vel(N);
+    std::vector<R> rho(N), mass(N), nu(N);
+    for (int i = 0; i < N; i++) {
+        pos[i].x = (R)sc.x[3 * i]; pos[i].y = (R)sc.x[3 * i + 1]; pos[i].z = (R)sc.x[3 * i + 2];
+        pos[i].w = 0;
+        zero[i].x = zero[i].y = zero[i].z = zero[i].w = 0;
+        vel[i] = zero[i];
+        if (sc.v) { vel[i].x = (R)sc.v[3 * i]; vel[i].y = (R)sc.v[3 * i + 1]; vel[i].z = (R)sc.v[3 * i + 2]; }
+        rho[i] = (R)sc.rho[i];
+        mass[i] = (R)sc.mass[i];
+        nu[i] = (R)sc.nu[i];
+    }
+    // F, Fbp, vt start at zero: the engine reads them before first writing
+    // them (particle.cpp:70-83), the oracle zero-initialises them
+    cudaMemcpyAsync(s->pos, pos.data(), v4, cudaMemcpyHostToDevice, s->st);
+    cudaMemcpyAsync(s->vel, vel.data(), v4, cudaMemcpyHostToDevice, s->st);
+    cudaMemcpyAsync(s->vt, zero.data(), v4, cudaMemcpyHostToDevice, s->st);
+    cudaMemcpyAsync(s->F, zero.data(), v4, cudaMemcpyHostToDevice, s->st);
+    cudaMemcpyAsync(s->Fbp, zero.data(), v4, cudaMemcpyHostToDevice, s->st);
+    cudaMemcpyAsync(s->rho, rho.data(), r1, cudaMemcpyHostToDevice, s->st);
+    cudaMemcpyAsync(s->orho, rho.data(), r1, cudaMemcpyHostToDevice, s->st);
+    cudaMemcpyAsync(s->mass, mass.data(), r1, cudaMemcpyHostToDevice, s->st);
+    cudaMemcpyAsync(s->nu, nu.data(), r1, cudaMemcpyHostToDevice, s->st);
+    if (!sd_alloc(s, &s->ndist, sizeof(R) * (size_t)N * s->kcap, err)) return false;
+    if (!sd_alloc(s, &s->ndw, sizeof(R) * (size_t)N * s->kcap, err)) return false;
+    cudaError_t e = cudaStreamSynchronize(s->st);
+    if (e != cudaSuccess) {
+        *err = std::string("SDPD upload: ") + cudaGetErrorString(e);
+        return false;
+    }
+    return true;
+}
+
+SdpdState* sdpd_create(const sp_scenario& sc, int precision, cudaStream_t st, std::string* err) {
+    SdpdState* s = new SdpdState();
+    s->prec = precision == SP_PREC_F64 ? SP_PREC_F64 : SP_PREC_F32;
+    s->N = sc.num_particles;
+    s->dim = sc.dimension;
+    s->h = sc.h;
+    s->dt = sc.dt;
+    s->rho0 = sc.rho0;
+    s->P0 = sc.P0;
+    s->stat = sc.static_domain ? 1 : 0;
+    for (int d = 0; d < 3; d++) s->g[d] = sc.gravity[d];
+    s->st = st;
+    cudaEventCreate(&s->e0);
+    cudaEventCreate(&s->e1);
+    // cell grid over the initial bounding box grown by 4h on every side;
+    // particles outside it fall into the edge cells (still exact, slower)
+    s->grid = make_grid(sc.x, s->N, s->dim, sc.h);
+    for (int d = 0; d < s->dim; d++) {
+        s->grid.lo[d] -= 4 * s->grid.cs;
+        s->grid.nc[d] += 8;
+    }
+    s->grid.ncell = s->grid.nc[0] * s->grid.nc[1] * s->grid.nc[2];
+    const int N = s->N;
+    bool ok = sd_alloc(s, (void**)&s->fixed, N, err) &&
+              sd_alloc(s, (void**)&s->cell, sizeof(int) * N, err) &&
+              sd_alloc(s, (void**)&s->order, sizeof(int) * N, err) &&
+              sd_alloc(s, (void**)&s->start, sizeof(int) * (s->grid.ncell + 1), err) &&
+              sd_alloc(s, (void**)&s->hist, sizeof(int) * s->grid.ncell, err) &&
+              sd_alloc(s, (void**)&s->fill, sizeof(int) * s->grid.ncell, err) &&
+              sd_alloc(s, (void**)&s->ncnt, sizeof(int) * N, err) &&
+              sd_alloc(s, (void**)&s->nidx, sizeof(int) * (size_t)N * s->kcap, err) &&
+              sd_alloc(s, (void**)&s->flag, sizeof(int), err);
+    if (ok) {
+        cudaMemcpyAsync(s->fixed, sc.fixed, N, cudaMemcpyHostToDevice, st);
+        cudaMemsetAsync(s->ncnt, 0, sizeof(int) * N, st);
+        ok = s->prec == SP_PREC_F64 ? upload<double>(s, sc, err) : upload<float>(s, sc, err);
+    }
+    if (!ok) {
+        sdpd_destroy(s);
+        return nullptr;
+    }
+    return s;
+}
+
+void sdpd_destroy(SdpdState* s) {
+    if (!s) return;
+    for (void* p : s->allocs) cudaFree(p);
+    if (s->e0) cudaEventDestroy(s->e0);
+    if (s->e1) cudaEventDestroy(s->e1);
+    delete s;
+}
+
+template <typename R>
+static int advance_t(SdpdState* s, int nsteps, double* ms, long long* launches, std::string* err) {
+    const int N = s->N, tb = 128, nb = (N + tb - 1) / tb;
+    cudaMemsetAsync(s->flag, 0, sizeof(int), s->st);
+    cudaEventRecord(s->e0, s->st);
+    long long l = 0;
+    for (int k = 0; k < nsteps; k++) {
+        SdpdDev<R> D = dev_view<R>(s);
+        cudaMemsetAsync(s->hist, 0, sizeof(int) * s->grid.ncell, s->st);
+        cudaMemsetAsync(s->fill, 0, sizeof(int) * s->grid.ncell, s->st);
+        sdpd_begin<R><<<nb, tb, 0, s->st>>>(D);
+        sdpd_scan<<<1, 1024, 0, s->st>>>(s->hist, s->start, s->grid.ncell);
+        sdpd_scatter<R><<<nb, tb, 0, s->st>>>(D);
+        sdpd_pairs<R, 48><<<nb, tb, 0, s->st>>>(D, s->step == 0 ? 1 : 0);
+        sdpd_corrector<R><<<nb, tb, 0, s->st>>>(D);
+        l += 5;
+        s->step++;
+    }
+    cudaEventRecord(s->e1, s->st);
+    int flag = 0;
+    cudaMemcpyAsync(&flag, s->flag, sizeof(int), cudaMemcpyDeviceToHost, s->st);
+    cudaError_t e = cudaStreamSynchronize(s->st);
+    if (e != cudaSuccess) {
+        *err = std::string("SDPD step: ") + cudaGetErrorString(e);
+        return SP_E_CUDA;
+    }
+    float t = 0;
+    cudaEventElapsedTime(&t, s->e0, s->e1);
+    *ms = t;
+    *launches = l;
+    if (flag & 1) {
+        *err = "SDPD: a particle has more neighbours than the list capacity (48)";
+        return SP_E_UNSUPPORTED;
+    }
+    if (flag & 2) {
+        *err = "SDPD: NaN/inf in particle state (particle.cpp:88-126)";
+        return SP_E_TRAJECTORY;
+    }
+    return SP_OK;
+}
+
+int sdpd_advance(SdpdState* s, int nsteps, double* ms, long long* launches, std::string* err) {
+    return s->prec == SP_PREC_F64 ? advance_t<double>(s, nsteps, ms, launches, err)
+                                  : advance_t<float>(s, nsteps, ms, launches, err);
+}
+
+template <typename R>
+static int get_state_t(SdpdState* s, double* x, double* v, double* rho, std::string* err) {
+    using V = typename Vec4<R>::T;
+    const int N = s->N;
+    std::vector<V> p(N), u(N);
+    std::vector<R> r(N);
+    cudaMemcpy(p.data(), s->pos, sizeof(V) * N, cudaMemcpyDeviceToHost);
+    cudaMemcpy(u.data(), s->vel, sizeof(V) * N, cudaMemcpyDeviceToHost);
+    cudaError_t e = cudaMemcpy(r.data(), s->rho, sizeof(R) * N, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+        *err = std::string("SDPD state copy: ") + cudaGetErrorString(e);
+        return SP_E_CUDA;
+    }
+    for (int i = 0; i < N; i++) {
+        if (x) { x[3 * i] = p[i].x; x[3 * i + 1] = p[i].y; x[3 * i + 2] = p[i].z; }
+        if (v) { v[3 * i] = u[i].x; v[3 * i + 1] = u[i].y; v[3 * i + 2] = u[i].z; }
+        if (rho) rho[i] = r[i];
+    }
+    return SP_OK;
+}
+
+int sdpd_get_state(SdpdState* s, double* x, double* v, double* rho, std::string* err) {
+    return s->prec == SP_PREC_F64 ? get_state_t<double>(s, x, v, rho, err)
+                                  : get_state_t<float>(s, x, v, rho, err);
+}
+
+template <typename R>
+static int copy_nbr_t(SdpdState* s, int kmax, int* count, int* idx, double* dist, double* dwdr,
+                      std::string* err) {
+    const int N = s->N, K = s->kcap;
+    std::vector<int> c(N), ix((size_t)N * K);
+    std::vector<R> d((size_t)N * K), w((size_t)N * K);
+    cudaMemcpy(c.data(), s->ncnt, sizeof(int) * N, cudaMemcpyDeviceToHost);
+    cudaMemcpy(ix.data(), s->nidx, sizeof(int) * ix.size(), cudaMemcpyDeviceToHost);
+    cudaMemcpy(d.data(), s->ndist, sizeof(R) * d.size(), cudaMemcpyDeviceToHost);
+    cudaError_t e = cudaMemcpy(w.data(), s->ndw, sizeof(R) * w.size(), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+        *err = std::string("SDPD list copy: ") + cudaGetErrorString(e);
+        return SP_E_CUDA;
+    }
+    for (int i = 0; i < N; i++) {
+        if (c[i] > kmax) {
+            *err = "kmax smaller than a neighbour count";
+            return SP_E_INVALID;
+        }
+        count[i] = c[i];
+        for (int k = 0; k < c[i]; k++) {
+            idx[(size_t)i * kmax + k] = ix[(size_t)i * K + k];
+            if (dist) dist[(size_t)i * kmax + k] = d[(size_t)i * K + k];
+            if (dwdr) dwdr[(size_t)i * kmax + k] = w[(size_t)i * K + k];
+        }
+    }
+    return SP_OK;
+}
+
+int sdpd_copy_neighbors(SdpdState* s, int kmax, int* count, int* idx, double* dist, double* dwdr,
+                        double* dij, std::string* err) {
+    (void)dij;
+    return s->prec == SP_PREC_F64 ? copy_nbr_t<double>(s, kmax, count, idx, dist, dwdr, err)
+                                  : copy_nbr_t<float>(s, kmax, count, idx, dist, dwdr, err);
+}
+
 }  // namespace spg

@@ -80,16 +80,7 @@ class Engine:
             raise EngineError(rc, self.error())
 
     # -- runs ----------------------------------------------------------------
-    def run(self, seeds, instance=None, selection: int = abi.SP_SELECT_EXACT,
-            want_counts: bool = True, want_moments: bool = False, u0=None,
-            timeout: float | None = None):
-        """Run one trajectory per seed.
-
-        Returns a dict with ``counts`` (list per trajectory of [T,N,S] int32
-        arrays) when ``want_counts``, ``moments`` (list per instance of
-        [T,N,S,2] int64 sums of x and x^2) when ``want_moments``, ``events``
-        ([ntraj,2] reaction/diffusion counts) and ``status`` codes.
-        """
+    def _prepare(self, seeds, instance, selection, want_counts, want_moments, u0, timeout):
         seeds = np.ascontiguousarray(seeds, dtype=np.uint64).reshape(-1)
         nt = seeds.shape[0]
         inst = None
@@ -124,28 +115,76 @@ class Engine:
         out.counts = ptr(counts if want_counts else None, C.c_int32)
         out.moments = ptr(moments if want_moments else None, C.c_int64)
         out.event_counts = ptr(events, C.c_int64)
-        rc = self.lib.sp_run(self._h, C.byref(args), C.byref(out))
+        # keep every buffer the C side points at alive for the run
+        self._run = dict(seeds=seeds, inst=inst, u0s=u0s, u0p=u0p, args=args, out=out, T=T,
+                         idx=idx, sizes=sizes, counts=counts, msizes=msizes, moments=moments,
+                         events=events, want_counts=want_counts, want_moments=want_moments)
+        return self._run
+
+    def _collect(self, rc):
+        r = self._run
+        nt = r["seeds"].shape[0]
         status = np.array([self.status(j)["code"] for j in range(nt)], np.int32)
         if rc not in (abi.SP_OK, abi.SP_E_TRAJECTORY, abi.SP_E_TIMEOUT):
             raise EngineError(rc, self.error())
-        res = {"events": events, "status": status, "rc": rc}
+        res = {"events": r["events"], "status": status, "rc": rc}
         if rc != abi.SP_OK:
             res["error"] = self.error()
-        if want_counts:
+        T = r["T"]
+        if r["want_counts"]:
             parts, o = [], 0
-            for j, i in enumerate(idx):
+            for j, i in enumerate(r["idx"]):
                 sc = self.scenarios[i]
-                parts.append(counts[o:o + sizes[j]].reshape(T[i], sc.num_particles, sc.num_species))
-                o += sizes[j]
+                n = r["sizes"][j]
+                parts.append(r["counts"][o:o + n].reshape(T[i], sc.num_particles, sc.num_species))
+                o += n
             res["counts"] = parts
-        if want_moments:
+        if r["want_moments"]:
             parts, o = [], 0
             for i, sc in enumerate(self.scenarios):
-                parts.append(moments[2 * o:2 * (o + msizes[i])].reshape(
+                n = r["msizes"][i]
+                parts.append(r["moments"][2 * o:2 * (o + n)].reshape(
                     T[i], sc.num_particles, sc.num_species, 2))
-                o += msizes[i]
+                o += n
             res["moments"] = parts
         return res
+
+    def run(self, seeds, instance=None, selection: int = abi.SP_SELECT_EXACT,
+            want_counts: bool = True, want_moments: bool = False, u0=None,
+            timeout: float | None = None):
+        """Run one trajectory per seed over the whole time span.
+
+        Returns a dict with ``counts`` (list per trajectory of [T,N,S] int32
+        arrays) when ``want_counts``, ``moments`` (list per instance of
+        [T,N,S,2] int64 sums of x and x^2) when ``want_moments``, ``events``
+        ([ntraj,2] reaction/diffusion counts) and ``status`` codes.
+        """
+        r = self._prepare(seeds, instance, selection, want_counts, want_moments, u0, timeout)
+        rc = self.lib.sp_run(self._h, C.byref(r["args"]), C.byref(r["out"]))
+        return self._collect(rc)
+
+    def start(self, seeds, instance=None, selection: int = abi.SP_SELECT_EXACT,
+              want_counts: bool = False, want_moments: bool = False, u0=None,
+              timeout: float | None = None):
+        """Begin a run (queues built, outputs at step 0 written); see advance/finish."""
+        r = self._prepare(seeds, instance, selection, want_counts, want_moments, u0, timeout)
+        self._check(self.lib.sp_run_start(self._h, C.byref(r["args"]), C.byref(r["out"])))
+
+    def advance(self, num_outputs: int = 1) -> int:
+        """Advance the run through the next ``num_outputs`` outputs."""
+        rc = self.lib.sp_run_continue(self._h, int(num_outputs))
+        if rc not in (abi.SP_OK,):
+            raise EngineError(rc, self.error())
+        return rc
+
+    def finish(self):
+        rc = self.lib.sp_run_finish(self._h)
+        return self._collect(rc)
+
+    def profile(self) -> dict:
+        p = abi.SpProfile()
+        self._check(self.lib.sp_last_profile(self._h, C.byref(p)))
+        return {"total_ms": p.total_ms, "kernel_ms": p.kernel_ms, "launches": p.launches}
 
     def status(self, j: int) -> dict:
         st = SpTrajStatus()

@@ -1,0 +1,95 @@
+"""CPU tests of the C ABI boundary: libspgpu.so builds for sm_103a, loads,
+exports every entry point declared in include/spgpu.h, its structures match
+the ctypes mirror byte for byte, and argument errors are reported before any
+device call."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from spatialpy_gb300 import abi
+from spatialpy_gb300 import scenario as S
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "spgpu.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(sp_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_every_declared_symbol_is_exported(spgpu_lib):
+    names = declared_functions()
+    assert set(names) == set(abi.EXPORTED_SYMBOLS), names
+    out = subprocess.run(["nm", "-D", "--defined-only", abi.LIB_PATH], capture_output=True,
+                         text=True).stdout
+    exported = set(re.findall(r"\bT (sp_[a-z_0-9]+)", out))
+    for n in names:
+        assert n in exported, n
+        assert hasattr(spgpu_lib, n)
+    assert spgpu_lib.sp_abi_version() == abi.ABI_VERSION
+
+
+STRUCTS = {"sp_scenario": abi.SpScenario, "sp_options": abi.SpOptions,
+           "sp_run_args": abi.SpRunArgs, "sp_outputs": abi.SpOutputs,
+           "sp_traj_status": abi.SpTrajStatus, "sp_profile": abi.SpProfile}
+
+
+def test_struct_layout_matches_header(tmp_path):
+    lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"',
+             "int main(void) {"]
+    for cname, py in STRUCTS.items():
+        lines.append(f'printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", str(src), "-o", str(exe)], check=True)
+    got = {}
+    for ln in subprocess.run([str(exe)], capture_output=True, text=True).stdout.splitlines():
+        cname, field, val = ln.split()
+        got[(cname, field)] = int(val)
+    for cname, py in STRUCTS.items():
+        assert got[(cname, "sizeof")] == C.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
+
+
+def _create(lib, sc):
+    s = (abi.SpScenario * 1)()
+    s[0] = abi.scenario_struct(sc)
+    h = C.c_void_p()
+    rc = lib.sp_create(s, 1, None, C.byref(h))
+    msg = lib.sp_last_error(h).decode()
+    lib.sp_destroy(h)
+    return rc, msg
+
+
+@pytest.mark.parametrize("mutate,needle", [
+    (lambda sc: sc.type.__setitem__(0, 5), "type"),
+    (lambda sc: setattr(sc, "h", 0.0), "h (basis function width)"),
+    (lambda sc: sc.rho.__setitem__(3, 0.0), "Rho"),
+    (lambda sc: sc.output_steps.__setitem__(1, 0), "output steps"),
+    (lambda sc: sc.rxn_reactants.__setitem__((1, 0), 7), "reactant"),
+])
+def test_argument_errors_before_device_calls(spgpu_lib, mutate, needle):
+    sc = S.config_birth_death_2d()
+    mutate(sc)
+    rc, msg = _create(spgpu_lib, sc)
+    assert rc == abi.SP_E_INVALID
+    assert needle in msg
+
+
+def test_null_arguments(spgpu_lib):
+    h = C.c_void_p()
+    assert spgpu_lib.sp_create(None, 1, None, C.byref(h)) == abi.SP_E_INVALID
+    assert spgpu_lib.sp_run(None, None, None) == abi.SP_E_INVALID
+    assert spgpu_lib.sp_status(None, 0, None) == abi.SP_E_INVALID
+    spgpu_lib.sp_destroy(None)

@@ -68,6 +68,67 @@ def test_trajectories_bitexact_vs_oracle(oracle_lib, case, selection):
         np.testing.assert_array_equal(res["events"][j], ev)
 
 
+def _wide_model():
+    """10 species, 12 reactions: runs the generic (shared-table) kernel."""
+    sc = S.config_birth_death_2d(n=5, count=0, t_end=3.0, num_points=4)
+    sp = [f"X{i}" for i in range(10)]
+    rx = [(2.0, {}, {"X0": 1}, None)]
+    for i in range(9):
+        rx.append((0.5, {f"X{i}": 1}, {f"X{i+1}": 1}, None))
+    rx.append((0.01, {"X9": 2}, {"X0": 1}, None))
+    rx.append((0.002, {"X3": 1, "X7": 1}, {}, None))
+    rate, kind, reac, allowed, jcN, irN, prN = S.mass_action(sp, rx, 1)
+    u0 = np.zeros((sc.num_particles, 10), np.uint32)
+    u0[:, 0] = 3
+    u0[7, 5] = 20
+    return sc.copy(species=sp, rxn_rate=rate, rxn_kind=kind, rxn_reactants=reac,
+                   rxn_allowed=allowed, jcN=jcN, irN=irN, prN=prN,
+                   diffusion=np.linspace(0.05, 0.5, 10).reshape(10, 1), u0=u0, name="wide")
+
+
+@pytest.mark.parametrize("variant", [0, 1])
+@pytest.mark.parametrize("case", ["rdme3d_6", "dimer", "wide"])
+def test_kernel_variants_bitexact(oracle_lib, case, variant):
+    sc = _wide_model() if case == "wide" else CASES[case]()
+    seeds = np.arange(4, dtype=np.uint64) + 424242
+    with _engine(sc, nsm_variant=variant) as eng:
+        res = eng.run(seeds, selection=abi.SP_SELECT_EXACT)
+    assert res["rc"] == abi.SP_OK, res.get("error")
+    for j, s in enumerate(seeds):
+        out, ev, _ = oracle_lib.nsm_trajectory(sc, int(s), 0)
+        np.testing.assert_array_equal(res["counts"][j], out)
+        np.testing.assert_array_equal(res["events"][j], ev)
+
+
+def test_stepwise_run_equals_run():
+    sc = S.config_rdme_3d(n=6, nA=300, nB=300, t_end=10.0, num_points=11)
+    seeds = np.arange(16, dtype=np.uint64) + 5
+    with _engine(sc) as eng:
+        a = eng.run(seeds, want_moments=True)
+        eng.start(seeds, want_counts=True, want_moments=True)
+        for _ in range(10):
+            eng.advance(1)
+        b = eng.finish()
+    for x, y in zip(a["counts"], b["counts"]):
+        np.testing.assert_array_equal(x, y)
+    np.testing.assert_array_equal(a["moments"][0], b["moments"][0])
+    np.testing.assert_array_equal(a["events"], b["events"])
+
+
+def test_budget_exhaustion_resumes_exactly(oracle_lib):
+    """A tiny per-launch event budget forces many resumable exits
+    (SP_TRAJ_BUDGET_EXHAUSTED); the host relaunches and the trajectory is
+    unchanged."""
+    sc = S.config_birth_death_2d(n=6, count=50, t_end=3.0, num_points=4)
+    seeds = np.arange(3, dtype=np.uint64) + 77
+    with _engine(sc, event_budget=17) as eng:
+        res = eng.run(seeds)
+    assert res["rc"] == abi.SP_OK
+    for j, s in enumerate(seeds):
+        out, ev, _ = oracle_lib.nsm_trajectory(sc, int(s), 0)
+        np.testing.assert_array_equal(res["counts"][j], out)
+
+
 def test_uneven_batch_bitexact(oracle_lib):
     scs = [S.config_birth_death_2d(n=7, count=30),
            S.config_birth_death_2d(n=23, count=300, k_birth=3.0),
