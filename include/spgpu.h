@@ -120,8 +120,12 @@ typedef struct sp_scenario {
 typedef struct sp_options {
     int32_t device;               /* CUDA device ordinal */
     int32_t sdpd_precision;       /* SP_PREC_F32 (default) or SP_PREC_F64 */
-    int32_t nsm_variant;          /* 0 = chosen per run (register-resident network when
-                                     S <= 8 and R <= 16), 1 = generic warp kernel */
+    int32_t nsm_variant;          /* 0 = chosen per run: register-resident network when
+                                     S <= 8 and R <= 16, speculative 32-event batches
+                                     when every domain has >= 2,048 voxels;
+                                     1 = generic sequential warp kernel;
+                                     2 = speculative batches wherever supported;
+                                     3 = sequential register kernel */
     int32_t reserved;
     int64_t event_budget;         /* max events per trajectory per launch (0 = default) */
 } sp_options;
@@ -164,6 +168,8 @@ typedef struct sp_traj_status {
     int32_t voxel;                /* voxel of the failing event, -1 if none */
     double  time;                 /* simulation time reached */
     int64_t events;               /* events executed */
+    int64_t batches;              /* speculative batches run (0 for sequential kernels) */
+    int64_t candidates;           /* candidate events examined by those batches */
 } sp_traj_status;
 
 typedef struct sp_handle sp_handle;

@@ -120,6 +120,8 @@ class SpTrajStatus(C.Structure):
         ("voxel", C.c_int32),
         ("time", C.c_double),
         ("events", C.c_int64),
+        ("batches", C.c_int64),
+        ("candidates", C.c_int64),
     ]
 
 

@@ -22,6 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 UNITS = {
     "engine.cu": [],
     "nsm.cu": ["-fmad=false"],
+    "nsm_batch.cu": ["-fmad=false"],
     "neighbors.cu": ["-fmad=false"],
     "sdpd.cu": ["-fmad=false"],
 }

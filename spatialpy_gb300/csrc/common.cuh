@@ -163,6 +163,7 @@ struct NsmInstance {
     const int32_t* nbr_cnt;           // [N]
     const int32_t* nbr_idx;           // [N*K]
     const float* cdf;                 // [N*S*K] running sums of D(s,type_j) D_ij
+    const int2* cdfj;                 // [N*S*K] (running sum as float bits, neighbour index)
     const float* ddiag;               // [N*S]
     const float* rate;                // [R] rate constants rounded to float
     const int32_t* kind;              // [R]
@@ -187,6 +188,11 @@ struct NsmTraj {
     long long* leaf;                  // [leaf_stride] next-event times (double bits)
     long long* node_t;                // [num_nodes] tree times, levels >= 1
     int32_t* node_i;                  // [num_nodes] tree voxel indices
+    long long* node_t2;               // [level_size[1]] second-smallest leaf time per group
+    double a_tot;                     // running sum of all voxel propensities (batch horizon)
+    float bscale;                     // events aimed for per batch horizon (adapted)
+    int32_t pad2;
+    int64_t nbatch, ncand;            // speculative batches and their candidates
 };
 
 }  // namespace spg

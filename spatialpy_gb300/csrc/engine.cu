@@ -26,6 +26,11 @@ void launch_nsm_advance(bool ref, bool smem_state, int variant, int warp_smem, i
                         NsmTraj* trajs, const NsmInstance* insts, int ntraj, int step_end,
                         double dt, long long budget, long long max_ns, int* work, int num_sms,
                         cudaStream_t st);
+int nsm_batch_smem(const NsmInstance& d);
+void launch_nsm_batch(bool ref, int variant, int warp_smem, NsmTraj* trajs,
+                      const NsmInstance* insts, int ntraj, int step_end, double dt,
+                      long long budget, long long max_ns, int* work, int num_sms,
+                      cudaStream_t st);
 void launch_nsm_snapshot(const NsmTraj* trajs, const NsmInstance* insts, int ntraj,
                          int32_t* counts, const long long* count_off, long long* moments,
                          const long long* mom_off, int out_index, cudaStream_t st);
@@ -53,6 +58,7 @@ struct Instance {
     int *nbr_cnt = nullptr, *nbr_idx = nullptr;
     double *nbr_dist = nullptr, *nbr_dwdr = nullptr, *nbr_dij = nullptr;
     float *cdf = nullptr, *ddiag = nullptr, *rate = nullptr;
+    int2* cdfj = nullptr;
     double* diffusion = nullptr;
     int *kind = nullptr, *reac = nullptr, *jcN = nullptr, *irN = nullptr, *prN = nullptr;
     uint8_t* allowed = nullptr;
@@ -70,7 +76,7 @@ struct RunState {
     std::vector<int> inst;
     std::vector<void*> tmp;
     std::chrono::steady_clock::time_point wall0;
-    bool smem_state = false, want_counts = false, want_mom = false;
+    bool smem_state = false, want_counts = false, want_mom = false, batch = false;
     int warp_smem = 0, wpb = 1, variant = 0, next_out = 0, result = SP_OK;
     long long ctot = 0, mtot = 0;
     int32_t* d_counts = nullptr;
@@ -282,8 +288,9 @@ static int setup_instance(sp_handle* h, const sp_scenario& s, Instance& I) {
         if (S > 0) {
             if ((rc = dev_alloc(h, &I.ddiag, (size_t)N * S))) return rc;
             if ((rc = dev_alloc(h, &I.cdf, (size_t)N * S * I.K))) return rc;
+            if ((rc = dev_alloc(h, &I.cdfj, (size_t)N * S * I.K))) return rc;
             launch_diffusion_tables(N, S, T, I.K, I.type, I.nbr_cnt, I.nbr_idx, I.nbr_dij,
-                                    I.diffusion, I.ddiag, I.cdf, h->st);
+                                    I.diffusion, I.ddiag, I.cdf, I.cdfj, h->st);
             SP_CUDA_TRY(cudaGetLastError());
         }
     } else {
@@ -303,6 +310,7 @@ static int setup_instance(sp_handle* h, const sp_scenario& s, Instance& I) {
     d.nbr_cnt = I.nbr_cnt;
     d.nbr_idx = I.nbr_idx;
     d.cdf = I.cdf;
+    d.cdfj = I.cdfj;
     d.ddiag = I.ddiag;
     d.rate = I.rate;
     d.kind = I.kind;
@@ -375,6 +383,7 @@ static int ensure_traj(sp_handle* h, int ntraj, const int* inst) {
         bytes += align(sizeof(long long) * (size_t)d.leaf_stride);
         bytes += align(sizeof(long long) * (size_t)d.num_nodes);
         bytes += align(sizeof(int32_t) * (size_t)d.num_nodes);
+        bytes += align(sizeof(long long) * (size_t)d.level_size[1]);
     }
     if (bytes > h->traj_bytes) {
         if (h->traj_mem) cudaFree(h->traj_mem);
@@ -398,6 +407,8 @@ static int ensure_traj(sp_handle* h, int ntraj, const int* inst) {
         T.node_t = (long long*)p;
         p += align(sizeof(long long) * (size_t)d.num_nodes);
         T.node_i = (int32_t*)p;
+        p += align(sizeof(int32_t) * (size_t)d.num_nodes);
+        T.node_t2 = (long long*)p;
     }
     return SP_OK;
 }
@@ -448,6 +459,9 @@ int sp_run_start(sp_handle* h, const sp_run_args* a, sp_outputs* out) {
         T.evn = 0;
         T.nrx = T.ndf = 0;
         T.t_last = 0.0;
+        T.a_tot = 0.0;
+        T.bscale = 20.0f;
+        T.nbatch = T.ncand = 0;
     }
     cudaStream_t st = h->st;
     R.active = true;
@@ -515,6 +529,17 @@ int sp_run_start(sp_handle* h, const sp_run_args* a, sp_outputs* out) {
     else if (maxT < 64 && maxS <= 4 && maxR <= 8) R.variant = 1;
     else if (maxT < 64 && maxS <= 8 && maxR <= 16) R.variant = 2;
     if (h->opt.nsm_variant == 1) R.variant = 0;   // force the generic warp kernel
+    // speculative batches for domains of >= 2,048 voxels (64 voxel groups)
+    // with register-resident networks; forced by nsm_variant == 2
+    int minN = 1 << 30, batch_smem = 0;
+    for (int j = 0; j < ntraj; j++) {
+        minN = std::min(minN, h->inst[R.inst[j]].N);
+        batch_smem = std::max(batch_smem, nsm_batch_smem(h->inst[R.inst[j]].desc));
+    }
+    R.batch = R.variant != 0 && batch_smem <= 200 * 1024 &&
+              (h->opt.nsm_variant == 2 || (h->opt.nsm_variant == 0 && minN >= 2048));
+    // nsm_variant == 3: sequential register kernel only
+    if (R.batch) R.warp_smem = batch_smem;
     launch_nsm_init(h->d_trajs, h->d_insts, ntraj, max_leaf, max_levels, d_u0, st);
     h->launches += 2 + max_levels;
     // output buffers
@@ -575,9 +600,13 @@ int sp_run_continue(sp_handle* h, int32_t num_outputs) {
             if (done >= num_outputs) break;
             for (;;) {
                 cudaEventRecord(h->ea, st);
-                launch_nsm_advance(ref, R.smem_state, R.variant, R.warp_smem, R.wpb, h->d_trajs,
-                                   h->d_insts, ntraj, target, h->dt, budget, max_ns, h->d_work,
-                                   h->num_sms, st);
+                if (R.batch)
+                    launch_nsm_batch(ref, R.variant, R.warp_smem, h->d_trajs, h->d_insts, ntraj,
+                                     target, h->dt, budget, max_ns, h->d_work, h->num_sms, st);
+                else
+                    launch_nsm_advance(ref, R.smem_state, R.variant, R.warp_smem, R.wpb, h->d_trajs,
+                                       h->d_insts, ntraj, target, h->dt, budget, max_ns, h->d_work,
+                                       h->num_sms, st);
                 cudaEventRecord(h->eb, st);
                 h->launches++;
                 cudaError_t e = cudaGetLastError();
@@ -701,6 +730,8 @@ int sp_status(sp_handle* h, int32_t traj, sp_traj_status* st) {
     st->voxel = T.err_voxel;
     st->time = T.t_last;
     st->events = T.nrx + T.ndf;
+    st->batches = T.nbatch;
+    st->candidates = T.ncand;
     return SP_OK;
 }
 

@@ -161,7 +161,7 @@ __global__ void neighbor_search_f64(const double* xq, const double* xt, int n, C
 // accumulated in double in list order and rounded to float.
 __global__ void diffusion_tables(int n, int S, int T, int kmax, const int* type, const int* count,
                                  const int* idx, const double* dij, const double* diffusion,
-                                 float* ddiag, float* cdf) {
+                                 float* ddiag, float* cdf, int2* cdfj) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n * S) return;
     const int i = e / S, s = e % S;
@@ -170,7 +170,9 @@ __global__ void diffusion_tables(int n, int S, int T, int kmax, const int* type,
         const int j = idx[(size_t)i * kmax + k];
         const double dc = diffusion[s * T + (type[j] - 1)];
         acc = acc + dc * dij[(size_t)i * kmax + k];
-        cdf[((size_t)i * S + s) * kmax + k] = (float)acc;
+        const size_t o = ((size_t)i * S + s) * kmax + k;
+        cdf[o] = (float)acc;
+        cdfj[o] = make_int2(__float_as_int((float)acc), j);
     }
     ddiag[e] = (float)acc;
 }
@@ -237,10 +239,10 @@ int run_neighbor_search(const double* d_xq, const double* d_xt, int n, const Cel
 
 void launch_diffusion_tables(int n, int S, int T, int kmax, const int* d_type, const int* d_count,
                              const int* d_idx, const double* d_dij, const double* d_diffusion,
-                             float* d_ddiag, float* d_cdf, cudaStream_t st) {
+                             float* d_ddiag, float* d_cdf, int2* d_cdfj, cudaStream_t st) {
     const int e = n * S;
     diffusion_tables<<<(e + 255) / 256, 256, 0, st>>>(n, S, T, kmax, d_type, d_count, d_idx, d_dij,
-                                                      d_diffusion, d_ddiag, d_cdf);
+                                                      d_diffusion, d_ddiag, d_cdf, d_cdfj);
 }
 
 }  // namespace spg

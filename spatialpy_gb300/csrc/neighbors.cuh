@@ -20,6 +20,6 @@ int run_neighbor_search(const double* d_xq, const double* d_xt, int n, const Cel
                         int* d_order, int* d_flag, cudaStream_t st);
 void launch_diffusion_tables(int n, int S, int T, int kmax, const int* d_type, const int* d_count,
                              const int* d_idx, const double* d_dij, const double* d_diffusion,
-                             float* d_ddiag, float* d_cdf, cudaStream_t st);
+                             float* d_ddiag, float* d_cdf, int2* d_cdfj, cudaStream_t st);
 
 }  // namespace spg

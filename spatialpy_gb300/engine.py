@@ -189,7 +189,8 @@ class Engine:
     def status(self, j: int) -> dict:
         st = SpTrajStatus()
         self._check(self.lib.sp_status(self._h, j, C.byref(st)))
-        return {"code": st.code, "voxel": st.voxel, "time": st.time, "events": st.events}
+        return {"code": st.code, "voxel": st.voxel, "time": st.time, "events": st.events,
+                "batches": st.batches, "candidates": st.candidates}
 
     def last_timing(self):
         ms = C.c_double()

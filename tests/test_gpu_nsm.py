@@ -86,8 +86,8 @@ def _wide_model():
                    diffusion=np.linspace(0.05, 0.5, 10).reshape(10, 1), u0=u0, name="wide")
 
 
-@pytest.mark.parametrize("variant", [0, 1])
-@pytest.mark.parametrize("case", ["rdme3d_6", "dimer", "wide"])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+@pytest.mark.parametrize("case", ["rdme3d_6", "dimer", "wide", "birth_death", "restricted"])
 def test_kernel_variants_bitexact(oracle_lib, case, variant):
     sc = _wide_model() if case == "wide" else CASES[case]()
     seeds = np.arange(4, dtype=np.uint64) + 424242
@@ -98,6 +98,38 @@ def test_kernel_variants_bitexact(oracle_lib, case, variant):
         out, ev, _ = oracle_lib.nsm_trajectory(sc, int(s), 0)
         np.testing.assert_array_equal(res["counts"][j], out)
         np.testing.assert_array_equal(res["events"][j], ev)
+
+
+@pytest.mark.parametrize("selection", [abi.SP_SELECT_EXACT, abi.SP_SELECT_REFERENCE])
+@pytest.mark.parametrize("n,dims", [(16, 3), (64, 2)])
+def test_batch_kernel_bitexact_large_domain(oracle_lib, n, dims, selection):
+    """Speculative 32-event batches on 4,096-voxel domains equal the
+    sequential oracle event for event (both selection rules)."""
+    t_end = 2.0 if dims == 3 else 0.2
+    sc = S.config_rdme_3d(n=n, nA=3000, nB=2500, t_end=t_end, num_points=5, dt=t_end / 4,
+                          dims=dims)
+    seeds = np.arange(6, dtype=np.uint64) + 99173
+    with _engine(sc, nsm_variant=2) as eng:
+        res = eng.run(seeds, selection=selection)
+    assert res["rc"] == abi.SP_OK, res.get("error")
+    for j, s in enumerate(seeds):
+        out, ev, _ = oracle_lib.nsm_trajectory(sc, int(s), selection)
+        np.testing.assert_array_equal(res["events"][j], ev)
+        np.testing.assert_array_equal(res["counts"][j], out)
+
+
+def test_batch_kernel_birth_death_large():
+    sc = S.config_birth_death_2d(n=64, count=3000, k_birth=2000.0, D=1e-4, t_end=0.5,
+                                 num_points=3, dt=0.25)
+    seeds = np.arange(4, dtype=np.uint64) + 5
+
+    import oracle
+    with _engine(sc, nsm_variant=2) as eng:
+        res = eng.run(seeds)
+    for j, s in enumerate(seeds):
+        out, ev, _ = oracle.nsm_trajectory(sc, int(s), 0)
+        np.testing.assert_array_equal(res["events"][j], ev)
+        np.testing.assert_array_equal(res["counts"][j], out)
 
 
 def test_stepwise_run_equals_run():
