@@ -325,7 +325,19 @@ def main():
                     help="DRAM bytes per event of the event-loop kernel from an ncu capture")
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu: the bench workload over two 0.05 intervals")
+    ap.add_argument("--profile-sdpd", action="store_true",
+                    help="small case for ncu: 30 SDPD steps of the dam break (FP32)")
     args = ap.parse_args()
+    if args.profile_sdpd:
+        import __graft_entry__ as g
+        g.build()
+        from spatialpy_gb300 import scenario as S
+        from spatialpy_gb300.engine import Engine
+        sc = S.config_dam_break()
+        with Engine(sc, sdpd_precision="f32") as eng:
+            eng.sdpd_advance(30)
+            print("profile sdpd", eng.last_timing())
+        return
     if args.profile_case:
         import __graft_entry__ as g
         g.build()

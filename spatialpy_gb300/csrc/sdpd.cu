@@ -4,16 +4,17 @@
 // with the kd-tree of :80-108): take_step1 (src/simulate.cpp:56-109),
 // find_neighbors + pairwiseForce (particle.cpp:240-294, model.cpp:39-191),
 // take_step2 with filterDensity and the boundary volume fraction
-// (simulate.cpp:132-173, model.cpp:194-329).  Per step, five launches:
+// (simulate.cpp:132-173, model.cpp:194-329).  Per step, a memset and three
+// launches (replayed from a CUDA graph in blocks of 20 steps):
 //
-//   begin     cell key of each particle at its start-of-step position (the
-//             kd-tree points of the step), copy of that position, predictor
-//   scan      exclusive scan of the cell histogram (one block)
-//   scatter   counting-sort scatter: tree points in cell order
+//   begin     cell of each particle at its start-of-step position (the
+//             kd-tree points of the step): the index and position go into
+//             the cell's slots (fixed capacity, atomic slot counter); then
+//             the predictor
 //   pairs     per particle: neighbour list of the moved position against the
-//             tree points, sorted by (r^2, j); pressure, viscous,
-//             background-pressure and transport forces and the density rate
-//             summed in list order
+//             tree points, sorted by (r^2, j) in shared memory; pressure,
+//             viscous, background-pressure and transport forces and the
+//             density rate summed in list order
 //   corrector corrector, Shepard filter every 20 steps, boundary volume
 //             fraction and bounce-back
 //
@@ -50,16 +51,19 @@ template <typename R>
 struct SdpdDev {
     int N, dim, step, stat;
     R h, dt, rho0, P0, alpha, g0, g1, g2;
-    typename Vec4<R>::T *pos, *vel, *vt, *F, *Fbp, *pold, *xs;
+    typename Vec4<R>::T *pos, *vel, *vt, *F, *Fbp, *pold;
     R *rho, *orho, *mass, *nu;
     const uint8_t* fixed;
-    int *cell, *order, *start, *hist, *fill;
+    int *ccnt, *cidx;               // per cell: slot count, particle index [ncell][CAP]
+    typename Vec4<R>::T* cpos;      // per cell slot: start-of-step position
     int *ncnt, *nidx;
     R *ndist, *ndw;
     int kcap;
     CellGrid g;
-    int* flag;   // bit 1: list overflow, bit 2: NaN state
+    int* flag;   // bit 1: list overflow, bit 2: NaN state, bit 4: cell overflow
 };
+
+constexpr int kCellCap = 16;
 
 template <typename R>
 __device__ __forceinline__ int cellc(R p, const CellGrid& g, int d) {
@@ -84,8 +88,13 @@ __global__ void sdpd_begin(SdpdDev<R> D) {
         atomicOr(D.flag, 2);
     const int c = (cellc<R>(p.x, D.g, 0) * D.g.nc[1] + cellc<R>(p.y, D.g, 1)) * D.g.nc[2] +
                   cellc<R>(p.z, D.g, 2);
-    D.cell[i] = c;
-    atomicAdd(&D.hist[c], 1);
+    const int slot = atomicAdd(&D.ccnt[c], 1);
+    if (slot < kCellCap) {
+        D.cidx[c * kCellCap + slot] = i;
+        D.cpos[c * kCellCap + slot] = p;
+    } else {
+        atomicOr(D.flag, 4);
+    }
     D.pold[i] = p;
     if (!D.stat && !D.fixed[i]) {
         const auto F = D.F[i];
@@ -116,23 +125,18 @@ __global__ void sdpd_begin(SdpdDev<R> D) {
     D.orho[i] = rho;
 }
 
-template <typename R>
-__global__ void sdpd_scatter(SdpdDev<R> D) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= D.N) return;
-    const int c = D.cell[i];
-    const int slot = D.start[c] + atomicAdd(&D.fill[c], 1);
-    D.order[slot] = i;
-    D.xs[slot] = D.pold[i];
-}
-
 // find_neighbors against the step's tree points + pairwiseForce (model.cpp:39-191)
-template <typename R, int KCAP>
-__global__ void __launch_bounds__(128) sdpd_pairs(SdpdDev<R> D, int first_step) {
+template <typename R, int KCAP, int TB>
+__global__ void __launch_bounds__(TB) sdpd_pairs(SdpdDev<R> D, int first_step) {
+    // per-thread sorted candidate lists in shared memory, element k of
+    // thread t at [k * TB + t] (consecutive threads, consecutive banks)
+    __shared__ R sd2[KCAP * TB];
+    __shared__ int sj[KCAP * TB];
+    const int tid = threadIdx.x;
+    R* cd2 = sd2 + tid;
+    int* cj = sj + tid;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= D.N) return;
-    R cd2[KCAP];
-    int cj[KCAP];
     // at the first step of a run the lists come from the unmoved points (take_step1)
     const auto q = first_step ? D.pold[i] : D.pos[i];
     const R h = D.h, sq = h * h;
@@ -156,10 +160,11 @@ __global__ void __launch_bounds__(128) sdpd_pairs(SdpdDev<R> D, int first_step) 
             for (int c = c2 - 1; c <= c2 + 1; c++) {
                 if (c < 0 || c >= D.g.nc[2]) continue;
                 const int cid = (a * D.g.nc[1] + b) * D.g.nc[2] + c;
-                const int e = D.start[cid + 1];
-                for (int t = D.start[cid]; t < e; t++) {
-                    const int j = D.order[t];
-                    const auto p = D.xs[t];
+                int e = D.ccnt[cid];
+                e = e < kCellCap ? e : kCellCap;
+                for (int t = 0; t < e; t++) {
+                    const int j = D.cidx[cid * kCellCap + t];
+                    const auto p = D.cpos[cid * kCellCap + t];
                     R d2 = 0;
                     const R t0 = q.x - p.x;
                     d2 = d2 + t0 * t0;
@@ -170,13 +175,16 @@ __global__ void __launch_bounds__(128) sdpd_pairs(SdpdDev<R> D, int first_step) 
                     if (sqrt(d2) > h) continue;              // particle.cpp:160-162
                     if (m >= KCAP || m >= D.kcap) { over = true; continue; }
                     int k = m++;
-                    while (k > 0 && (d2 < cd2[k - 1] || (d2 == cd2[k - 1] && j < cj[k - 1]))) {
-                        cd2[k] = cd2[k - 1];
-                        cj[k] = cj[k - 1];
+                    while (k > 0) {
+                        const R pd = cd2[(k - 1) * TB];
+                        const int pj = cj[(k - 1) * TB];
+                        if (!(d2 < pd || (d2 == pd && j < pj))) break;
+                        cd2[k * TB] = pd;
+                        cj[k * TB] = pj;
                         k--;
                     }
-                    cd2[k] = d2;
-                    cj[k] = j;
+                    cd2[k * TB] = d2;
+                    cj[k * TB] = j;
                 }
             }
         }
@@ -192,8 +200,8 @@ __global__ void __launch_bounds__(128) sdpd_pairs(SdpdDev<R> D, int first_step) 
     const R Pi = P0 * (rhoi / rho0 - (R)1.0);
     R Fx = D.g0, Fy = D.g1, Fz = D.g2, Bx = 0, By = 0, Bz = 0, Fr = 0;
     for (int k = 0; k < m; k++) {
-        const int j = cj[k];
-        const R r = sqrt(cd2[k]);
+        const int j = cj[k * TB];
+        const R r = sqrt(cd2[k * TB]);
         const R R_ = r / h;
         const R dWdr = alpha * ((R)-12 * r / (h * h)) * (((R)1 - R_) * ((R)1 - R_));
         const size_t o = (size_t)i * D.kcap + k;
@@ -328,40 +336,6 @@ __global__ void sdpd_corrector(SdpdDev<R> D) {
     D.rho[i] = rho;
 }
 
-__global__ void sdpd_scan(const int* hist, int* start, int n) {
-    __shared__ int warp_sums[32];
-    __shared__ int carry;
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int base = 0; base < n; base += blockDim.x) {
-        const int i = base + threadIdx.x;
-        const int v = i < n ? hist[i] : 0;
-        int incl = v;
-        for (int o = 1; o < 32; o <<= 1) {
-            const int t = __shfl_up_sync(SP_FULL, incl, o);
-            if (lane >= o) incl += t;
-        }
-        if (lane == 31) warp_sums[wid] = incl;
-        __syncthreads();
-        if (wid == 0) {
-            int ws = lane < (int)(blockDim.x >> 5) ? warp_sums[lane] : 0;
-            for (int o = 1; o < 32; o <<= 1) {
-                const int t = __shfl_up_sync(SP_FULL, ws, o);
-                if (lane >= o) ws += t;
-            }
-            warp_sums[lane] = ws;
-        }
-        __syncthreads();
-        const int before = (wid > 0 ? warp_sums[wid - 1] : 0) + carry;
-        if (i < n) start[i] = before + incl - v;
-        __syncthreads();
-        if (threadIdx.x == blockDim.x - 1) carry = before + incl;
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) start[n] = carry;
-}
-
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -373,12 +347,12 @@ struct SdpdState {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     std::vector<void*> allocs;
     void *pos = nullptr, *vel = nullptr, *vt = nullptr, *F = nullptr, *Fbp = nullptr,
-         *pold = nullptr, *xs = nullptr, *rho = nullptr, *orho = nullptr, *mass = nullptr,
+         *pold = nullptr, *cpos = nullptr, *rho = nullptr, *orho = nullptr, *mass = nullptr,
          *nu = nullptr, *ndist = nullptr, *ndw = nullptr;
     uint8_t* fixed = nullptr;
-    int *cell = nullptr, *order = nullptr, *start = nullptr, *hist = nullptr, *fill = nullptr,
-        *ncnt = nullptr, *nidx = nullptr, *flag = nullptr;
+    int *ccnt = nullptr, *cidx = nullptr, *ncnt = nullptr, *nidx = nullptr, *flag = nullptr;
     CellGrid grid{};
+    cudaGraphExec_t graph20 = nullptr;   // 20 steps starting at a multiple of 20 (>= 20)
 };
 
 static bool sd_alloc(SdpdState* s, void** p, size_t bytes, std::string* err) {
@@ -410,10 +384,10 @@ static SdpdDev<R> dev_view(SdpdState* s) {
     D.g1 = (R)s->g[1];
     D.g2 = (R)s->g[2];
     D.pos = (V*)s->pos; D.vel = (V*)s->vel; D.vt = (V*)s->vt; D.F = (V*)s->F; D.Fbp = (V*)s->Fbp;
-    D.pold = (V*)s->pold; D.xs = (V*)s->xs;
+    D.pold = (V*)s->pold; D.cpos = (V*)s->cpos;
     D.rho = (R*)s->rho; D.orho = (R*)s->orho; D.mass = (R*)s->mass; D.nu = (R*)s->nu;
     D.fixed = s->fixed;
-    D.cell = s->cell; D.order = s->order; D.start = s->start; D.hist = s->hist; D.fill = s->fill;
+    D.ccnt = s->ccnt; D.cidx = s->cidx;
     D.ncnt = s->ncnt; D.nidx = s->nidx; D.ndist = (R*)s->ndist; D.ndw = (R*)s->ndw;
     D.kcap = s->kcap;
     D.g = s->grid;
@@ -426,9 +400,10 @@ static bool upload(SdpdState* s, const sp_scenario& sc, std::string* err) {
     using V = typename Vec4<R>::T;
     const int N = sc.num_particles;
     const size_t v4 = sizeof(V) * N, r1 = sizeof(R) * N;
-    void** four[] = {&s->pos, &s->vel, &s->vt, &s->F, &s->Fbp, &s->pold, &s->xs};
+    void** four[] = {&s->pos, &s->vel, &s->vt, &s->F, &s->Fbp, &s->pold};
     for (void** p : four)
         if (!sd_alloc(s, p, v4, err)) return false;
+    if (!sd_alloc(s, &s->cpos, sizeof(V) * (size_t)s->grid.ncell * kCellCap, err)) return false;
     void** ones[] = {&s->rho, &s->orho, &s->mass, &s->nu};
     for (void** p : ones)
         if (!sd_alloc(s, p, r1, err)) return false;
@@ -489,11 +464,8 @@ SdpdState* sdpd_create(const sp_scenario& sc, int precision, cudaStream_t st, st
     s->grid.ncell = s->grid.nc[0] * s->grid.nc[1] * s->grid.nc[2];
     const int N = s->N;
     bool ok = sd_alloc(s, (void**)&s->fixed, N, err) &&
-              sd_alloc(s, (void**)&s->cell, sizeof(int) * N, err) &&
-              sd_alloc(s, (void**)&s->order, sizeof(int) * N, err) &&
-              sd_alloc(s, (void**)&s->start, sizeof(int) * (s->grid.ncell + 1), err) &&
-              sd_alloc(s, (void**)&s->hist, sizeof(int) * s->grid.ncell, err) &&
-              sd_alloc(s, (void**)&s->fill, sizeof(int) * s->grid.ncell, err) &&
+              sd_alloc(s, (void**)&s->ccnt, sizeof(int) * s->grid.ncell, err) &&
+              sd_alloc(s, (void**)&s->cidx, sizeof(int) * (size_t)s->grid.ncell * kCellCap, err) &&
               sd_alloc(s, (void**)&s->ncnt, sizeof(int) * N, err) &&
               sd_alloc(s, (void**)&s->nidx, sizeof(int) * (size_t)N * s->kcap, err) &&
               sd_alloc(s, (void**)&s->flag, sizeof(int), err);
@@ -511,6 +483,7 @@ SdpdState* sdpd_create(const sp_scenario& sc, int precision, cudaStream_t st, st
 
 void sdpd_destroy(SdpdState* s) {
     if (!s) return;
+    if (s->graph20) cudaGraphExecDestroy(s->graph20);
     for (void* p : s->allocs) cudaFree(p);
     if (s->e0) cudaEventDestroy(s->e0);
     if (s->e1) cudaEventDestroy(s->e1);
@@ -518,22 +491,49 @@ void sdpd_destroy(SdpdState* s) {
 }
 
 template <typename R>
-static int advance_t(SdpdState* s, int nsteps, double* ms, long long* launches, std::string* err) {
+static void enqueue_step(SdpdState* s, int step) {
     const int N = s->N, tb = 128, nb = (N + tb - 1) / tb;
+    SdpdDev<R> D = dev_view<R>(s);
+    D.step = step;
+    cudaMemsetAsync(s->ccnt, 0, sizeof(int) * s->grid.ncell, s->st);
+    sdpd_begin<R><<<nb, tb, 0, s->st>>>(D);
+    constexpr int TP = sizeof(R) == 4 ? 128 : 64;   // 48 KB of list slots per block
+    sdpd_pairs<R, 48, TP><<<(N + TP - 1) / TP, TP, 0, s->st>>>(D, step == 0 ? 1 : 0);
+    sdpd_corrector<R><<<nb, tb, 0, s->st>>>(D);
+}
+
+template <typename R>
+static int advance_t(SdpdState* s, int nsteps, double* ms, long long* launches, std::string* err) {
     cudaMemsetAsync(s->flag, 0, sizeof(int), s->st);
     cudaEventRecord(s->e0, s->st);
     long long l = 0;
-    for (int k = 0; k < nsteps; k++) {
-        SdpdDev<R> D = dev_view<R>(s);
-        cudaMemsetAsync(s->hist, 0, sizeof(int) * s->grid.ncell, s->st);
-        cudaMemsetAsync(s->fill, 0, sizeof(int) * s->grid.ncell, s->st);
-        sdpd_begin<R><<<nb, tb, 0, s->st>>>(D);
-        sdpd_scan<<<1, 1024, 0, s->st>>>(s->hist, s->start, s->grid.ncell);
-        sdpd_scatter<R><<<nb, tb, 0, s->st>>>(D);
-        sdpd_pairs<R, 48><<<nb, tb, 0, s->st>>>(D, s->step == 0 ? 1 : 0);
-        sdpd_corrector<R><<<nb, tb, 0, s->st>>>(D);
-        l += 5;
-        s->step++;
+    int k = 0;
+    while (k < nsteps) {
+        if (s->step >= 20 && s->step % 20 == 0 && nsteps - k >= 20) {
+            // steps only differ through step % 20 (Shepard filter) and the
+            // first step, so one captured block of 20 replays anywhere >= 20
+            if (!s->graph20) {
+                cudaGraph_t g;
+                cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal);
+                for (int q = 0; q < 20; q++) enqueue_step<R>(s, 20 + q);
+                cudaError_t e = cudaStreamEndCapture(s->st, &g);
+                if (e == cudaSuccess) e = cudaGraphInstantiate(&s->graph20, g, 0);
+                cudaGraphDestroy(g);
+                if (e != cudaSuccess) {
+                    *err = std::string("SDPD graph capture: ") + cudaGetErrorString(e);
+                    return SP_E_CUDA;
+                }
+            }
+            cudaGraphLaunch(s->graph20, s->st);
+            l += 60;
+            k += 20;
+            s->step += 20;
+        } else {
+            enqueue_step<R>(s, s->step);
+            l += 3;
+            k++;
+            s->step++;
+        }
     }
     cudaEventRecord(s->e1, s->st);
     int flag = 0;
@@ -549,6 +549,10 @@ static int advance_t(SdpdState* s, int nsteps, double* ms, long long* launches, 
     *launches = l;
     if (flag & 1) {
         *err = "SDPD: a particle has more neighbours than the list capacity (48)";
+        return SP_E_UNSUPPORTED;
+    }
+    if (flag & 4) {
+        *err = "SDPD: more than 16 particles in one cell of edge h";
         return SP_E_UNSUPPORTED;
     }
     if (flag & 2) {
