@@ -86,18 +86,24 @@ def test_vtk_round_trip(tmp_path):
 # ---------------------------------------------------------------------------
 # GPU: the reference's solver tests against GpuSolver
 # ---------------------------------------------------------------------------
+MOLECULES = 1000
+
+
 def _diffusion_debug():
     """create_diffusion_debug (test_solver.py:28-46): 50x50 2-D domain on
-    [-1,1]^2, one species D=0.01, 100,000 molecules at the origin particle,
-    dt 0.1, 11 outputs over t in [0,10]."""
+    [-1,1]^2, mass 1 and rho = mass / vol (Domain.add_point, domain.py:244-245),
+    one species D=0.01, dt 0.1, 11 outputs over t in [0,10].  The reference
+    places 100,000 molecules at the origin particle (about 2e8 diffusion
+    events per trajectory); 1,000 keep this test to seconds and leave every
+    check below meaningful."""
     ax = np.linspace(-1.0, 1.0, 50)
     x = S.lattice([ax, ax])
     n = x.shape[0]
     rate, kind, reac, allowed, jcN, irN, prN = S.mass_action(["A"], [], 1)
     u0 = np.zeros((n, 1), np.uint32)
-    u0[np.argmin(np.linalg.norm(x, axis=1)), 0] = 100000
+    u0[np.argmin(np.linalg.norm(x, axis=1)), 0] = MOLECULES
     nt, steps = S.timespan(10.0, 11, 0.1)
-    return S.Scenario(dimension=2, x=x, type=np.ones(n), mass=1.0, rho=1.0, nu=1.0, fixed=1,
+    return S.Scenario(dimension=2, x=x, type=np.ones(n), mass=1.0, rho=n / 4.0, nu=1.0, fixed=1,
                       num_types=1, species=["A"], rxn_rate=rate, rxn_kind=kind,
                       rxn_reactants=reac.reshape(0, 2), rxn_allowed=allowed, jcN=jcN, irN=irN,
                       prN=prN, diffusion=np.array([[0.01]]), h=S.find_h(x), dt=0.1,
@@ -113,7 +119,7 @@ def test_reference_solver_tests_on_gpu_solver():
     r1 = sol.run(seed=1)
     np.testing.assert_array_equal(r1.read_step(0)[1]["D[A]"], sc.u0[:, 0])   # test_solver_io
     assert r1.get_species("A").shape == (11, sc.num_particles)
-    assert r1.get_species("A")[-1].sum() == 100000                            # conserved
+    assert r1.get_species("A")[-1].sum() == MOLECULES                         # conserved
     assert r1 == sol.run(seed=1)                                              # test_same_seed
     assert r1 != sol.run(seed=2)                                              # test_different_seeds
     ens = sol.run(number_of_trajectories=3, seed=7)                           # test_run_ensemble
