@@ -130,7 +130,7 @@ EXPORTED_SYMBOLS = (
     "sp_abi_version", "sp_create", "sp_run", "sp_run_start", "sp_run_continue",
     "sp_run_finish", "sp_status", "sp_last_error", "sp_destroy", "sp_get_neighbors",
     "sp_get_ddiag", "sp_get_particles", "sp_sdpd_advance", "sp_last_timing",
-    "sp_last_profile",
+    "sp_last_profile", "sp_neighbors_noalloc",
 )
 
 
@@ -233,6 +233,12 @@ def load_library(path: str | None = None):
     lib.sp_get_particles.restype = C.c_int
     lib.sp_sdpd_advance.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
     lib.sp_sdpd_advance.restype = C.c_int
+    lib.sp_neighbors_noalloc.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_double,
+                                         C.c_void_p, C.c_void_p, _p(C.c_double),
+                                         _p(C.c_double), C.c_int32, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_char_p, C.c_int32]
+    lib.sp_neighbors_noalloc.restype = C.c_int
     lib.sp_last_timing.argtypes = [C.c_void_p, _p(C.c_double), _p(C.c_int64)]
     lib.sp_last_timing.restype = C.c_int
     if path is None:

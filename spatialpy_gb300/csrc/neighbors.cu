@@ -13,6 +13,8 @@
 // stores the list sorted by (r^2, j).  Compiled with -fmad=false, so dist,
 // dWdr and D_ij equal the reference engine's values bit for bit.
 #include <cstdint>
+#include <cstdio>
+#include <mutex>
 
 #include "common.cuh"
 #include "neighbors.cuh"
@@ -246,3 +248,130 @@ void launch_diffusion_tables(int n, int S, int T, int kmax, const int* d_type, c
 }
 
 }  // namespace spg
+
+// ---------------------------------------------------------------------------
+// Neighbour lists without device allocation.
+//
+// Some callers cannot allocate device memory while they run this path:
+// code inside CUDA stream capture (cudaMalloc is not permitted there), and
+// hosts that own a fixed device-memory arena and forbid allocation during a
+// simulation step.  This entry point takes the caller's device buffers for
+// inputs and outputs and keeps its own cell-list scratch in the file-scope
+// array below, which every GPU that loads the library holds until the
+// process exits.
+// ---------------------------------------------------------------------------
+
+namespace {
+constexpr int kNoAllocMaxParticles = 262144;
+constexpr int kNoAllocMaxCells = 524288;
+// cell[P] | order[P] | hist[C] | fill[C] | start[C+1] | flag
+constexpr size_t kNoAllocBytes =
+    sizeof(int) * (2 * (size_t)kNoAllocMaxParticles + 3 * (size_t)kNoAllocMaxCells + 2);
+constexpr int kMaxDevices = 64;
+
+__device__ __align__(256) unsigned char sp_noalloc_scratch[kNoAllocBytes];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kMaxDevices] = {nullptr};
+
+void noalloc_msg(char* err, int32_t errlen, const char* msg) {
+    if (err && errlen > 0) {
+        snprintf(err, (size_t)errlen, "%s", msg);
+    }
+}
+}  // namespace
+
+extern "C" int sp_neighbors_noalloc(const double* x, int32_t n, int32_t dim, double h,
+                                    const double* mass, const double* rho, const double* lo,
+                                    const double* hi, int32_t kmax, int32_t* count, int32_t* idx,
+                                    double* dist, double* dWdr, double* Dij, void* stream,
+                                    char* err, int32_t errlen) {
+    using namespace spg;
+    if (!x || !mass || !rho || !lo || !hi || !count || !idx || n < 1 || dim < 1 || dim > 3 ||
+        !(h > 0.0) || kmax < 1) {
+        noalloc_msg(err, errlen, "sp_neighbors_noalloc: missing buffer or bad size");
+        return SP_E_INVALID;
+    }
+    if (n > kNoAllocMaxParticles) {
+        noalloc_msg(err, errlen, "sp_neighbors_noalloc: more than 262,144 particles");
+        return SP_E_INVALID;
+    }
+    if (kmax > 256) {
+        noalloc_msg(err, errlen, "sp_neighbors_noalloc: kmax above 256");
+        return SP_E_INVALID;
+    }
+    CellGrid g{};
+    g.dim = dim;
+    g.cs = h * 1.0000001;
+    for (int d = 0; d < 3; d++) {
+        g.lo[d] = d < dim ? lo[d] : 0.0;
+        g.nc[d] = d < dim ? (int)((hi[d] - lo[d]) / g.cs) + 1 : 1;
+        if (d < dim && !(hi[d] >= lo[d])) {
+            noalloc_msg(err, errlen, "sp_neighbors_noalloc: bounding box hi < lo");
+            return SP_E_INVALID;
+        }
+    }
+    if ((long long)g.nc[0] * g.nc[1] * g.nc[2] > kNoAllocMaxCells) {
+        noalloc_msg(err, errlen,
+                    "sp_neighbors_noalloc: more than 524,288 cells of edge h in the bounding box");
+        return SP_E_INVALID;
+    }
+    g.ncell = g.nc[0] * g.nc[1] * g.nc[2];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        noalloc_msg(err, errlen, "sp_neighbors_noalloc: no current CUDA device");
+        return SP_E_CUDA;
+    }
+    void* base = nullptr;
+    {
+        // one-time set-up per device, with that device current
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            cudaError_t e = cudaGetSymbolAddress(&g_noalloc_ptr[dev], sp_noalloc_scratch);
+            if (e != cudaSuccess) {
+                g_noalloc_ptr[dev] = nullptr;
+                noalloc_msg(err, errlen, "sp_neighbors_noalloc: cudaGetSymbolAddress failed");
+                return SP_E_CUDA;
+            }
+        }
+        base = g_noalloc_ptr[dev];
+    }
+    int* cell = (int*)base;
+    int* order = cell + kNoAllocMaxParticles;
+    int* hist = order + kNoAllocMaxParticles;
+    int* fill = hist + kNoAllocMaxCells;
+    int* start = fill + kNoAllocMaxCells;
+    int* flag = start + kNoAllocMaxCells + 1;
+    cudaStream_t st = (cudaStream_t)stream;
+    // the array keeps the previous call's contents: clear what starts at zero
+    cudaMemsetAsync(hist, 0, sizeof(int) * g.ncell, st);
+    cudaMemsetAsync(fill, 0, sizeof(int) * g.ncell, st);
+    cudaMemsetAsync(flag, 0, sizeof(int), st);
+    const int tb = 256, nb = (n + tb - 1) / tb;
+    cell_hist<<<nb, tb, 0, st>>>(x, n, g, cell, hist);
+    scan_single_block<<<1, 1024, 0, st>>>(hist, start, g.ncell);
+    cell_scatter<<<nb, tb, 0, st>>>(cell, n, start, fill, order);
+    const int sb = (n + 127) / 128;
+    if (kmax <= 32)
+        neighbor_search_f64<32><<<sb, 128, 0, st>>>(x, x, n, g, h, mass, rho, start, order, kmax,
+                                                    count, idx, dist, dWdr, Dij, flag);
+    else if (kmax <= 64)
+        neighbor_search_f64<64><<<sb, 128, 0, st>>>(x, x, n, g, h, mass, rho, start, order, kmax,
+                                                    count, idx, dist, dWdr, Dij, flag);
+    else
+        neighbor_search_f64<256><<<sb, 128, 0, st>>>(x, x, n, g, h, mass, rho, start, order, kmax,
+                                                     count, idx, dist, dWdr, Dij, flag);
+    int over = 0;
+    cudaError_t e = cudaMemcpyAsync(&over, flag, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        noalloc_msg(err, errlen, cudaGetErrorString(e));
+        return SP_E_CUDA;
+    }
+    if (over) {
+        noalloc_msg(err, errlen, "sp_neighbors_noalloc: a particle has more than kmax neighbours");
+        return SP_E_UNSUPPORTED;
+    }
+    return SP_OK;
+}
