@@ -43,6 +43,10 @@ SEED0 = 20260101
 # voxel + 4 |G_r| dependency entries for a reaction event
 B_DIFF = 2 * (8 * 3 + 16 * 4 + 24) + 8 * 32      # 480
 B_RXN = 8 * 3 + 16 * 4 + 24 + 4 * 5              # 132
+# DRAM bytes (read + write) per event of nsm_advance_batch on this workload,
+# from one ncu capture of the profile case (--profile-case: 6.388 GB over
+# 8,894,255 events in the captured launch; profiles/nsm_advance_batch_rdme40.txt)
+DRAM_BYTES_PER_EVENT = 718.0
 
 
 def workload(intervals: int | None = None):
@@ -165,7 +169,7 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def cpu_baseline(threads: int | None = None, ntraj: int = 64, intervals: int = 2):
+def cpu_baseline(threads: int | None = None, ntraj: int = 128, intervals: int = 8):
     """The oracle (CPU restatement of the reference algorithm) on the host
     cores, a bounded sample of the same workload."""
     import oracle
@@ -274,6 +278,8 @@ def run_ours(args, world, rank, local, pg):
     bytes_per_event = frac_rxn * B_RXN + (1 - frac_rxn) * B_DIFF
     peak, peak_src = measured_peak()
     achieved = events * bytes_per_event / (prof["kernel_ms"] / 1e3) / 1e9
+    per_launch_events = events / max(1, prof["launches"])
+    traffic_pe = args.traffic if args.traffic is not None else DRAM_BYTES_PER_EVENT
     eng.close()
 
     # e2e: sp_run through the C ABI with host buffers, K intervals
@@ -296,8 +302,11 @@ def run_ours(args, world, rank, local, pg):
         "dtype": "int32 counts, f32 propensities, f64 clock", "data": "synthetic",
         "config": config_dict(sc),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": args.traffic,
-                     "kernel": "nsm_advance_small", "peak_source": peak_src,
+                     "frac": achieved / peak,
+                     "traffic": traffic_pe * per_launch_events,
+                     "traffic_note": "ncu DRAM bytes per event x events per launch",
+                     "algorithmic_bytes_per_launch": bytes_per_event * per_launch_events,
+                     "kernel": prof["kernel"], "peak_source": peak_src,
                      "bytes_per_event": bytes_per_event},
         "e2e": {"value": e2e_events / e2e_s, "unit": UNIT,
                 "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps},
@@ -322,7 +331,8 @@ def main():
     ap.add_argument("--skip-sdpd", action="store_true")
     ap.add_argument("--sdpd-steps", type=int, default=200)
     ap.add_argument("--traffic", type=float, default=None,
-                    help="DRAM bytes per event of the event-loop kernel from an ncu capture")
+                    help="DRAM bytes per event of the event-loop kernel from an ncu capture "
+                         "(default: the committed capture's figure)")
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu: the bench workload over two 0.05 intervals")
     ap.add_argument("--profile-sdpd", action="store_true",
@@ -345,8 +355,14 @@ def main():
         from spatialpy_gb300.engine import Engine
         sc = S.config_rdme_3d(t_end=0.1, num_points=3, dt=0.05)
         with Engine(sc) as eng:
-            r = eng.run(np.arange(SEED0, SEED0 + NTRAJ, dtype=np.uint64), want_counts=False)
-            print("profile case events", int(r["events"].sum()), eng.profile())
+            eng.start(np.arange(SEED0, SEED0 + NTRAJ, dtype=np.uint64), want_moments=False)
+            done = 0
+            for launch in range(2):
+                eng.advance(1)
+                ev = sum(eng.status(j)["events"] for j in range(NTRAJ))
+                print(f"profile case launch {launch}: {ev - done} events", eng.profile())
+                done = ev
+            eng.finish()
         return
     world, rank, local, pg = dist_setup()
     if args.impl == "reference":
