@@ -223,8 +223,12 @@ typedef struct sp_profile {
     double total_ms;
     double kernel_ms;
     int64_t launches;
-    int64_t reserved;
+    int64_t kernel;     /* event-loop kernel of the last run: SP_KERNEL_* */
 } sp_profile;
+#define SP_KERNEL_NONE 0
+#define SP_KERNEL_GENERIC 1      /* nsm_advance_generic: any network, one warp per trajectory */
+#define SP_KERNEL_SEQUENTIAL 2   /* nsm_advance_small: register-resident network */
+#define SP_KERNEL_BATCH 3        /* nsm_advance_batch: speculative 32-event batches */
 int sp_last_profile(sp_handle* h, sp_profile* p);
 
 /*

@@ -10,7 +10,7 @@
 
 static int SPO_NB(int n, int dim, const REAL *xq, const REAL *xt, REAL h, const REAL *mass,
                   const REAL *rho, int kmax, int32_t *count, int32_t *idx, REAL *dist,
-                  REAL *dwdr, const REAL *self_d2) {
+                  REAL *dwdr, const REAL *self_d2, REAL *dij) {
     /* same predicate and order as spo_neighbors, in REAL arithmetic */
     REAL lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
     for (int d = 0; d < dim; d++) {
@@ -93,17 +93,29 @@ static int SPO_NB(int n, int dim, const REAL *xq, const REAL *xt, REAL h, const 
             idx[(size_t)i * kmax + k] = cj[k];
             dist[(size_t)i * kmax + k] = r;
             dwdr[(size_t)i * kmax + k] = alpha * (K_(-12) * r / (h * h)) * ((K_(1) - R) * (K_(1) - R));
+            if (dij) {
+                /* D_ij of add_to_neighbor_list (particle.cpp:181-187) with the
+                   densities current at the search, operator order kept */
+                const int j = cj[k];
+                const REAL r2 = cd2[k];
+                const REAL ih = K_(1.0) / h;
+                const REAL ihsq = ih * ih;
+                const REAL dhr = h - r;
+                const REAL wfd = K_(-25.066903536973515383) * dhr * dhr * ihsq * ihsq * ihsq * ih;
+                dij[(size_t)i * kmax + k] = K_(-2.0) * (mass[i] * mass[j]) / (mass[i] + mass[j]) *
+                                            (rho[i] + rho[j]) / (rho[i] * rho[j]) * r2 * wfd /
+                                            (r2 + K_(0.01) * h * h);
+            }
         }
     }
 #undef CELLD
     free(cd2); free(cj); free(start); free(cell); free(order);
-    (void)mass; (void)rho;
     return rc;
 }
 
 int SPO_FN(const sp_scenario *sc, int32_t step0, int32_t nsteps, int32_t mode, int32_t kmax,
            double *x_io, double *v_io, double *vt_io, double *rho_io, double *F_io,
-           double *Fbp_io, double *Frho_io, int32_t *nbr_count) {
+           double *Fbp_io, double *Frho_io, int32_t *nbr_count, spo_sdpd_lists *lists) {
     const int n = sc->num_particles, dim = sc->dimension;
     const REAL h = (REAL)sc->h, dt = (REAL)sc->dt, rho0 = (REAL)sc->rho0, P0 = (REAL)sc->P0;
     const REAL g[3] = {(REAL)sc->gravity[0], (REAL)sc->gravity[1], (REAL)sc->gravity[2]};
@@ -120,6 +132,7 @@ int SPO_FN(const sp_scenario *sc, int32_t step0, int32_t nsteps, int32_t mode, i
     REAL *ndw = (REAL *)malloc(sizeof(REAL) * (size_t)n * kmax);
     int32_t *nidx = (int32_t *)malloc(sizeof(int32_t) * (size_t)n * kmax);
     int32_t *ncnt = (int32_t *)malloc(sizeof(int32_t) * n);
+    REAL *ndij = lists ? (REAL *)malloc(sizeof(REAL) * (size_t)n * kmax) : NULL;
     for (int i = 0; i < 3 * n; i++) {
         x[i] = (REAL)x_io[i]; v[i] = (REAL)v_io[i]; vt[i] = (REAL)vt_io[i];
         F[i] = (REAL)F_io[i]; Fbp[i] = (REAL)Fbp_io[i];
@@ -170,7 +183,8 @@ int SPO_FN(const sp_scenario *sc, int32_t step0, int32_t nsteps, int32_t mode, i
                 }
                 sd2[i] = s2;
             }
-        if (SPO_NB(n, dim, q, tp, h, m, rho, kmax, ncnt, nidx, ndist, ndw, selfmode ? sd2 : NULL)) {
+        if (SPO_NB(n, dim, q, tp, h, m, rho, kmax, ncnt, nidx, ndist, ndw, selfmode ? sd2 : NULL,
+                   ndij)) {
             rc = -1;
             break;
         }
@@ -289,6 +303,13 @@ int SPO_FN(const sp_scenario *sc, int32_t step0, int32_t nsteps, int32_t mode, i
     }
     for (int i = 0; i < n; i++) { rho_io[i] = rho[i]; Frho_io[i] = Frho[i]; }
     if (nbr_count) memcpy(nbr_count, ncnt, sizeof(int32_t) * n);
+    if (lists) {
+        /* the lists of the last step, as the NSM of that step reads them */
+        memcpy(lists->count, ncnt, sizeof(int32_t) * n);
+        memcpy(lists->idx, nidx, sizeof(int32_t) * (size_t)n * kmax);
+        for (size_t e = 0; e < (size_t)n * kmax; e++) lists->dij[e] = (double)ndij[e];
+    }
+    free(ndij);
     free(x); free(xt); free(v); free(vt); free(F); free(Fbp); free(rho); free(orho); free(Frho);
     free(m); free(nu); free(nrm); free(ndist); free(ndw); free(nidx); free(ncnt); free(sd2);
     return rc;

@@ -367,138 +367,179 @@ static inline double draw_time(double t, float e, float a) {
     return a > 0.0f ? t + (double)(e / a) : HUGE_VAL;
 }
 
-static int nsm_run(const nsm_tables_t *t, const uint32_t *u0, uint64_t seed, int selection,
-                   int32_t *out, int64_t *ev) {
-    const sp_scenario *sc = t->sc;
-    const int N = t->N, S = t->S, K = t->K;
-    int32_t *x = (int32_t *)malloc(sizeof(int32_t) * (size_t)N * S);
-    for (size_t i = 0; i < (size_t)N * S; i++) x[i] = (int32_t)u0[i];
+/* one trajectory's state between windows */
+typedef struct {
+    int32_t *x;
     heap_t h;
-    h.n = N;
-    h.heap = (int32_t *)malloc(sizeof(int32_t) * N);
-    h.pos = (int32_t *)malloc(sizeof(int32_t) * N);
-    h.tau = (double *)malloc(sizeof(double) * N);
-    const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
-    /* queue build at t0 = 0 (NRMConstant_v5::build, :52-71): stream 1 */
+    uint32_t key[2];
+    uint64_t evn;
+    int64_t nrx, ndf;
+    int status;
+} nsm_state_t;
+
+static void nsm_state_init(nsm_state_t *st, const nsm_tables_t *t, const uint32_t *u0,
+                           uint64_t seed) {
+    const int N = t->N, S = t->S;
+    st->x = (int32_t *)malloc(sizeof(int32_t) * (size_t)N * S);
+    for (size_t i = 0; i < (size_t)N * S; i++) st->x[i] = (int32_t)u0[i];
+    st->h.n = N;
+    st->h.heap = (int32_t *)malloc(sizeof(int32_t) * N);
+    st->h.pos = (int32_t *)malloc(sizeof(int32_t) * N);
+    st->h.tau = (double *)malloc(sizeof(double) * N);
+    st->key[0] = (uint32_t)seed;
+    st->key[1] = (uint32_t)(seed >> 32);
+    st->evn = 0;
+    st->nrx = st->ndf = 0;
+    st->status = SP_TRAJ_OK;
+}
+
+static void nsm_state_free(nsm_state_t *st) {
+    free(st->x); free(st->h.heap); free(st->h.pos); free(st->h.tau);
+}
+
+/* queue build at t0 (NRMConstant_v5::build, :52-71): Philox stream 1, counter
+   (voxel, build_index) */
+static void nsm_build(const nsm_tables_t *t, nsm_state_t *st, double t0, uint32_t build_index) {
+    const int N = t->N, S = t->S;
+    heap_t *h = &st->h;
     for (int v = 0; v < N; v++) {
         float srr, sdr;
-        voxel_rates(t, v, x + (size_t)v * S, v, &srr, &sdr);
-        uint32_t ctr[4] = {(uint32_t)v, 0u, 1u, 0u}, r[4];
-        spo_philox4x32_10(ctr, key, r);
-        h.tau[v] = draw_time(0.0, spo_neglog_f(u32f(r[0])), srr + sdr);
-        h.heap[v] = v;
-        h.pos[v] = v;
+        voxel_rates(t, v, st->x + (size_t)v * S, v, &srr, &sdr);
+        uint32_t ctr[4] = {(uint32_t)v, build_index, 1u, 0u}, r[4];
+        spo_philox4x32_10(ctr, st->key, r);
+        h->tau[v] = draw_time(t0, spo_neglog_f(u32f(r[0])), srr + sdr);
+        h->heap[v] = v;
+        h->pos[v] = v;
     }
     for (int i = N / 2 - 1; i >= 0; i--) {      /* heapify */
         int j = i;
         for (;;) {
             int l = 2 * j + 1, rr = l + 1, m = j;
-            if (l < N && hless(&h, h.heap[l], h.heap[m])) m = l;
-            if (rr < N && hless(&h, h.heap[rr], h.heap[m])) m = rr;
+            if (l < N && hless(h, h->heap[l], h->heap[m])) m = l;
+            if (rr < N && hless(h, h->heap[rr], h->heap[m])) m = rr;
             if (m == j) break;
-            hswap(&h, j, m);
+            hswap(h, j, m);
             j = m;
         }
     }
-    uint64_t evn = 0;
-    int64_t nrx = 0, ndf = 0;
-    int status = SP_TRAJ_OK;
+}
+
+/* the events of one engine step, up to t_end = dt*step + dt
+   (nsm_core__take_step, simulate_rdme.cpp:211-472) */
+static void nsm_window(const nsm_tables_t *t, nsm_state_t *st, int step, int selection) {
+    const sp_scenario *sc = t->sc;
+    const int S = t->S, K = t->K;
+    int32_t *x = st->x;
+    heap_t *hp = &st->h;
+    const double t_end = sc->dt * (double)step + sc->dt;   /* simulate_rdme.cpp:67,215 */
+    for (;;) {
+        const int v = hp->heap[0];
+        const double tt = hp->tau[v];
+        if (tt == HUGE_VAL) break;
+        if (selection == SP_SELECT_EXACT && tt > t_end) break;
+        uint32_t ctr[4] = {(uint32_t)st->evn, (uint32_t)(st->evn >> 32), 0u, 0u}, r[4];
+        spo_philox4x32_10(ctr, st->key, r);
+        st->evn++;
+        const float ua = u24(r[0]), ub = u24(r[1]);
+        const float e0 = spo_neglog_f(u32f(r[2])), e1 = spo_neglog_f(u32f(r[3]));
+        int32_t *xv = x + (size_t)v * S;
+        float srr, sdr;
+        voxel_rates(t, v, xv, v, &srr, &sdr);
+        const float tot = srr + sdr;
+        if (ua * tot <= srr) {                               /* :255 rand1 <= srrate/totrate */
+            const float target = selection == SP_SELECT_EXACT ? ua * tot : ua * srr;
+            float cum = 0.0f;
+            int re = -1, last = -1;
+            for (int q = 0; q < t->R; q++) {
+                const float a = prop(t, q, xv, t->vol[v], t->ivol[v], sc->type[v]);
+                cum = cum + a;
+                if (a > 0.0f) {
+                    last = q;
+                    if (target <= cum) { re = q; break; }
+                }
+            }
+            if (re < 0) re = last;
+            if (re < 0) { st->status = SP_TRAJ_SELECT_OVERFLOW; break; }
+            for (int64_t i = sc->jcN[re]; i < sc->jcN[re + 1]; i++) {   /* :285-296 */
+                xv[sc->irN[i]] += sc->prN[i];
+                if (xv[sc->irN[i]] < 0) st->status = SP_TRAJ_NEG_COUNT;
+            }
+            if (st->status) break;
+            voxel_rates(t, v, xv, v, &srr, &sdr);
+            hp->tau[v] = draw_time(tt, e0, srr + sdr);
+            hfix(hp, v);
+            st->nrx++;
+        } else {
+            const float target = selection == SP_SELECT_EXACT ? ua * tot - srr : ua * sdr;
+            float cum = 0.0f;
+            int sp = -1, last = -1;
+            for (int s = 0; s < S; s++) {                      /* :319-321 */
+                const float wgt = t->ddiag[(size_t)v * S + s] * (float)xv[s];
+                cum = cum + wgt;
+                if (wgt > 0.0f) {
+                    last = s;
+                    if (target <= cum) { sp = s; break; }
+                }
+            }
+            if (sp < 0) sp = last;
+            if (sp < 0) { st->status = SP_TRAJ_SELECT_OVERFLOW; break; }
+            const float target2 = ub * t->ddiag[(size_t)v * S + sp];   /* :353-354 */
+            const float *c = t->cdf + ((size_t)v * S + sp) * K;
+            int k = -1, lastk = -1;
+            float prev = 0.0f;
+            for (int q = 0; q < t->cnt[v]; q++) {             /* :359-367 */
+                if (c[q] > prev) {
+                    lastk = q;
+                    if (c[q] > target2) { k = q; break; }
+                }
+                prev = c[q];
+            }
+            if (k < 0) k = lastk;
+            if (k < 0) { st->status = SP_TRAJ_SELECT_OVERFLOW; break; }
+            const int w = t->idx[(size_t)v * K + k];
+            int32_t *xw = x + (size_t)w * S;
+            xv[sp] -= 1;                                          /* :394-402 */
+            xw[sp] += 1;            /* w == v (a moving particle's own start-of-step
+                                       point in its list): the count is unchanged */
+            voxel_rates(t, v, xv, v, &srr, &sdr);
+            hp->tau[v] = draw_time(tt, e0, srr + sdr);
+            hfix(hp, v);
+            /* the engine evaluates the destination's reactions with the
+               source voxel's volume (simulate_rdme.cpp:431-433) */
+            voxel_rates(t, w, xw, selection == SP_SELECT_REFERENCE ? v : w, &srr, &sdr);
+            hp->tau[w] = draw_time(tt, e1, srr + sdr);
+            hfix(hp, w);
+            st->ndf++;
+        }
+        if (selection == SP_SELECT_REFERENCE && tt > t_end) break;   /* :233 */
+    }
+}
+
+/* static domain: one queue build at t = 0, then every step's window */
+static int nsm_run(const nsm_tables_t *t, const uint32_t *u0, uint64_t seed, int selection,
+                   int32_t *out, int64_t *ev) {
+    const sp_scenario *sc = t->sc;
+    const size_t NS = (size_t)t->N * t->S;
+    nsm_state_t st;
+    nsm_state_init(&st, t, u0, seed);
+    nsm_build(t, &st, 0.0, 0u);
     int oi = 0;
     const int nout = sc->num_outputs;
-    for (int step = 0; step < sc->num_steps && status == SP_TRAJ_OK; step++) {
+    for (int step = 0; step < sc->num_steps && st.status == SP_TRAJ_OK; step++) {
         while (oi < nout && sc->output_steps[oi] <= step) {
-            if (out) for (size_t i = 0; i < (size_t)N * S; i++) out[(size_t)oi * N * S + i] = x[i];
+            if (out) memcpy(out + (size_t)oi * NS, st.x, sizeof(int32_t) * NS);
             oi++;
         }
-        const double t_end = sc->dt * (double)step + sc->dt;   /* simulate_rdme.cpp:67,215 */
-        for (;;) {
-            const int v = h.heap[0];
-            const double tt = h.tau[v];
-            if (tt == HUGE_VAL) break;
-            if (selection == SP_SELECT_EXACT && tt > t_end) break;
-            uint32_t ctr[4] = {(uint32_t)evn, (uint32_t)(evn >> 32), 0u, 0u}, r[4];
-            spo_philox4x32_10(ctr, key, r);
-            evn++;
-            const float ua = u24(r[0]), ub = u24(r[1]);
-            const float e0 = spo_neglog_f(u32f(r[2])), e1 = spo_neglog_f(u32f(r[3]));
-            int32_t *xv = x + (size_t)v * S;
-            float srr, sdr;
-            voxel_rates(t, v, xv, v, &srr, &sdr);
-            const float tot = srr + sdr;
-            if (ua * tot <= srr) {                               /* :255 rand1 <= srrate/totrate */
-                const float target = selection == SP_SELECT_EXACT ? ua * tot : ua * srr;
-                float cum = 0.0f;
-                int re = -1, last = -1;
-                for (int q = 0; q < t->R; q++) {
-                    const float a = prop(t, q, xv, t->vol[v], t->ivol[v], sc->type[v]);
-                    cum = cum + a;
-                    if (a > 0.0f) {
-                        last = q;
-                        if (target <= cum) { re = q; break; }
-                    }
-                }
-                if (re < 0) re = last;
-                if (re < 0) { status = SP_TRAJ_SELECT_OVERFLOW; break; }
-                for (int64_t i = sc->jcN[re]; i < sc->jcN[re + 1]; i++) {   /* :285-296 */
-                    xv[sc->irN[i]] += sc->prN[i];
-                    if (xv[sc->irN[i]] < 0) status = SP_TRAJ_NEG_COUNT;
-                }
-                if (status) break;
-                voxel_rates(t, v, xv, v, &srr, &sdr);
-                h.tau[v] = draw_time(tt, e0, srr + sdr);
-                hfix(&h, v);
-                nrx++;
-            } else {
-                const float target = selection == SP_SELECT_EXACT ? ua * tot - srr : ua * sdr;
-                float cum = 0.0f;
-                int sp = -1, last = -1;
-                for (int s = 0; s < S; s++) {                      /* :319-321 */
-                    const float wgt = t->ddiag[(size_t)v * S + s] * (float)xv[s];
-                    cum = cum + wgt;
-                    if (wgt > 0.0f) {
-                        last = s;
-                        if (target <= cum) { sp = s; break; }
-                    }
-                }
-                if (sp < 0) sp = last;
-                if (sp < 0) { status = SP_TRAJ_SELECT_OVERFLOW; break; }
-                const float target2 = ub * t->ddiag[(size_t)v * S + sp];   /* :353-354 */
-                const float *c = t->cdf + ((size_t)v * S + sp) * K;
-                int k = -1, lastk = -1;
-                float prev = 0.0f;
-                for (int q = 0; q < t->cnt[v]; q++) {             /* :359-367 */
-                    if (c[q] > prev) {
-                        lastk = q;
-                        if (c[q] > target2) { k = q; break; }
-                    }
-                    prev = c[q];
-                }
-                if (k < 0) k = lastk;
-                if (k < 0) { status = SP_TRAJ_SELECT_OVERFLOW; break; }
-                const int w = t->idx[(size_t)v * K + k];
-                int32_t *xw = x + (size_t)w * S;
-                xv[sp] -= 1;                                          /* :394-402 */
-                xw[sp] += 1;
-                voxel_rates(t, v, xv, v, &srr, &sdr);
-                h.tau[v] = draw_time(tt, e0, srr + sdr);
-                hfix(&h, v);
-                /* the engine evaluates the destination's reactions with the
-                   source voxel's volume (simulate_rdme.cpp:431-433) */
-                voxel_rates(t, w, xw, selection == SP_SELECT_REFERENCE ? v : w, &srr, &sdr);
-                h.tau[w] = draw_time(tt, e1, srr + sdr);
-                hfix(&h, w);
-                ndf++;
-            }
-            if (selection == SP_SELECT_REFERENCE && tt > t_end) break;   /* :233 */
-        }
+        nsm_window(t, &st, step, selection);
     }
     while (out && oi < nout) {
-        for (size_t i = 0; i < (size_t)N * S; i++) out[(size_t)oi * N * S + i] = x[i];
+        memcpy(out + (size_t)oi * NS, st.x, sizeof(int32_t) * NS);
         oi++;
     }
-    ev[0] = nrx;
-    ev[1] = ndf;
-    free(x); free(h.heap); free(h.pos); free(h.tau);
+    ev[0] = st.nrx;
+    ev[1] = st.ndf;
+    const int status = st.status;
+    nsm_state_free(&st);
     return status;
 }
 
@@ -553,4 +594,91 @@ int spo_nsm_ensemble(const sp_scenario *sc, const uint32_t *u0, const uint64_t *
     free(th);
     tables_free(&t);
     return threads;
+}
+
+/* ------------------------------------------------------------------------
+ * Moving domain with species: the SDPD flow (shared by all trajectories)
+ * and, every step, fresh diffusion tables, volumes and event queues.
+ * ------------------------------------------------------------------------ */
+int spo_coupled_ensemble(const sp_scenario *sc, const uint32_t *u0, const uint64_t *seeds,
+                         int32_t ntraj, int32_t selection, int32_t precision, int32_t mode,
+                         int32_t kmax, int32_t *out, int64_t *ev, int32_t *status, double *px,
+                         double *prho) {
+    const int N = sc->num_particles, S = sc->num_species, R = sc->num_reactions;
+    const size_t NS = (size_t)N * S;
+    double *x = (double *)malloc(sizeof(double) * 3 * N), *v = (double *)calloc(3 * N, sizeof(double));
+    double *vt = (double *)calloc(3 * N, sizeof(double)), *F = (double *)calloc(3 * N, sizeof(double));
+    double *Fbp = (double *)calloc(3 * N, sizeof(double)), *rho = (double *)malloc(sizeof(double) * N);
+    double *Frho = (double *)calloc(N, sizeof(double));
+    memcpy(x, sc->x, sizeof(double) * 3 * N);
+    if (sc->v) memcpy(v, sc->v, sizeof(double) * 3 * N);
+    memcpy(rho, sc->rho, sizeof(double) * N);
+    spo_sdpd_lists L;
+    L.count = (int32_t *)calloc(N, sizeof(int32_t));
+    L.idx = (int32_t *)malloc(sizeof(int32_t) * (size_t)N * kmax);
+    L.dij = (double *)malloc(sizeof(double) * (size_t)N * kmax);
+    nsm_tables_t t;
+    memset(&t, 0, sizeof(t));
+    t.sc = sc;
+    t.N = N;
+    t.S = S;
+    t.R = R;
+    t.T = sc->num_types;
+    t.K = kmax;
+    t.cnt = L.count;
+    t.idx = L.idx;
+    t.cdf = (float *)calloc(NS * kmax, sizeof(float));
+    t.ddiag = (float *)calloc(NS, sizeof(float));
+    t.vol = (float *)malloc(sizeof(float) * N);
+    t.ivol = (float *)malloc(sizeof(float) * N);
+    t.rate = (float *)malloc(sizeof(float) * (R > 0 ? R : 1));
+    for (int r = 0; r < R; r++) t.rate[r] = (float)sc->rxn_rate[r];
+    nsm_state_t *st = (nsm_state_t *)malloc(sizeof(nsm_state_t) * ntraj);
+    for (int j = 0; j < ntraj; j++) nsm_state_init(&st[j], &t, u0, seeds[j]);
+    int rc = 0, oi = 0;
+    const int nout = sc->num_outputs;
+    for (int step = 0; step < sc->num_steps && !rc; step++) {
+        while (oi < nout && sc->output_steps[oi] <= step) {
+            for (int j = 0; j < ntraj && out; j++)
+                memcpy(out + ((size_t)j * nout + oi) * NS, st[j].x, sizeof(int32_t) * NS);
+            if (px) memcpy(px + (size_t)oi * 3 * N, x, sizeof(double) * 3 * N);
+            if (prho) memcpy(prho + (size_t)oi * N, rho, sizeof(double) * N);
+            oi++;
+        }
+        rc = precision == 64
+                 ? spo_sdpd_f64(sc, step, 1, mode, kmax, x, v, vt, rho, F, Fbp, Frho, NULL, &L)
+                 : spo_sdpd_f32(sc, step, 1, mode, kmax, x, v, vt, rho, F, Fbp, Frho, NULL, &L);
+        if (rc) break;
+        /* nsm_core__initialize_rxn/diff_propensities (simulate_rdme.cpp:113-152)
+           with this step's lists and the end-of-step densities */
+        spo_diffusion_tables(sc, kmax, L.count, L.idx, L.dij, t.ddiag, t.cdf);
+        for (int i = 0; i < N; i++) {
+            t.vol[i] = (float)(sc->mass[i] / rho[i]);
+            t.ivol[i] = (float)(rho[i] / sc->mass[i]);
+        }
+        /* nsm_core__initialize_heap at step*dt, then take_step (:53-68) */
+        for (int j = 0; j < ntraj; j++) {
+            if (st[j].status != SP_TRAJ_OK) continue;
+            nsm_build(&t, &st[j], sc->dt * (double)step, (uint32_t)step);
+            nsm_window(&t, &st[j], step, selection);
+        }
+    }
+    while (!rc && oi < nout) {
+        for (int j = 0; j < ntraj && out; j++)
+            memcpy(out + ((size_t)j * nout + oi) * NS, st[j].x, sizeof(int32_t) * NS);
+        if (px) memcpy(px + (size_t)oi * 3 * N, x, sizeof(double) * 3 * N);
+        if (prho) memcpy(prho + (size_t)oi * N, rho, sizeof(double) * N);
+        oi++;
+    }
+    for (int j = 0; j < ntraj; j++) {
+        ev[2 * j] = st[j].nrx;
+        ev[2 * j + 1] = st[j].ndf;
+        if (status) status[j] = st[j].status;
+        nsm_state_free(&st[j]);
+    }
+    free(st);
+    free(t.cdf); free(t.ddiag); free(t.vol); free(t.ivol); free(t.rate);
+    free(L.count); free(L.idx); free(L.dij);
+    free(x); free(v); free(vt); free(F); free(Fbp); free(rho); free(Frho);
+    return rc;
 }

@@ -60,12 +60,6 @@ int spo_nsm_ensemble(const sp_scenario *sc, const uint32_t *u0, const uint64_t *
                      int32_t ntraj, int32_t selection, int32_t threads, int32_t *out,
                      int64_t *ev, int32_t *status);
 
-/*
- * Advance one NSM trajectory over an explicit window with caller-provided
- * diffusion tables: used by the coupled SDPD test.  State in/out:
- * counts[N*S], tau[N] (next-event times), ev_counter (Philox event index).
- */
-
 /* SDPD flow (sdpd_oracle.c), FP64 and FP32 builds.  mode bits:
  *   1 = Gauss-Seidel density reads in the boundary-volume-fraction pass (the
  *       order a single engine thread produces, model.cpp:284-288)
@@ -74,12 +68,36 @@ int spo_nsm_ensemble(const sp_scenario *sc, const uint32_t *u0, const uint64_t *
  *   4 = with 2: a particle's distance to its own start-of-step point is the
  *       predictor displacement |dt vt| (the FP32 engine's rule)
  * State arrays are [N*3] / [N] in double; nsteps engine steps from step0. */
+/* Neighbour lists of the last step's force pass (count[N], idx/dij[N*kmax]),
+ * D_ij (particle.cpp:181-187) computed in the build's arithmetic from the
+ * post-predictor densities, widened to double. */
+typedef struct spo_sdpd_lists {
+    int32_t *count;
+    int32_t *idx;
+    double *dij;
+} spo_sdpd_lists;
 int spo_sdpd_f64(const sp_scenario *sc, int32_t step0, int32_t nsteps, int32_t mode, int32_t kmax,
                  double *x, double *v, double *vt, double *rho, double *F, double *Fbp,
-                 double *Frho, int32_t *nbr_count);
+                 double *Frho, int32_t *nbr_count, spo_sdpd_lists *lists);
 int spo_sdpd_f32(const sp_scenario *sc, int32_t step0, int32_t nsteps, int32_t mode, int32_t kmax,
                  double *x, double *v, double *vt, double *rho, double *F, double *Fbp,
-                 double *Frho, int32_t *nbr_count);
+                 double *Frho, int32_t *nbr_count, spo_sdpd_lists *lists);
+
+/*
+ * Moving domain with stochastic species (simulate_threads.cpp:232-281 with
+ * simulate_rdme.cpp:53-68 on a non-static domain): every step runs the SDPD
+ * step (precision 32 or 64, `mode` bits as above), rebuilds Ddiag and the
+ * destination weights from that step's lists, the volumes m/rho from the
+ * end-of-step density, and every trajectory's event queue at t = step*dt
+ * (Philox build stream index = step), then runs that trajectory's events up
+ * to (step+1)*dt.  out: [ntraj][num_outputs][N][S] counts or NULL; px/prho:
+ * [num_outputs][N*3] / [num_outputs][N] flow state or NULL; ev: [ntraj*2];
+ * status: [ntraj].  Returns 0, -1 on a list overflow, 2 on NaN state.
+ */
+int spo_coupled_ensemble(const sp_scenario *sc, const uint32_t *u0, const uint64_t *seeds,
+                         int32_t ntraj, int32_t selection, int32_t precision, int32_t mode,
+                         int32_t kmax, int32_t *out, int64_t *ev, int32_t *status, double *px,
+                         double *prho);
 
 #ifdef __cplusplus
 }

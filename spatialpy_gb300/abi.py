@@ -110,7 +110,7 @@ class SpProfile(C.Structure):
         ("total_ms", C.c_double),
         ("kernel_ms", C.c_double),
         ("launches", C.c_int64),
-        ("reserved", C.c_int64),
+        ("kernel", C.c_int64),
     ]
 
 

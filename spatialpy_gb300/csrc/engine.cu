@@ -20,7 +20,10 @@
 
 namespace spg {
 void launch_nsm_init(NsmTraj* trajs, const NsmInstance* insts, int ntraj, int max_leaf,
-                     int max_levels, const uint32_t* const* u0, cudaStream_t st);
+                     int max_levels, const uint32_t* const* u0, bool build_queue,
+                     cudaStream_t st);
+void launch_nsm_rebuild(NsmTraj* trajs, const NsmInstance* insts, int ntraj, int max_leaf,
+                        int max_levels, double t0, uint32_t build_index, cudaStream_t st);
 int nsm_warp_smem(const NsmInstance& d, bool with_state);
 void launch_nsm_advance(bool ref, bool smem_state, int variant, int warp_smem, int wpb,
                         NsmTraj* trajs, const NsmInstance* insts, int ntraj, int step_end,
@@ -81,6 +84,12 @@ struct RunState {
     long long ctot = 0, mtot = 0;
     int32_t* d_counts = nullptr;
     long long *d_mom = nullptr, *d_coff = nullptr, *d_moff = nullptr;
+    // moving domain with species: one flow (instance cinst) shared by every
+    // trajectory, stepped here; particle outputs of that instance
+    bool coupled = false, want_part = false;
+    int cinst = -1, step = 0, max_leaf = 0, max_levels = 0;
+    long long poff = 0, ptot = 0;   // offset of cinst / total, in particles x outputs
+    double *d_px = nullptr, *d_pv = nullptr, *d_prho = nullptr;
 };
 
 struct sp_handle {
@@ -105,6 +114,7 @@ struct sp_handle {
     std::string err;
     double last_ms = 0, adv_ms = 0;
     long long last_launches = 0, launches = 0;
+    int last_kernel = SP_KERNEL_NONE;
     RunState run;
 };
 
@@ -296,6 +306,21 @@ static int setup_instance(sp_handle* h, const sp_scenario& s, Instance& I) {
     } else {
         I.sdpd = sdpd_create(s, h->opt.sdpd_precision, h->st, &h->err);
         if (!I.sdpd) return SP_E_CUDA;
+        if (S > 0) {
+            // species on a moving domain: the flow's force-pass lists carry
+            // D_ij and feed the per-step diffusion tables
+            if ((rc = sdpd_enable_dij(I.sdpd, &h->err))) return rc;
+            const SdpdLists L = sdpd_lists(I.sdpd);
+            I.K = L.kcap;
+            I.nbr_cnt = L.count;
+            I.nbr_idx = L.idx;
+            if ((rc = dev_alloc(h, &I.ddiag, (size_t)N * S))) return rc;
+            if ((rc = dev_alloc(h, &I.cdf, (size_t)N * S * I.K))) return rc;
+            if ((rc = dev_alloc(h, &I.cdfj, (size_t)N * S * I.K))) return rc;
+            SP_CUDA_TRY(cudaMemsetAsync(I.ddiag, 0, sizeof(float) * N * S, h->st));
+            SP_CUDA_TRY(cudaMemsetAsync(I.cdf, 0, sizeof(float) * N * S * I.K, h->st));
+            SP_CUDA_TRY(cudaMemsetAsync(I.cdfj, 0, sizeof(int2) * N * S * I.K, h->st));
+        }
     }
     NsmInstance& d = I.desc;
     d.N = N;
@@ -443,9 +468,18 @@ int sp_run_start(sp_handle* h, const sp_run_args* a, sp_outputs* out) {
     for (int j = 0; j < ntraj; j++) {
         R.inst[j] = a->instance ? a->instance[j] : 0;
         if (R.inst[j] < 0 || R.inst[j] >= ninst) return fail(h, SP_E_INVALID, "instance index out of range");
-        if (!h->inst[R.inst[j]].is_static)
-            return fail(h, SP_E_UNSUPPORTED, "sp_run: moving (non-static) domains are run by sp_sdpd_advance");
         if (h->inst[R.inst[j]].S == 0) return fail(h, SP_E_INVALID, "sp_run: model has no species");
+        if (!h->inst[R.inst[j]].is_static) R.coupled = true;
+    }
+    if (R.coupled) {
+        // one shared flow: every trajectory runs the same moving instance
+        for (int j = 1; j < ntraj; j++)
+            if (R.inst[j] != R.inst[0])
+                return fail(h, SP_E_INVALID,
+                            "sp_run: the trajectories of a moving-domain model must all run one instance");
+        R.cinst = R.inst[0];
+        int rc0 = sdpd_reset(h->inst[R.cinst].sdpd, &h->err);
+        if (rc0) return rc0;
     }
     int rc = ensure_traj(h, ntraj, R.inst.data());
     if (rc) return rc;
@@ -540,8 +574,12 @@ int sp_run_start(sp_handle* h, const sp_run_args* a, sp_outputs* out) {
               (h->opt.nsm_variant == 2 || (h->opt.nsm_variant == 0 && minN >= 2048));
     // nsm_variant == 3: sequential register kernel only
     if (R.batch) R.warp_smem = batch_smem;
-    launch_nsm_init(h->d_trajs, h->d_insts, ntraj, max_leaf, max_levels, d_u0, st);
-    h->launches += 2 + max_levels;
+    h->last_kernel = R.batch ? SP_KERNEL_BATCH
+                   : R.variant != 0 ? SP_KERNEL_SEQUENTIAL : SP_KERNEL_GENERIC;
+    R.max_leaf = max_leaf;
+    R.max_levels = max_levels;
+    launch_nsm_init(h->d_trajs, h->d_insts, ntraj, max_leaf, max_levels, d_u0, !R.coupled, st);
+    h->launches += R.coupled ? 1 : 2 + max_levels;
     // output buffers
     const int nout = (int)h->output_steps.size();
     std::vector<long long> count_off(ntraj), mom_off(ninst);
@@ -570,12 +608,91 @@ int sp_run_start(sp_handle* h, const sp_run_args* a, sp_outputs* out) {
         cudaMemcpyAsync(R.d_moff, mom_off.data(), sizeof(long long) * ninst, cudaMemcpyHostToDevice, st);
         cudaMemsetAsync(R.d_mom, 0, sizeof(long long) * 2 * R.mtot, st);
     }
+    R.want_part = R.coupled && a->want_particles && out &&
+                  (out->particle_x || out->particle_v || out->particle_rho);
+    if (R.want_part) {
+        // particle outputs: [sum_i num_outputs * N_i (* 3)], instance-major
+        R.ptot = 0;
+        for (int i = 0; i < ninst; i++) {
+            if (i == R.cinst) R.poff = R.ptot;
+            R.ptot += (long long)nout * h->inst[i].N;
+        }
+        if (a->buffers_on_device) {
+            R.d_px = out->particle_x;
+            R.d_pv = out->particle_v;
+            R.d_prho = out->particle_rho;
+        } else {
+            if (out->particle_x && (rc = dmalloc((void**)&R.d_px, sizeof(double) * 3 * R.ptot))) return rc;
+            if (out->particle_v && (rc = dmalloc((void**)&R.d_pv, sizeof(double) * 3 * R.ptot))) return rc;
+            if (out->particle_rho && (rc = dmalloc((void**)&R.d_prho, sizeof(double) * R.ptot))) return rc;
+        }
+    }
+    R.step = 0;
     R.next_out = 0;
     R.result = SP_OK;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) { run_release(h); return spg_set_cuda_error(h, e, "sp_run_start", __FILE__, __LINE__); }
     // outputs at step 0 need no events
     return sp_run_continue(h, 0);
+}
+
+// Moving domain with species, steps R.step .. target-1 (simulate_threads.cpp:
+// 232-281 with simulate_rdme.cpp:53-68 on a non-static domain): per step the
+// SDPD step, the diffusion tables from its force-pass lists, the volumes from
+// the end-of-step density, every trajectory's queue rebuilt at step*dt
+// (Philox build index = step) and its events up to (step+1)*dt.  Statuses and
+// the flow's error flags are read once, at the target output.
+static int coupled_steps(sp_handle* h, int target, bool ref, long long budget, long long max_ns) {
+    RunState& R = h->run;
+    Instance& I = h->inst[R.cinst];
+    cudaStream_t st = h->st;
+    const int ntraj = R.args.num_trajectories;
+    cudaEventRecord(h->ea, st);
+    while (R.step < target) {
+        sdpd_enqueue_step(I.sdpd);
+        const SdpdLists L = sdpd_lists(I.sdpd);
+        if (L.f64)
+            launch_diffusion_tables(I.N, I.S, I.T, I.K, I.type, L.count, L.idx,
+                                    (const double*)L.dij, I.diffusion, I.ddiag, I.cdf, I.cdfj, st);
+        else
+            launch_diffusion_tables_f32(I.N, I.S, I.T, I.K, I.type, L.count, L.idx,
+                                        (const float*)L.dij, I.diffusion, I.ddiag, I.cdf, I.cdfj,
+                                        st);
+        sdpd_launch_volumes(I.sdpd, I.mass, I.vol, I.ivol);
+        launch_nsm_rebuild(h->d_trajs, h->d_insts, ntraj, R.max_leaf, R.max_levels,
+                           h->dt * (double)R.step, (uint32_t)R.step, st);
+        if (R.batch)
+            launch_nsm_batch(ref, R.variant, R.warp_smem, h->d_trajs, h->d_insts, ntraj,
+                             R.step + 1, h->dt, budget, max_ns, h->d_work, h->num_sms, st);
+        else
+            launch_nsm_advance(ref, R.smem_state, R.variant, R.warp_smem, R.wpb, h->d_trajs,
+                               h->d_insts, ntraj, R.step + 1, h->dt, budget, max_ns, h->d_work,
+                               h->num_sms, st);
+        h->launches += 3 + 1 + 1 + 2 + R.max_levels + 2;
+        R.step++;
+    }
+    cudaEventRecord(h->eb, st);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) { run_release(h); return spg_set_cuda_error(h, e, "coupled step", __FILE__, __LINE__); }
+    int rc = sdpd_check_flag(I.sdpd, &h->err);   // synchronises the stream
+    if (rc == SP_E_CUDA) { run_release(h); return rc; }
+    if (rc != SP_OK) { R.result = rc; return SP_OK; }
+    e = cudaMemcpyAsync(h->h_trajs.data(), h->d_trajs, sizeof(NsmTraj) * ntraj,
+                        cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) { run_release(h); return spg_set_cuda_error(h, e, "coupled step sync", __FILE__, __LINE__); }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, h->ea, h->eb);
+    h->adv_ms += ms;
+    // a step's events run in one launch: an exhausted budget or deadline
+    // there is an error, not a pause
+    for (int j = 0; j < ntraj; j++)
+        if (h->h_trajs[j].status != SP_TRAJ_OK) R.result = SP_E_TRAJECTORY;
+    if (R.result == SP_OK && R.args.timeout_s > 0) {
+        const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - R.wall0).count();
+        if (el > R.args.timeout_s) R.result = SP_E_TIMEOUT;
+    }
+    return SP_OK;
 }
 
 int sp_run_continue(sp_handle* h, int32_t num_outputs) {
@@ -596,7 +713,12 @@ int sp_run_continue(sp_handle* h, int32_t num_outputs) {
     SP_CUDA_TRY(cudaEventRecord(h->e0, st));
     while (R.next_out < nout && R.result == SP_OK) {
         const int target = h->output_steps[R.next_out];
-        if (target > 0) {
+        if (target > 0 && R.coupled) {
+            if (done >= num_outputs) break;
+            const int rc = coupled_steps(h, target, ref, budget, max_ns);
+            if (rc != SP_OK) return rc;
+            done++;
+        } else if (target > 0) {
             if (done >= num_outputs) break;
             for (;;) {
                 cudaEventRecord(h->ea, st);
@@ -646,6 +768,13 @@ int sp_run_continue(sp_handle* h, int32_t num_outputs) {
                                 R.d_coff, R.want_mom ? R.d_mom : nullptr, R.d_moff, R.next_out, st);
             h->launches++;
         }
+        if (R.want_part) {
+            const long long o = R.poff + (long long)R.next_out * h->inst[R.cinst].N;
+            sdpd_launch_state_out(h->inst[R.cinst].sdpd, R.d_px ? R.d_px + 3 * o : nullptr,
+                                  R.d_pv ? R.d_pv + 3 * o : nullptr,
+                                  R.d_prho ? R.d_prho + o : nullptr);
+            h->launches++;
+        }
         R.next_out++;
     }
     cudaEventRecord(h->e1, st);
@@ -682,6 +811,18 @@ int sp_run_finish(sp_handle* h) {
             cudaMemcpyAsync(R.out.counts, R.d_counts, sizeof(int32_t) * R.ctot, cudaMemcpyDeviceToHost, st);
         if (R.want_mom)
             cudaMemcpyAsync(R.out.moments, R.d_mom, sizeof(long long) * 2 * R.mtot, cudaMemcpyDeviceToHost, st);
+        if (R.want_part) {
+            const long long n = (long long)h->output_steps.size() * h->inst[R.cinst].N;
+            if (R.d_px)
+                cudaMemcpyAsync(R.out.particle_x + 3 * R.poff, R.d_px + 3 * R.poff,
+                                sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st);
+            if (R.d_pv)
+                cudaMemcpyAsync(R.out.particle_v + 3 * R.poff, R.d_pv + 3 * R.poff,
+                                sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st);
+            if (R.d_prho)
+                cudaMemcpyAsync(R.out.particle_rho + R.poff, R.d_prho + R.poff,
+                                sizeof(double) * n, cudaMemcpyDeviceToHost, st);
+        }
     }
     cudaMemcpyAsync(h->h_trajs.data(), h->d_trajs, sizeof(NsmTraj) * ntraj, cudaMemcpyDeviceToHost, st);
     cudaError_t e = cudaStreamSynchronize(st);
@@ -718,7 +859,7 @@ int sp_last_profile(sp_handle* h, sp_profile* p) {
     p->total_ms = h->last_ms;
     p->kernel_ms = h->adv_ms;
     p->launches = h->last_launches;
-    p->reserved = 0;
+    p->kernel = h->last_kernel;
     return SP_OK;
 }
 

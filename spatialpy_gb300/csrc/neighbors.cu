@@ -160,9 +160,11 @@ __global__ void neighbor_search_f64(const double* xq, const double* xt, int n, C
 
 // Ddiag[i,s] = sum_k D(s, type_j) D_ij (simulate_rdme.cpp:142-148) and the
 // running sums over the list scanned by the destination choice (:359-367),
-// accumulated in double in list order and rounded to float.
+// accumulated in double in list order and rounded to float.  D_ij comes in
+// double (static lists) or float (the FP32 flow's lists).
+template <typename DT>
 __global__ void diffusion_tables(int n, int S, int T, int kmax, const int* type, const int* count,
-                                 const int* idx, const double* dij, const double* diffusion,
+                                 const int* idx, const DT* dij, const double* diffusion,
                                  float* ddiag, float* cdf, int2* cdfj) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n * S) return;
@@ -171,7 +173,7 @@ __global__ void diffusion_tables(int n, int S, int T, int kmax, const int* type,
     for (int k = 0; k < count[i]; k++) {
         const int j = idx[(size_t)i * kmax + k];
         const double dc = diffusion[s * T + (type[j] - 1)];
-        acc = acc + dc * dij[(size_t)i * kmax + k];
+        acc = acc + dc * (double)dij[(size_t)i * kmax + k];
         const size_t o = ((size_t)i * S + s) * kmax + k;
         cdf[o] = (float)acc;
         cdfj[o] = make_int2(__float_as_int((float)acc), j);
@@ -243,8 +245,17 @@ void launch_diffusion_tables(int n, int S, int T, int kmax, const int* d_type, c
                              const int* d_idx, const double* d_dij, const double* d_diffusion,
                              float* d_ddiag, float* d_cdf, int2* d_cdfj, cudaStream_t st) {
     const int e = n * S;
-    diffusion_tables<<<(e + 255) / 256, 256, 0, st>>>(n, S, T, kmax, d_type, d_count, d_idx, d_dij,
-                                                      d_diffusion, d_ddiag, d_cdf, d_cdfj);
+    diffusion_tables<double><<<(e + 255) / 256, 256, 0, st>>>(
+        n, S, T, kmax, d_type, d_count, d_idx, d_dij, d_diffusion, d_ddiag, d_cdf, d_cdfj);
+}
+
+void launch_diffusion_tables_f32(int n, int S, int T, int kmax, const int* d_type,
+                                 const int* d_count, const int* d_idx, const float* d_dij,
+                                 const double* d_diffusion, float* d_ddiag, float* d_cdf,
+                                 int2* d_cdfj, cudaStream_t st) {
+    const int e = n * S;
+    diffusion_tables<float><<<(e + 255) / 256, 256, 0, st>>>(
+        n, S, T, kmax, d_type, d_count, d_idx, d_dij, d_diffusion, d_ddiag, d_cdf, d_cdfj);
 }
 
 }  // namespace spg

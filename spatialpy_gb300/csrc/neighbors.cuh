@@ -21,5 +21,9 @@ int run_neighbor_search(const double* d_xq, const double* d_xt, int n, const Cel
 void launch_diffusion_tables(int n, int S, int T, int kmax, const int* d_type, const int* d_count,
                              const int* d_idx, const double* d_dij, const double* d_diffusion,
                              float* d_ddiag, float* d_cdf, int2* d_cdfj, cudaStream_t st);
+void launch_diffusion_tables_f32(int n, int S, int T, int kmax, const int* d_type,
+                                 const int* d_count, const int* d_idx, const float* d_dij,
+                                 const double* d_diffusion, float* d_ddiag, float* d_cdf,
+                                 int2* d_cdfj, cudaStream_t st);
 
 }  // namespace spg

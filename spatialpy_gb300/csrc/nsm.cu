@@ -367,7 +367,9 @@ __global__ void __launch_bounds__(128) nsm_advance_generic(NsmTraj* trajs, const
                     const float ivolw = REF ? ivolv : I.ivol[w];
                     const bool samegrp = (w >> 5) == (v >> 5);
                     long long lgw = samegrp ? lgv : LF[(w & ~31) + lane];
-                    if (lane == sp) { xv -= 1; xw += 1; }               // :394-402
+                    // :394-402; a moving particle can list its own start-of-step
+                    // point, and a move onto itself leaves the count unchanged
+                    if (lane == sp && w != v) { xv -= 1; xw += 1; }
                     if (lane == sp) {
                         X[(size_t)v * S + sp] = xv;
                         X[(size_t)w * S + sp] = xw;
@@ -674,7 +676,11 @@ __global__ void __launch_bounds__(128) nsm_advance_small(NsmTraj* trajs, const N
                     int nxv = 0, nxw = 0;
 #pragma unroll
                     for (int s = 0; s < MS; s++)                      // :394-402
-                        if (s == sp) { xv[s] -= 1; xw[s] += 1; nxv = xv[s]; nxw = xw[s]; }
+                        if (s == sp) {
+                            if (w != v) { xv[s] -= 1; xw[s] += 1; }   // a move onto itself
+                            nxv = xv[s];
+                            nxw = xw[s];
+                        }
                     if (lane == 0) {
                         X[(size_t)v * S + sp] = nxv;
                         X[(size_t)w * S + sp] = nxw;
@@ -756,11 +762,32 @@ __global__ void nsm_copy_u0(NsmTraj* trajs, const NsmInstance* insts, int ntraj,
 // ---------------------------------------------------------------------------
 // host launchers
 // ---------------------------------------------------------------------------
+__global__ void nsm_reset_totals(NsmTraj* trajs, int ntraj) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < ntraj) trajs[j].a_tot = 0.0;
+}
+
+void launch_nsm_rebuild(NsmTraj* trajs, const NsmInstance* insts, int ntraj, int max_leaf,
+                        int max_levels, double t0, uint32_t build_index, cudaStream_t st) {
+    const int gx = (max_leaf + 255) / 256 < 64 ? (max_leaf + 255) / 256 : 64;
+    dim3 g(gx, ntraj);
+    nsm_reset_totals<<<(ntraj + 127) / 128, 128, 0, st>>>(trajs, ntraj);
+    nsm_init_leaves<<<g, 256, 0, st>>>(trajs, insts, ntraj, t0, build_index);
+    for (int l = 0; l < max_levels; l++) {
+        const int gbx = (max_leaf / 32 + 3) / 4 + 1 < 64 ? (max_leaf / 32 + 3) / 4 + 1 : 64;
+        nsm_build_level<<<dim3(gbx, ntraj), 128, 0, st>>>(trajs, insts, ntraj, l);
+    }
+}
+
+// u0 copy, then (build_queue) the queue at t = 0 with build index 0; a
+// moving domain builds its queues per step instead (launch_nsm_rebuild)
 void launch_nsm_init(NsmTraj* trajs, const NsmInstance* insts, int ntraj, int max_leaf,
-                     int max_levels, const uint32_t* const* u0, cudaStream_t st) {
+                     int max_levels, const uint32_t* const* u0, bool build_queue,
+                     cudaStream_t st) {
     const int gx = (max_leaf + 255) / 256 < 64 ? (max_leaf + 255) / 256 : 64;
     dim3 g(gx, ntraj);
     if (u0) nsm_copy_u0<<<g, 256, 0, st>>>(trajs, insts, ntraj, u0);
+    if (!build_queue) return;
     nsm_init_leaves<<<g, 256, 0, st>>>(trajs, insts, ntraj, 0.0, 0u);
     for (int l = 0; l < max_levels; l++) {
         const int gbx = (max_leaf / 32 + 3) / 4 + 1 < 64 ? (max_leaf / 32 + 3) / 4 + 1 : 64;

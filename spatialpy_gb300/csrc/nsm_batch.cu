@@ -396,7 +396,7 @@ __global__ void __launch_bounds__(32) nsm_advance_batch(NsmTraj* trajs, const Ns
                                 const float a0w = srr + sdr;
 #pragma unroll
                                 for (int s = 0; s < MS; s++)              // :394-402
-                                    if (s == sp) { xv[s] -= 1; xw[s] += 1; }
+                                    if (s == sp && w != v) { xv[s] -= 1; xw[s] += 1; }
                                 rates_small<MS, MR, EX>(Q, xv, dv, volv, ivolv, typev, srr, sdr);
                                 const float a1v = srr + sdr;
                                 rates_small<MS, MR, EX>(Q, xw, dw, volw, ivolw, typew, srr, sdr);

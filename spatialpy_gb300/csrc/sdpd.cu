@@ -58,6 +58,7 @@ struct SdpdDev {
     typename Vec4<R>::T* cpos;      // per cell slot: start-of-step position
     int *ncnt, *nidx;
     R *ndist, *ndw;
+    R* ndij;     // D_ij per list entry, or nullptr when no species diffuse
     int kcap;
     CellGrid g;
     int* flag;   // bit 1: list overflow, bit 2: NaN state, bit 4: cell overflow
@@ -208,6 +209,18 @@ __global__ void __launch_bounds__(TB) sdpd_pairs(SdpdDev<R> D, int first_step) {
         D.nidx[o] = j;
         D.ndist[o] = r;
         D.ndw[o] = dWdr;
+        if (D.ndij) {
+            // D_ij of add_to_neighbor_list (particle.cpp:181-187) from the
+            // post-predictor densities, in the reference's operator order
+            const R r2 = cd2[k * TB];
+            const R ih = (R)1.0 / h;
+            const R ihsq = ih * ih;
+            const R dhr = h - r;
+            const R wfd = (R)-25.066903536973515383 * dhr * dhr * ihsq * ihsq * ihsq * ih;
+            const R mj = D.mass[j], rj = D.rho[j];
+            D.ndij[o] = (R)-2.0 * (mi * mj) / (mi + mj) * (rhoi + rj) / (rhoi * rj) * r2 * wfd /
+                        (r2 + (R)0.01 * h * h);
+        }
         if (R_ > (R)1.0 || r == (R)0) continue;
         const auto xj = D.pos[j];
         const auto vj4 = D.vel[j];
@@ -351,6 +364,9 @@ struct SdpdState {
          *nu = nullptr, *ndist = nullptr, *ndw = nullptr;
     uint8_t* fixed = nullptr;
     int *ccnt = nullptr, *cidx = nullptr, *ncnt = nullptr, *nidx = nullptr, *flag = nullptr;
+    void* ndij = nullptr;
+    // initial state (REAL-typed 4-vectors and densities) for sdpd_reset
+    std::vector<unsigned char> init_pos, init_vel, init_rho;
     CellGrid grid{};
     cudaGraphExec_t graph20 = nullptr;   // 20 steps starting at a multiple of 20 (>= 20)
 };
@@ -389,6 +405,7 @@ static SdpdDev<R> dev_view(SdpdState* s) {
     D.fixed = s->fixed;
     D.ccnt = s->ccnt; D.cidx = s->cidx;
     D.ncnt = s->ncnt; D.nidx = s->nidx; D.ndist = (R*)s->ndist; D.ndw = (R*)s->ndw;
+    D.ndij = (R*)s->ndij;
     D.kcap = s->kcap;
     D.g = s->grid;
     D.flag = s->flag;
@@ -419,6 +436,9 @@ static bool upload(SdpdState* s, const sp_scenario& sc, std::string* err) {
         mass[i] = (R)sc.mass[i];
         nu[i] = (R)sc.nu[i];
     }
+    s->init_pos.assign((unsigned char*)pos.data(), (unsigned char*)pos.data() + v4);
+    s->init_vel.assign((unsigned char*)vel.data(), (unsigned char*)vel.data() + v4);
+    s->init_rho.assign((unsigned char*)rho.data(), (unsigned char*)rho.data() + r1);
     // F, Fbp, vt start at zero: the engine reads them before first writing
     // them (particle.cpp:70-83), the oracle zero-initialises them
     cudaMemcpyAsync(s->pos, pos.data(), v4, cudaMemcpyHostToDevice, s->st);
@@ -627,6 +647,113 @@ int sdpd_copy_neighbors(SdpdState* s, int kmax, int* count, int* idx, double* di
     (void)dij;
     return s->prec == SP_PREC_F64 ? copy_nbr_t<double>(s, kmax, count, idx, dist, dwdr, err)
                                   : copy_nbr_t<float>(s, kmax, count, idx, dist, dwdr, err);
+}
+
+// ---------------------------------------------------------------------------
+// coupling with the NSM (moving domain with species)
+// ---------------------------------------------------------------------------
+int sdpd_enable_dij(SdpdState* s, std::string* err) {
+    if (s->ndij) return SP_OK;
+    const size_t rb = s->prec == SP_PREC_F64 ? sizeof(double) : sizeof(float);
+    if (!sd_alloc(s, &s->ndij, rb * (size_t)s->N * s->kcap, err)) return SP_E_NOMEM;
+    return SP_OK;
+}
+
+int sdpd_reset(SdpdState* s, std::string* err) {
+    const size_t v4 = s->init_pos.size(), r1 = s->init_rho.size();
+    cudaMemcpyAsync(s->pos, s->init_pos.data(), v4, cudaMemcpyHostToDevice, s->st);
+    cudaMemcpyAsync(s->vel, s->init_vel.data(), v4, cudaMemcpyHostToDevice, s->st);
+    cudaMemsetAsync(s->vt, 0, v4, s->st);
+    cudaMemsetAsync(s->F, 0, v4, s->st);
+    cudaMemsetAsync(s->Fbp, 0, v4, s->st);
+    cudaMemcpyAsync(s->rho, s->init_rho.data(), r1, cudaMemcpyHostToDevice, s->st);
+    cudaMemcpyAsync(s->orho, s->init_rho.data(), r1, cudaMemcpyHostToDevice, s->st);
+    cudaMemsetAsync(s->ncnt, 0, sizeof(int) * s->N, s->st);
+    cudaMemsetAsync(s->flag, 0, sizeof(int), s->st);
+    cudaError_t e = cudaStreamSynchronize(s->st);   // host staging buffers stay valid
+    if (e != cudaSuccess) {
+        *err = std::string("SDPD reset: ") + cudaGetErrorString(e);
+        return SP_E_CUDA;
+    }
+    s->step = 0;
+    return SP_OK;
+}
+
+void sdpd_enqueue_step(SdpdState* s) {
+    if (s->prec == SP_PREC_F64) enqueue_step<double>(s, s->step);
+    else enqueue_step<float>(s, s->step);
+    s->step++;
+}
+
+SdpdLists sdpd_lists(SdpdState* s) {
+    SdpdLists L;
+    L.count = s->ncnt;
+    L.idx = s->nidx;
+    L.dij = s->ndij;
+    L.rho = s->rho;
+    L.kcap = s->kcap;
+    L.f64 = s->prec == SP_PREC_F64;
+    L.step = s->step;
+    return L;
+}
+
+template <typename R>
+__global__ void sdpd_volumes(int n, const double* mass, const R* rho, float* vol, float* ivol) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double r = (double)rho[i];
+    vol[i] = (float)(mass[i] / r);     // simulate_rdme.cpp:123, 247
+    ivol[i] = (float)(r / mass[i]);
+}
+
+void sdpd_launch_volumes(SdpdState* s, const double* mass, float* vol, float* ivol) {
+    const int n = s->N, tb = 256;
+    if (s->prec == SP_PREC_F64)
+        sdpd_volumes<double><<<(n + tb - 1) / tb, tb, 0, s->st>>>(n, mass, (const double*)s->rho, vol, ivol);
+    else
+        sdpd_volumes<float><<<(n + tb - 1) / tb, tb, 0, s->st>>>(n, mass, (const float*)s->rho, vol, ivol);
+}
+
+template <typename R>
+__global__ void sdpd_state_out(SdpdDev<R> D, double* x, double* v, double* rho) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= D.N) return;
+    const auto p = D.pos[i];
+    const auto u = D.vel[i];
+    if (x) { x[3 * i] = p.x; x[3 * i + 1] = p.y; x[3 * i + 2] = p.z; }
+    if (v) { v[3 * i] = u.x; v[3 * i + 1] = u.y; v[3 * i + 2] = u.z; }
+    if (rho) rho[i] = D.rho[i];
+}
+
+void sdpd_launch_state_out(SdpdState* s, double* x, double* v, double* rho) {
+    const int n = s->N, tb = 256;
+    if (s->prec == SP_PREC_F64)
+        sdpd_state_out<double><<<(n + tb - 1) / tb, tb, 0, s->st>>>(dev_view<double>(s), x, v, rho);
+    else
+        sdpd_state_out<float><<<(n + tb - 1) / tb, tb, 0, s->st>>>(dev_view<float>(s), x, v, rho);
+}
+
+int sdpd_check_flag(SdpdState* s, std::string* err) {
+    int flag = 0;
+    cudaMemcpyAsync(&flag, s->flag, sizeof(int), cudaMemcpyDeviceToHost, s->st);
+    cudaError_t e = cudaStreamSynchronize(s->st);
+    if (e != cudaSuccess) {
+        *err = std::string("SDPD step: ") + cudaGetErrorString(e);
+        return SP_E_CUDA;
+    }
+    if (flag & 1) {
+        *err = "SDPD: a particle has more neighbours than the list capacity (48)";
+        return SP_E_UNSUPPORTED;
+    }
+    if (flag & 4) {
+        *err = "SDPD: more than 16 particles in one cell of edge h";
+        return SP_E_UNSUPPORTED;
+    }
+    if (flag & 2) {
+        *err = "SDPD: NaN/inf in particle state (particle.cpp:88-126)";
+        return SP_E_TRAJECTORY;
+    }
+    return SP_OK;
 }
 
 }  // namespace spg

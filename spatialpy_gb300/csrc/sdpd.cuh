@@ -20,4 +20,26 @@ int sdpd_get_state(SdpdState* s, double* x, double* v, double* rho, std::string*
 int sdpd_copy_neighbors(SdpdState* s, int kmax, int* count, int* idx, double* dist, double* dwdr,
                         double* dij, std::string* err);
 
+// Coupling with the NSM on a moving domain (simulate_threads.cpp:232-281):
+// the lists of the last step's force pass with D_ij, and the flow state.
+struct SdpdLists {
+    int* count;      // [N]
+    int* idx;        // [N][kcap]
+    void* dij;       // [N][kcap] REAL (float, or double when f64)
+    void* rho;       // [N] REAL
+    int kcap;
+    bool f64;
+    int step;        // steps taken
+};
+int sdpd_enable_dij(SdpdState* s, std::string* err);            // lists carry D_ij from now on
+int sdpd_reset(SdpdState* s, std::string* err);                 // back to the initial state, step 0
+void sdpd_enqueue_step(SdpdState* s);                           // one step, no host sync
+SdpdLists sdpd_lists(SdpdState* s);
+// vol = m / rho, 1/vol = rho / m from the current densities (float)
+void sdpd_launch_volumes(SdpdState* s, const double* mass, float* vol, float* ivol);
+// device copies of the state in double (any pointer may be null)
+void sdpd_launch_state_out(SdpdState* s, double* x, double* v, double* rho);
+// synchronises; SP_OK or the error a step flagged (list/cell overflow, NaN)
+int sdpd_check_flag(SdpdState* s, std::string* err);
+
 }  // namespace spg

@@ -15,6 +15,9 @@ from . import abi
 from .abi import SpOptions, SpOutputs, SpRunArgs, SpTrajStatus, ptr
 
 
+KERNEL_NAMES = {1: "nsm_advance_generic", 2: "nsm_advance_small", 3: "nsm_advance_batch"}
+
+
 class EngineError(RuntimeError):
     def __init__(self, code: int, message: str):
         super().__init__(f"[{code}] {message}")
@@ -29,7 +32,8 @@ class Engine:
     scenarios : Scenario or list of Scenario
         Model instances (a list runs heterogeneous batches in one launch).
     sdpd_precision : "f32" or "f64"
-    nsm_variant : 0 autotuned, 1 sequential warp, 2 speculative batch warp
+    nsm_variant : 0 chosen per run, 1 generic sequential warp, 2 speculative batch
+        warp, 3 sequential register-resident warp
     """
 
     def __init__(self, scenarios, device: int = 0, sdpd_precision: str = "f32",
@@ -80,7 +84,8 @@ class Engine:
             raise EngineError(rc, self.error())
 
     # -- runs ----------------------------------------------------------------
-    def _prepare(self, seeds, instance, selection, want_counts, want_moments, u0, timeout):
+    def _prepare(self, seeds, instance, selection, want_counts, want_moments, u0, timeout,
+                 want_particles=False):
         seeds = np.ascontiguousarray(seeds, dtype=np.uint64).reshape(-1)
         nt = seeds.shape[0]
         inst = None
@@ -115,10 +120,22 @@ class Engine:
         out.counts = ptr(counts if want_counts else None, C.c_int32)
         out.moments = ptr(moments if want_moments else None, C.c_int64)
         out.event_counts = ptr(events, C.c_int64)
+        # moving domains: flow state at every output, instance-major
+        psizes = [T[i] * sc.num_particles for i, sc in enumerate(self.scenarios)]
+        np_tot = int(sum(psizes)) if want_particles else 0
+        px = np.zeros(3 * np_tot)
+        pv = np.zeros(3 * np_tot)
+        prho = np.zeros(np_tot)
+        args.want_particles = int(want_particles)
+        if want_particles:
+            out.particle_x = ptr(px, C.c_double)
+            out.particle_v = ptr(pv, C.c_double)
+            out.particle_rho = ptr(prho, C.c_double)
         # keep every buffer the C side points at alive for the run
         self._run = dict(seeds=seeds, inst=inst, u0s=u0s, u0p=u0p, args=args, out=out, T=T,
                          idx=idx, sizes=sizes, counts=counts, msizes=msizes, moments=moments,
-                         events=events, want_counts=want_counts, want_moments=want_moments)
+                         events=events, want_counts=want_counts, want_moments=want_moments,
+                         want_particles=want_particles, psizes=psizes, px=px, pv=pv, prho=prho)
         return self._run
 
     def _collect(self, rc):
@@ -147,19 +164,32 @@ class Engine:
                     T[i], sc.num_particles, sc.num_species, 2))
                 o += n
             res["moments"] = parts
+        if r["want_particles"]:
+            xs, vs, rs, o = [], [], [], 0
+            for i, sc in enumerate(self.scenarios):
+                n = r["psizes"][i]
+                xs.append(r["px"][3 * o:3 * (o + n)].reshape(T[i], sc.num_particles, 3))
+                vs.append(r["pv"][3 * o:3 * (o + n)].reshape(T[i], sc.num_particles, 3))
+                rs.append(r["prho"][o:o + n].reshape(T[i], sc.num_particles))
+                o += n
+            res["particles"] = list(zip(xs, vs, rs))
         return res
 
     def run(self, seeds, instance=None, selection: int = abi.SP_SELECT_EXACT,
             want_counts: bool = True, want_moments: bool = False, u0=None,
-            timeout: float | None = None):
+            timeout: float | None = None, want_particles: bool = False):
         """Run one trajectory per seed over the whole time span.
 
         Returns a dict with ``counts`` (list per trajectory of [T,N,S] int32
         arrays) when ``want_counts``, ``moments`` (list per instance of
         [T,N,S,2] int64 sums of x and x^2) when ``want_moments``, ``events``
-        ([ntraj,2] reaction/diffusion counts) and ``status`` codes.
+        ([ntraj,2] reaction/diffusion counts) and ``status`` codes.  On a
+        moving domain every trajectory shares the flow; ``want_particles``
+        adds ``particles`` (per instance: positions [T,N,3], velocities
+        [T,N,3], densities [T,N] at the outputs).
         """
-        r = self._prepare(seeds, instance, selection, want_counts, want_moments, u0, timeout)
+        r = self._prepare(seeds, instance, selection, want_counts, want_moments, u0, timeout,
+                          want_particles)
         rc = self.lib.sp_run(self._h, C.byref(r["args"]), C.byref(r["out"]))
         return self._collect(rc)
 
@@ -184,7 +214,8 @@ class Engine:
     def profile(self) -> dict:
         p = abi.SpProfile()
         self._check(self.lib.sp_last_profile(self._h, C.byref(p)))
-        return {"total_ms": p.total_ms, "kernel_ms": p.kernel_ms, "launches": p.launches}
+        return {"total_ms": p.total_ms, "kernel_ms": p.kernel_ms, "launches": p.launches,
+                "kernel": KERNEL_NAMES.get(p.kernel, "none")}
 
     def status(self, j: int) -> dict:
         st = SpTrajStatus()

@@ -209,11 +209,28 @@ class GpuSolver(_RefSolver):
         return first
 
     def _run_flow(self, seeds, times, timeout):
-        """Moving domain without species: the SDPD flow, particle state at
-        every output step."""
+        """Moving domain: the SDPD flow with particle state at every output;
+        with stochastic species, every trajectory's NSM runs over that one
+        flow (queues rebuilt each step, simulate_rdme.cpp:53-68)."""
         sc = self.scenario
-        if sc.num_species > 0 and sc.u0 is not None and sc.u0.sum() > 0:
-            raise SimulationError("moving domains with stochastic species are not supported yet")
+        if sc.num_species > 0 and sc.u0 is not None:
+            try:
+                res = self.engine.run(seeds, selection=self.selection, want_counts=True,
+                                      timeout=timeout, want_particles=True)
+            except EngineError as err:
+                raise SimulationError(f"Solver execution failed: {err}") from err
+            if res["rc"] not in (abi.SP_OK, abi.SP_E_TIMEOUT):
+                raise SimulationError(f"Solver execution failed: {res.get('error')}")
+            particles = res["particles"][0]
+            first = None
+            for j in range(len(seeds)):
+                r = GpuResult(self.model, sc, res["counts"][j], times, particles=particles)
+                r.timeout = res["rc"] == abi.SP_E_TIMEOUT
+                if first is None:
+                    first = r
+                else:
+                    first.append(r)
+            return first
         xs, vs, rs = [], [], []
         done = 0
         for step in sc.output_steps:

@@ -1,0 +1,23 @@
+"""Moving-domain scenarios with stochastic species, shared by the CPU and GPU
+tests of the coupled flow + NSM path."""
+import numpy as np
+
+from spatialpy_gb300 import scenario as S
+
+
+def dam_break_species(spacing_div=16, num_steps=60, num_outputs=4, D=0.05, molecules=2000,
+                      network="decay"):
+    """The dam break (fluid type 1, walls type 2) with one species S diffusing
+    in the fluid only.  network: "decay" (S -> 0), "full" (adds 0 -> S on
+    fluid particles, whose rate k*vol follows the changing density, and
+    2S -> 0, whose rate uses 1/vol), "none" (diffusion only)."""
+    sc = S.config_dam_break(spacing_div=spacing_div, num_steps=num_steps,
+                            num_outputs=num_outputs, species_D=D, molecules=molecules)
+    rxns = {"decay": [(0.01, {"S": 1}, {}, None)],
+            "full": [(0.5, {"S": 1}, {}, None), (2e5, {}, {"S": 1}, [1]),
+                     (2e-7, {"S": 2}, {}, None)],
+            "none": []}[network]
+    rate, kind, reac, allowed, jcN, irN, prN = S.mass_action(["S"], rxns, 2)
+    return sc.copy(rxn_rate=rate, rxn_kind=kind, rxn_reactants=reac.reshape(-1, 2),
+                   rxn_allowed=allowed, jcN=jcN, irN=irN, prN=prN,
+                   name=f"dam_break_species_{network}")

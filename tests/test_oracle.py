@@ -160,3 +160,27 @@ def test_sdpd_f32_close_to_f64_without_self_pairs(oracle_lib):
     b = oracle_lib.sdpd(sc, oracle_lib.SdpdState(sc), 41, "f32", 0)
     assert np.abs(a.x - b.x).max() <= 1e-6
     assert np.linalg.norm(a.v - b.v) <= 1e-3 * np.linalg.norm(a.v)
+
+
+def test_coupled_oracle_flow_and_species(oracle_lib):
+    """Moving domain with species (simulate_rdme.cpp:53-68 on a non-static
+    domain): the flow part equals the plain SDPD oracle stepped to each
+    output; molecules stay in the fluid (walls have D = 0); with diffusion
+    only the total is conserved; a rerun repeats every count."""
+    from .coupled_cases import dam_break_species
+    sc = dam_break_species(network="none", num_steps=41, num_outputs=3)
+    seeds = np.arange(3, dtype=np.uint64) + 11
+    out, ev, st, px, pr = oracle_lib.coupled_ensemble(sc, seeds)
+    assert (st == 0).all() and (ev[:, 1] > 0).all() and (ev[:, 0] == 0).all()
+    np.testing.assert_array_equal(out.sum(axis=(2, 3)), sc.u0.sum())
+    assert out[:, :, sc.type == 2].sum() == 0
+    flow = oracle_lib.SdpdState(sc)
+    done = 0
+    for k, step in enumerate(sc.output_steps):
+        oracle_lib.sdpd(sc, flow, int(step) - done, "f32", 6, kmax=48)
+        done = int(step)
+        np.testing.assert_array_equal(px[k], flow.x)
+        np.testing.assert_array_equal(pr[k], flow.rho)
+    out2, ev2, _, _, _ = oracle_lib.coupled_ensemble(sc, seeds)
+    np.testing.assert_array_equal(out, out2)
+    np.testing.assert_array_equal(ev, ev2)
