@@ -242,6 +242,89 @@ def run_sdpd(args):
                          "bytes_per_particle_step": B_SDPD}}
 
 
+COUPLED_TRAJ = 64
+
+
+def run_coupled(args, with_cpu: bool):
+    """Dam break with its advected species: 84,696 particles, one FP32 flow,
+    64 NSM trajectories of species S (D = 1e-3 in the fluid, decay 0.01,
+    50,000 molecules in the top 10 % of the fluid).  Per step: SDPD step,
+    diffusion tables from its lists, volumes, 64 queue rebuilds and the
+    step's events.  Device time of K steps after W warm-up steps."""
+    from spatialpy_gb300 import scenario as S
+    from spatialpy_gb300.engine import Engine
+    W, K = 20, args.coupled_steps
+    sc = S.config_dam_break(num_steps=W + K)
+    sc = sc.copy(output_steps=np.array([0, W, W + K], np.int32))
+    seeds = np.arange(SEED0, SEED0 + COUPLED_TRAJ, dtype=np.uint64)
+    with Engine(sc, sdpd_precision="f32") as eng:
+        eng.start(seeds)
+        eng.advance(1)
+        e0 = sum(eng.status(j)["events"] for j in range(COUPLED_TRAJ))
+        eng.advance(1)
+        prof = eng.profile()
+        e1 = sum(eng.status(j)["events"] for j in range(COUPLED_TRAJ))
+        eng.finish()
+    sec = prof["total_ms"] / 1e3
+    out = {"metric": "SDPD particle-steps/s (flow + 64 species trajectories)",
+           "value": sc.num_particles * K / sec, "unit": "particle-steps/s",
+           "events_per_s": (e1 - e0) / sec, "steps": K, "warmup": W,
+           "ms_per_step": prof["total_ms"] / K, "dtype": "f32 flow, int32 counts",
+           "gpu_launches": int(prof["launches"]), "event_kernel": prof["kernel"],
+           "config": {"workload": "dam break 84,696 particles + species S over 64 "
+                                  "trajectories (decay 0.01, D=1e-3 fluid only)",
+                      "particles": int(sc.num_particles), "trajectories": COUPLED_TRAJ}}
+    if with_cpu:
+        import oracle
+        oracle.build()
+        n = 3
+        sc3 = S.config_dam_break(num_steps=n, num_outputs=2)
+        t0 = time.perf_counter()
+        _, ev, _, _, _ = oracle.coupled_ensemble(sc3, seeds, want_particles=False,
+                                                 want_counts=False)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {
+            "value": sc3.num_particles * n / dt, "unit": "particle-steps/s",
+            "events_per_s": float(ev.sum() / dt), "cores": os.cpu_count() or 1,
+            "kind": "port",
+            "sample": f"first {n} steps, 64 trajectories: SDPD on one thread, trajectories "
+                      f"on all cores ({dt:.1f} s)"}
+    return out
+
+
+def run_uneven(args):
+    """Batched uneven ensemble: 4,096 birth-death instances (2-D/3-D
+    lattices, 400-40,000 voxels log-uniform, rates and D within +-1 decade),
+    one trajectory each, all in one persistent launch per output interval
+    (warps take trajectories from an atomic counter).  The ensemble's
+    propensity totals span 4 decades (up to 1e9 events per unit time in one
+    trajectory), so a bounded sample is timed: the first K output intervals
+    of 0.01 (t in [0, 10] cut into 1,000 intervals)."""
+    from spatialpy_gb300 import scenario as S
+    from spatialpy_gb300.engine import Engine
+    K = args.uneven_intervals
+    t0 = time.perf_counter()
+    scs = S.config_uneven_ensemble(num_intervals=1000)
+    build_s = time.perf_counter() - t0
+    n = len(scs)
+    seeds = np.arange(SEED0, SEED0 + n, dtype=np.uint64)
+    with Engine(scs) as eng:
+        eng.start(seeds, instance=np.arange(n, dtype=np.int32))
+        eng.advance(K)
+        prof = eng.profile()
+        ev = sum(eng.status(j)["events"] for j in range(n))
+        eng.finish()
+    sec = prof["total_ms"] / 1e3
+    vox = sum(sc.num_particles for sc in scs)
+    return {"metric": "SSA events/s (uneven ensemble)", "value": ev / sec, "unit": "events/s",
+            "intervals": K, "ms_per_interval": prof["total_ms"] / K,
+            "gpu_launches": int(prof["launches"]), "event_kernel": prof["kernel"],
+            "config": {"workload": "4,096 birth-death instances, 2-D/3-D, 400-40,000 "
+                                   "voxels log-uniform, one trajectory each, first "
+                                   f"{K} output interval(s) of 0.01", "voxels_total": int(vox),
+                       "host_setup_s": round(build_s, 1)}}
+
+
 def run_ours(args, world, rank, local, pg):
     import __graft_entry__ as g
     g.build()
@@ -294,6 +377,9 @@ def run_ours(args, world, rank, local, pg):
     d2h = r2["moments"][0].nbytes + r2["events"].nbytes
 
     sdpd = run_sdpd(args) if not args.skip_sdpd else None
+    coupled = (run_coupled(args, rank == 0 and not args.skip_cpu)
+               if not args.skip_sdpd and args.coupled_steps > 0 else None)
+    uneven = run_uneven(args) if args.uneven_intervals > 0 else None
 
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -316,6 +402,10 @@ def run_ours(args, world, rank, local, pg):
     }
     if sdpd is not None:
         out["secondary"] = sdpd
+    if coupled is not None:
+        out["secondary_coupled"] = coupled
+    if uneven is not None:
+        out["secondary_uneven"] = uneven
     if rank == 0 and not args.skip_cpu:
         out["cpu_baseline"] = cpu_baseline()
     return out
@@ -330,6 +420,10 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-sdpd", action="store_true")
     ap.add_argument("--sdpd-steps", type=int, default=200)
+    ap.add_argument("--uneven-intervals", type=int, default=1,
+                    help="timed intervals of the 4,096-instance uneven ensemble (0 = skip)")
+    ap.add_argument("--coupled-steps", type=int, default=100,
+                    help="timed steps of the flow + species workload (0 = skip)")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per event of the event-loop kernel from an ncu capture "
                          "(default: the committed capture's figure)")

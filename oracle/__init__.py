@@ -70,8 +70,9 @@ def lib():
                 [_p(C.c_double)] * 7 + [_p(C.c_int32), C.c_void_p]
         L.spo_coupled_ensemble.argtypes = [_p(SpScenario), _p(C.c_uint32), _p(C.c_uint64),
                                            C.c_int32, C.c_int32, C.c_int32, C.c_int32,
-                                           C.c_int32, _p(C.c_int32), _p(C.c_int64),
-                                           _p(C.c_int32), _p(C.c_double), _p(C.c_double)]
+                                           C.c_int32, C.c_int32, _p(C.c_int32),
+                                           _p(C.c_int64), _p(C.c_int32), _p(C.c_double),
+                                           _p(C.c_double)]
         _lib = L
     return _lib
 
@@ -184,7 +185,8 @@ def sdpd(sc, state: SdpdState, nsteps: int, precision: str = "f64", mode: int = 
 
 
 def coupled_ensemble(sc, seeds, selection: int = 0, precision: str = "f32", mode: int = 6,
-                     kmax: int = 48, u0=None, want_particles: bool = True):
+                     kmax: int = 48, u0=None, want_particles: bool = True, threads: int = 0,
+                     want_counts: bool = True):
     """Moving domain with species: the SDPD flow plus, every step, new
     diffusion tables, volumes and event queues for each trajectory.
     Returns (counts [ntraj,T,N,S], events [ntraj,2], status [ntraj],
@@ -193,14 +195,14 @@ def coupled_ensemble(sc, seeds, selection: int = 0, precision: str = "f32", mode
     seeds = np.ascontiguousarray(seeds, np.uint64)
     nt, T, n = len(seeds), len(sc.output_steps), sc.num_particles
     s = scenario_struct(sc)
-    out = np.zeros((nt, T, n, sc.num_species), np.int32)
+    out = np.zeros((nt, T, n, sc.num_species), np.int32) if want_counts else None
     ev = np.zeros((nt, 2), np.int64)
     st = np.zeros(nt, np.int32)
     px = np.zeros((T, n, 3)) if want_particles else None
     pr = np.zeros((T, n)) if want_particles else None
     rc = lib().spo_coupled_ensemble(C.byref(s), _ptr(u0, C.c_uint32), _ptr(seeds, C.c_uint64),
                                     nt, selection, 64 if precision == "f64" else 32, mode, kmax,
-                                    _ptr(out, C.c_int32), _ptr(ev, C.c_int64),
+                                    threads, _ptr(out, C.c_int32), _ptr(ev, C.c_int64),
                                     _ptr(st, C.c_int32), _ptr(px, C.c_double),
                                     _ptr(pr, C.c_double))
     if rc != 0:

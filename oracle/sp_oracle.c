@@ -600,11 +600,36 @@ int spo_nsm_ensemble(const sp_scenario *sc, const uint32_t *u0, const uint64_t *
  * Moving domain with species: the SDPD flow (shared by all trajectories)
  * and, every step, fresh diffusion tables, volumes and event queues.
  * ------------------------------------------------------------------------ */
+typedef struct {
+    const nsm_tables_t *t;
+    nsm_state_t *st;
+    int ntraj, step, selection, next;
+    pthread_mutex_t mu;
+} cstep_t;
+
+static void *coupled_worker(void *arg) {
+    cstep_t *c = (cstep_t *)arg;
+    for (;;) {
+        pthread_mutex_lock(&c->mu);
+        const int j = c->next++;
+        pthread_mutex_unlock(&c->mu);
+        if (j >= c->ntraj) break;
+        if (c->st[j].status != SP_TRAJ_OK) continue;
+        nsm_build(c->t, &c->st[j], c->t->sc->dt * (double)c->step, (uint32_t)c->step);
+        nsm_window(c->t, &c->st[j], c->step, c->selection);
+    }
+    return NULL;
+}
+
 int spo_coupled_ensemble(const sp_scenario *sc, const uint32_t *u0, const uint64_t *seeds,
                          int32_t ntraj, int32_t selection, int32_t precision, int32_t mode,
-                         int32_t kmax, int32_t *out, int64_t *ev, int32_t *status, double *px,
-                         double *prho) {
+                         int32_t kmax, int32_t threads, int32_t *out, int64_t *ev,
+                         int32_t *status, double *px, double *prho) {
     const int N = sc->num_particles, S = sc->num_species, R = sc->num_reactions;
+    int nth = threads <= 0 ? (int)sysconf(_SC_NPROCESSORS_ONLN) : threads;
+    if (nth > ntraj) nth = ntraj;
+    if (nth < 1) nth = 1;
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nth);
     const size_t NS = (size_t)N * S;
     double *x = (double *)malloc(sizeof(double) * 3 * N), *v = (double *)calloc(3 * N, sizeof(double));
     double *vt = (double *)calloc(3 * N, sizeof(double)), *F = (double *)calloc(3 * N, sizeof(double));
@@ -656,11 +681,14 @@ int spo_coupled_ensemble(const sp_scenario *sc, const uint32_t *u0, const uint64
             t.vol[i] = (float)(sc->mass[i] / rho[i]);
             t.ivol[i] = (float)(rho[i] / sc->mass[i]);
         }
-        /* nsm_core__initialize_heap at step*dt, then take_step (:53-68) */
-        for (int j = 0; j < ntraj; j++) {
-            if (st[j].status != SP_TRAJ_OK) continue;
-            nsm_build(&t, &st[j], sc->dt * (double)step, (uint32_t)step);
-            nsm_window(&t, &st[j], step, selection);
+        /* nsm_core__initialize_heap at step*dt, then take_step (:53-68);
+           trajectories are independent within a step */
+        cstep_t cs = {&t, st, ntraj, step, selection, 0, PTHREAD_MUTEX_INITIALIZER};
+        if (nth <= 1) {
+            coupled_worker(&cs);
+        } else {
+            for (int i = 0; i < nth; i++) pthread_create(&th[i], NULL, coupled_worker, &cs);
+            for (int i = 0; i < nth; i++) pthread_join(th[i], NULL);
         }
     }
     while (!rc && oi < nout) {
@@ -677,6 +705,7 @@ int spo_coupled_ensemble(const sp_scenario *sc, const uint32_t *u0, const uint64
         nsm_state_free(&st[j]);
     }
     free(st);
+    free(th);
     free(t.cdf); free(t.ddiag); free(t.vol); free(t.ivol); free(t.rate);
     free(L.count); free(L.idx); free(L.dij);
     free(x); free(v); free(vt); free(F); free(Fbp); free(rho); free(Frho);

@@ -90,14 +90,16 @@ int spo_sdpd_f32(const sp_scenario *sc, int32_t step0, int32_t nsteps, int32_t m
  * destination weights from that step's lists, the volumes m/rho from the
  * end-of-step density, and every trajectory's event queue at t = step*dt
  * (Philox build stream index = step), then runs that trajectory's events up
- * to (step+1)*dt.  out: [ntraj][num_outputs][N][S] counts or NULL; px/prho:
+ * to (step+1)*dt.  The SDPD step runs on one thread, the trajectories of a
+ * step on `threads` POSIX threads (0 = all cores).
+ * out: [ntraj][num_outputs][N][S] counts or NULL; px/prho:
  * [num_outputs][N*3] / [num_outputs][N] flow state or NULL; ev: [ntraj*2];
  * status: [ntraj].  Returns 0, -1 on a list overflow, 2 on NaN state.
  */
 int spo_coupled_ensemble(const sp_scenario *sc, const uint32_t *u0, const uint64_t *seeds,
                          int32_t ntraj, int32_t selection, int32_t precision, int32_t mode,
-                         int32_t kmax, int32_t *out, int64_t *ev, int32_t *status, double *px,
-                         double *prho);
+                         int32_t kmax, int32_t threads, int32_t *out, int64_t *ev,
+                         int32_t *status, double *px, double *prho);
 
 #ifdef __cplusplus
 }
