@@ -122,7 +122,9 @@ typedef struct sp_options {
     int32_t sdpd_precision;       /* SP_PREC_F32 (default) or SP_PREC_F64 */
     int32_t nsm_variant;          /* 0 = chosen per run: register-resident network when
                                      S <= 8 and R <= 16, speculative 32-event batches
-                                     when every domain has >= 2,048 voxels;
+                                     for domains of >= 2,048 voxels (static domains:
+                                     larger and smaller domains of one run go to the
+                                     two kernels, launched concurrently);
                                      1 = generic sequential warp kernel;
                                      2 = speculative batches wherever supported;
                                      3 = sequential register kernel */
@@ -229,6 +231,8 @@ typedef struct sp_profile {
 #define SP_KERNEL_GENERIC 1      /* nsm_advance_generic: any network, one warp per trajectory */
 #define SP_KERNEL_SEQUENTIAL 2   /* nsm_advance_small: register-resident network */
 #define SP_KERNEL_BATCH 3        /* nsm_advance_batch: speculative 32-event batches */
+#define SP_KERNEL_MIXED 4        /* batch kernel for domains of >= 2,048 voxels and
+                                    nsm_advance_small for the rest, concurrently */
 int sp_last_profile(sp_handle* h, sp_profile* p);
 
 /*

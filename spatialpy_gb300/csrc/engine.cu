@@ -28,12 +28,12 @@ int nsm_warp_smem(const NsmInstance& d, bool with_state);
 void launch_nsm_advance(bool ref, bool smem_state, int variant, int warp_smem, int wpb,
                         NsmTraj* trajs, const NsmInstance* insts, int ntraj, int step_end,
                         double dt, long long budget, long long max_ns, int* work, int num_sms,
-                        cudaStream_t st);
+                        const int* tlist, cudaStream_t st);
 int nsm_batch_smem(const NsmInstance& d);
 void launch_nsm_batch(bool ref, int variant, int warp_smem, NsmTraj* trajs,
                       const NsmInstance* insts, int ntraj, int step_end, double dt,
                       long long budget, long long max_ns, int* work, int num_sms,
-                      cudaStream_t st);
+                      const int* tlist, cudaStream_t st);
 void launch_nsm_snapshot(const NsmTraj* trajs, const NsmInstance* insts, int ntraj,
                          int32_t* counts, const long long* count_off, long long* moments,
                          const long long* mom_off, int out_index, cudaStream_t st);
@@ -72,6 +72,14 @@ struct Instance {
 
 }  // namespace
 
+// One event kernel and its launch shape over a set of trajectories.
+struct KernelGroup {
+    bool batch = false, smem_state = false;
+    int variant = 0, warp_smem = 0, wpb = 1;
+    std::vector<int> list;     // trajectories, in launch order
+    int* d_list = nullptr;     // device copy, or nullptr for 0..ntraj-1
+};
+
 struct RunState {
     bool active = false;
     sp_run_args args{};
@@ -79,8 +87,10 @@ struct RunState {
     std::vector<int> inst;
     std::vector<void*> tmp;
     std::chrono::steady_clock::time_point wall0;
-    bool smem_state = false, want_counts = false, want_mom = false, batch = false;
-    int warp_smem = 0, wpb = 1, variant = 0, next_out = 0, result = SP_OK;
+    bool want_counts = false, want_mom = false;
+    int next_out = 0, result = SP_OK;
+    KernelGroup grp[2];
+    int ngroups = 1;
     long long ctot = 0, mtot = 0;
     int32_t* d_counts = nullptr;
     long long *d_mom = nullptr, *d_coff = nullptr, *d_moff = nullptr;
@@ -95,8 +105,9 @@ struct RunState {
 struct sp_handle {
     int device = 0;
     int num_sms = 0;
-    cudaStream_t st = nullptr;
-    cudaEvent_t e0 = nullptr, e1 = nullptr, ea = nullptr, eb = nullptr;
+    cudaStream_t st = nullptr, st2 = nullptr;   // st2: the second kernel group
+    cudaEvent_t e0 = nullptr, e1 = nullptr, ea = nullptr, eb = nullptr, fork = nullptr,
+                join = nullptr;
     sp_options opt{};
     std::vector<Instance> inst;
     std::vector<void*> allocs;
@@ -379,6 +390,9 @@ int sp_create(const sp_scenario* scenarios, int32_t num_scenarios, const sp_opti
     SP_CUDA_TRY(cudaEventCreate(&h->e1));
     SP_CUDA_TRY(cudaEventCreate(&h->ea));
     SP_CUDA_TRY(cudaEventCreate(&h->eb));
+    SP_CUDA_TRY(cudaStreamCreateWithFlags(&h->st2, cudaStreamNonBlocking));
+    SP_CUDA_TRY(cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming));
+    SP_CUDA_TRY(cudaEventCreateWithFlags(&h->join, cudaEventDisableTiming));
     h->dt = s0.dt;
     h->num_steps = s0.num_steps;
     h->output_steps.assign(s0.output_steps, s0.output_steps + s0.num_outputs);
@@ -391,7 +405,7 @@ int sp_create(const sp_scenario* scenarios, int32_t num_scenarios, const sp_opti
     }
     int rc = dev_upload(h, &h->d_insts, descs.data(), descs.size());
     if (rc) return rc;
-    if ((rc = dev_alloc(h, &h->d_work, 1))) return rc;
+    if ((rc = dev_alloc(h, &h->d_work, 2))) return rc;
     SP_CUDA_TRY(cudaStreamSynchronize(h->st));
     return SP_OK;
 }
@@ -447,6 +461,78 @@ static void run_release(sp_handle* h) {
     for (void* p : R.tmp) cudaFree(p);
     R.tmp.clear();
     R.active = false;
+}
+
+// register-resident network variant for the trajectories `js` (0 = generic)
+static int net_variant(sp_handle* h, const std::vector<int>& js, const std::vector<int>& inst) {
+    int minS = 1 << 30, minR = 1 << 30, maxS = 0, maxR = 0, maxT = 0;
+    for (int j : js) {
+        const Instance& I = h->inst[inst[j]];
+        minS = std::min(minS, I.S);
+        minR = std::min(minR, I.R);
+        maxS = std::max(maxS, I.S);
+        maxR = std::max(maxR, I.R);
+        maxT = std::max(maxT, I.T);
+    }
+    if (h->opt.nsm_variant == 1) return 0;   // the generic warp kernel, forced
+    if (maxT < 64 && minS == maxS && minR == maxR && maxS == 1 && maxR == 2) return 3;
+    if (maxT < 64 && minS == maxS && minR == maxR && maxS == 3 && maxR == 4) return 4;
+    if (maxT < 64 && maxS <= 4 && maxR <= 8) return 1;
+    if (maxT < 64 && maxS <= 8 && maxR <= 16) return 2;
+    return 0;
+}
+
+// kernel and launch shape for the trajectories `js`
+static int choose_group(sp_handle* h, const RunState& R, const std::vector<int>& js,
+                        bool want_batch, KernelGroup& G) {
+    int state_bytes = 0, tree_bytes = 0, batch_bytes = 0;
+    for (int j : js) {
+        const NsmInstance& d = h->inst[R.inst[j]].desc;
+        state_bytes = std::max(state_bytes, nsm_warp_smem(d, true));
+        tree_bytes = std::max(tree_bytes, nsm_warp_smem(d, false));
+        batch_bytes = std::max(batch_bytes, nsm_batch_smem(d));
+    }
+    G.list = js;
+    // shared-memory policy: whole trajectory state when it fits in 48 KB per
+    // warp, else the tree only (levels >= 1, 12 bytes per node)
+    G.smem_state = state_bytes <= 48 * 1024;
+    G.warp_smem = G.smem_state ? state_bytes : tree_bytes;
+    if (G.warp_smem > 200 * 1024)
+        return fail(h, SP_E_UNSUPPORTED, "domain too large for the shared-memory event queue");
+    G.wpb = G.warp_smem <= 24 * 1024 ? 4 : G.warp_smem <= 48 * 1024 ? 2 : 1;
+    G.variant = net_variant(h, js, R.inst);
+    // speculative batches need a register-resident network
+    G.batch = want_batch && G.variant != 0 && batch_bytes <= 200 * 1024;
+    if (G.batch) G.warp_smem = batch_bytes;
+    return SP_OK;
+}
+
+// one launch of every kernel group, to step_end; group 1 runs on st2
+static void launch_groups(sp_handle* h, bool ref, int step_end, long long budget,
+                          long long max_ns) {
+    RunState& R = h->run;
+    const int ntraj = R.args.num_trajectories;
+    for (int g = 0; g < R.ngroups; g++) {
+        KernelGroup& G = R.grp[g];
+        cudaStream_t s = g == 0 ? h->st : h->st2;
+        if (g == 1) {
+            cudaEventRecord(h->fork, h->st);
+            cudaStreamWaitEvent(h->st2, h->fork, 0);
+        }
+        const int n = R.ngroups == 1 ? ntraj : (int)G.list.size();
+        const int* tl = R.ngroups == 1 ? nullptr : G.d_list;
+        if (G.batch)
+            launch_nsm_batch(ref, G.variant, G.warp_smem, h->d_trajs, h->d_insts, n, step_end,
+                             h->dt, budget, max_ns, h->d_work + g, h->num_sms, tl, s);
+        else
+            launch_nsm_advance(ref, G.smem_state, G.variant, G.warp_smem, G.wpb, h->d_trajs,
+                               h->d_insts, n, step_end, h->dt, budget, max_ns, h->d_work + g,
+                               h->num_sms, tl, s);
+    }
+    if (R.ngroups == 2) {
+        cudaEventRecord(h->join, h->st2);
+        cudaStreamWaitEvent(h->st, h->join, 0);
+    }
 }
 
 int sp_run_start(sp_handle* h, const sp_run_args* a, sp_outputs* out) {
@@ -529,57 +615,58 @@ int sp_run_start(sp_handle* h, const sp_run_args* a, sp_outputs* out) {
     const uint32_t** d_u0 = nullptr;
     if ((rc = dmalloc((void**)&d_u0, sizeof(void*) * ninst))) return rc;
     cudaMemcpyAsync(d_u0, u0ptr.data(), sizeof(void*) * ninst, cudaMemcpyHostToDevice, st);
-    int max_leaf = 0, max_levels = 0, smem_state_bytes = 0, smem_tree_bytes = 0;
-    int maxS = 0, maxR = 0, maxT = 0;
+    int max_leaf = 0, max_levels = 0;
     for (int j = 0; j < ntraj; j++) {
-        const Instance& I = h->inst[R.inst[j]];
-        const NsmInstance& d = I.desc;
+        const NsmInstance& d = h->inst[R.inst[j]].desc;
         max_leaf = std::max(max_leaf, d.leaf_stride);
         max_levels = std::max(max_levels, d.levels);
-        smem_state_bytes = std::max(smem_state_bytes, nsm_warp_smem(d, true));
-        smem_tree_bytes = std::max(smem_tree_bytes, nsm_warp_smem(d, false));
-        maxS = std::max(maxS, I.S);
-        maxR = std::max(maxR, I.R);
-        maxT = std::max(maxT, I.T);
     }
-    // shared-memory policy: whole trajectory state when it fits in 48 KB per
-    // warp, else the tree only (levels >= 1, 12 bytes per node)
-    R.smem_state = smem_state_bytes <= 48 * 1024;
-    R.warp_smem = R.smem_state ? smem_state_bytes : smem_tree_bytes;
-    if (R.warp_smem > 200 * 1024) {
-        run_release(h);
-        return fail(h, SP_E_UNSUPPORTED, "domain too large for the shared-memory event queue");
+    // kernel groups: with the default policy, domains of >= 2,048 voxels
+    // (64 voxel groups) run the speculative batch kernel and smaller ones a
+    // sequential kernel, the two groups concurrently on two streams
+    std::vector<int> all(ntraj), big, small;
+    for (int j = 0; j < ntraj; j++) all[j] = j;
+    if (h->opt.nsm_variant == 0) {
+        for (int j = 0; j < ntraj; j++) {
+            const Instance& I = h->inst[R.inst[j]];
+            const bool eligible = I.N >= 2048 && net_variant(h, {j}, R.inst) != 0 &&
+                                  nsm_batch_smem(I.desc) <= 200 * 1024;
+            (eligible ? big : small).push_back(j);
+        }
     }
-    R.wpb = R.warp_smem <= 24 * 1024 ? 4 : R.warp_smem <= 48 * 1024 ? 2 : 1;
-    // kernel variant: register-resident networks when small enough
-    int minS = 1 << 30, minR = 1 << 30;
-    for (int j = 0; j < ntraj; j++) {
-        minS = std::min(minS, h->inst[R.inst[j]].S);
-        minR = std::min(minR, h->inst[R.inst[j]].R);
+    if (!big.empty() && !small.empty()) {
+        R.ngroups = 2;
+        rc = choose_group(h, R, big, true, R.grp[0]);
+        if (rc == SP_OK) rc = choose_group(h, R, small, false, R.grp[1]);
+    } else {
+        R.ngroups = 1;
+        const bool want_batch = h->opt.nsm_variant == 2 || (h->opt.nsm_variant == 0 && !big.empty());
+        rc = choose_group(h, R, all, want_batch, R.grp[0]);
     }
-    R.variant = 0;
-    if (maxT < 64 && minS == maxS && minR == maxR && maxS == 1 && maxR == 2) R.variant = 3;
-    else if (maxT < 64 && minS == maxS && minR == maxR && maxS == 3 && maxR == 4) R.variant = 4;
-    else if (maxT < 64 && maxS <= 4 && maxR <= 8) R.variant = 1;
-    else if (maxT < 64 && maxS <= 8 && maxR <= 16) R.variant = 2;
-    if (h->opt.nsm_variant == 1) R.variant = 0;   // force the generic warp kernel
-    // speculative batches for domains of >= 2,048 voxels (64 voxel groups)
-    // with register-resident networks; forced by nsm_variant == 2
-    int minN = 1 << 30, batch_smem = 0;
-    for (int j = 0; j < ntraj; j++) {
-        minN = std::min(minN, h->inst[R.inst[j]].N);
-        batch_smem = std::max(batch_smem, nsm_batch_smem(h->inst[R.inst[j]].desc));
-    }
-    R.batch = R.variant != 0 && batch_smem <= 200 * 1024 &&
-              (h->opt.nsm_variant == 2 || (h->opt.nsm_variant == 0 && minN >= 2048));
-    // nsm_variant == 3: sequential register kernel only
-    if (R.batch) R.warp_smem = batch_smem;
-    h->last_kernel = R.batch ? SP_KERNEL_BATCH
-                   : R.variant != 0 ? SP_KERNEL_SEQUENTIAL : SP_KERNEL_GENERIC;
+    if (rc) { run_release(h); return rc; }
+    h->last_kernel = R.ngroups == 2 ? SP_KERNEL_MIXED
+                   : R.grp[0].batch ? SP_KERNEL_BATCH
+                   : R.grp[0].variant != 0 ? SP_KERNEL_SEQUENTIAL : SP_KERNEL_GENERIC;
     R.max_leaf = max_leaf;
     R.max_levels = max_levels;
     launch_nsm_init(h->d_trajs, h->d_insts, ntraj, max_leaf, max_levels, d_u0, !R.coupled, st);
     h->launches += R.coupled ? 1 : 2 + max_levels;
+    if (R.ngroups == 2) {
+        // largest total propensity first, so the longest trajectories start
+        // first (longest-processing-time order)
+        SP_CUDA_TRY(cudaMemcpyAsync(h->h_trajs.data(), h->d_trajs, sizeof(NsmTraj) * ntraj,
+                                    cudaMemcpyDeviceToHost, st));
+        SP_CUDA_TRY(cudaStreamSynchronize(st));
+        for (int g = 0; g < 2; g++) {
+            KernelGroup& G = R.grp[g];
+            std::stable_sort(G.list.begin(), G.list.end(), [&](int a, int b) {
+                return h->h_trajs[a].a_tot > h->h_trajs[b].a_tot;
+            });
+            if ((rc = dmalloc((void**)&G.d_list, sizeof(int) * G.list.size()))) return rc;
+            SP_CUDA_TRY(cudaMemcpyAsync(G.d_list, G.list.data(), sizeof(int) * G.list.size(),
+                                        cudaMemcpyHostToDevice, st));
+        }
+    }
     // output buffers
     const int nout = (int)h->output_steps.size();
     std::vector<long long> count_off(ntraj), mom_off(ninst);
@@ -661,14 +748,8 @@ static int coupled_steps(sp_handle* h, int target, bool ref, long long budget, l
         sdpd_launch_volumes(I.sdpd, I.mass, I.vol, I.ivol);
         launch_nsm_rebuild(h->d_trajs, h->d_insts, ntraj, R.max_leaf, R.max_levels,
                            h->dt * (double)R.step, (uint32_t)R.step, st);
-        if (R.batch)
-            launch_nsm_batch(ref, R.variant, R.warp_smem, h->d_trajs, h->d_insts, ntraj,
-                             R.step + 1, h->dt, budget, max_ns, h->d_work, h->num_sms, st);
-        else
-            launch_nsm_advance(ref, R.smem_state, R.variant, R.warp_smem, R.wpb, h->d_trajs,
-                               h->d_insts, ntraj, R.step + 1, h->dt, budget, max_ns, h->d_work,
-                               h->num_sms, st);
-        h->launches += 3 + 1 + 1 + 2 + R.max_levels + 2;
+        launch_groups(h, ref, R.step + 1, budget, max_ns);
+        h->launches += 3 + 1 + 1 + 2 + R.max_levels + 1;
         R.step++;
     }
     cudaEventRecord(h->eb, st);
@@ -722,15 +803,9 @@ int sp_run_continue(sp_handle* h, int32_t num_outputs) {
             if (done >= num_outputs) break;
             for (;;) {
                 cudaEventRecord(h->ea, st);
-                if (R.batch)
-                    launch_nsm_batch(ref, R.variant, R.warp_smem, h->d_trajs, h->d_insts, ntraj,
-                                     target, h->dt, budget, max_ns, h->d_work, h->num_sms, st);
-                else
-                    launch_nsm_advance(ref, R.smem_state, R.variant, R.warp_smem, R.wpb, h->d_trajs,
-                                       h->d_insts, ntraj, target, h->dt, budget, max_ns, h->d_work,
-                                       h->num_sms, st);
+                launch_groups(h, ref, target, budget, max_ns);
                 cudaEventRecord(h->eb, st);
-                h->launches++;
+                h->launches += R.ngroups;
                 cudaError_t e = cudaGetLastError();
                 if (e != cudaSuccess) { run_release(h); return spg_set_cuda_error(h, e, "nsm_advance", __FILE__, __LINE__); }
                 e = cudaMemcpyAsync(h->h_trajs.data(), h->d_trajs, sizeof(NsmTraj) * ntraj,
@@ -895,6 +970,9 @@ void sp_destroy(sp_handle* h) {
     if (h->e1) cudaEventDestroy(h->e1);
     if (h->ea) cudaEventDestroy(h->ea);
     if (h->eb) cudaEventDestroy(h->eb);
+    if (h->fork) cudaEventDestroy(h->fork);
+    if (h->join) cudaEventDestroy(h->join);
+    if (h->st2) cudaStreamDestroy(h->st2);
     if (h->st) cudaStreamDestroy(h->st);
     delete h;
 }

@@ -193,7 +193,7 @@ template <bool REF, bool SMEM_STATE>
 __global__ void __launch_bounds__(128) nsm_advance_generic(NsmTraj* trajs, const NsmInstance* insts,
                                                    int ntraj, int step_end, double dt,
                                                    long long budget, long long max_ns, int* work,
-                                                   int warp_smem_bytes) {
+                                                   int warp_smem_bytes, const int* tlist) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31;
     unsigned char* wsm = smem + (size_t)(threadIdx.x >> 5) * warp_smem_bytes;
@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(128) nsm_advance_generic(NsmTraj* trajs, const
         if (lane == 0) j = atomicAdd(work, 1);
         j = __shfl_sync(SP_FULL, j, 0);
         if (j >= ntraj) return;
-        NsmTraj& T = trajs[j];
+        NsmTraj& T = trajs[tlist ? tlist[j] : j];
         if (T.status != SP_TRAJ_OK || T.step >= step_end) continue;
         const NsmInstance& I = insts[T.inst];
         const int S = I.S, K = I.K, NN = I.num_nodes;
@@ -464,7 +464,8 @@ template <bool REF, bool SMEM_STATE, int MS, int MR, bool EX>
 __global__ void __launch_bounds__(128) nsm_advance_small(NsmTraj* trajs, const NsmInstance* insts,
                                                          int ntraj, int step_end, double dt,
                                                          long long budget, long long max_ns,
-                                                         int* work, int warp_smem_bytes) {
+                                                         int* work, int warp_smem_bytes,
+                                                         const int* tlist) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31;
     unsigned char* wsm = smem + (size_t)(threadIdx.x >> 5) * warp_smem_bytes;
@@ -473,7 +474,7 @@ __global__ void __launch_bounds__(128) nsm_advance_small(NsmTraj* trajs, const N
         if (lane == 0) j = atomicAdd(work, 1);
         j = __shfl_sync(SP_FULL, j, 0);
         if (j >= ntraj) return;
-        NsmTraj& T = trajs[j];
+        NsmTraj& T = trajs[tlist ? tlist[j] : j];
         if (T.status != SP_TRAJ_OK || T.step >= step_end) continue;
         const NsmInstance& I = insts[T.inst];
         const int S = I.S, K = I.K, NN = I.num_nodes;
@@ -805,7 +806,7 @@ int nsm_warp_smem(const NsmInstance& d, bool with_state) {
 }
 
 typedef void (*AdvanceFn)(NsmTraj*, const NsmInstance*, int, int, double, long long, long long,
-                          int*, int);
+                          int*, int, const int*);
 
 template <bool REF, bool SM>
 static AdvanceFn pick_kernel(int variant) {
@@ -820,10 +821,12 @@ static AdvanceFn pick_kernel(int variant) {
 
 // variant: 0 generic (any S, R); 1 small (S <= 4, R <= 8); 2 small (S <= 8,
 // R <= 16); 3 exactly S = 1, R = 2; 4 exactly S = 3, R = 4
+// tlist: the trajectories to advance (ntraj entries, taken in order), or
+// nullptr for 0..ntraj-1
 void launch_nsm_advance(bool ref, bool smem_state, int variant, int warp_smem, int wpb,
                         NsmTraj* trajs, const NsmInstance* insts, int ntraj, int step_end,
                         double dt, long long budget, long long max_ns, int* work, int num_sms,
-                        cudaStream_t st) {
+                        const int* tlist, cudaStream_t st) {
     cudaMemsetAsync(work, 0, sizeof(int), st);
     // one warp per block until every SM has a block
     if (ntraj <= 2 * num_sms) wpb = 1;
@@ -837,7 +840,7 @@ void launch_nsm_advance(bool ref, bool smem_state, int variant, int warp_smem, i
                        : (smem_state ? pick_kernel<false, true>(variant) : pick_kernel<false, false>(variant));
     cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     fn<<<blocks, wpb * 32, smem, st>>>(trajs, insts, ntraj, step_end, dt, budget, max_ns, work,
-                                       warp_smem);
+                                       warp_smem, tlist);
 }
 
 void launch_nsm_snapshot(const NsmTraj* trajs, const NsmInstance* insts, int ntraj,

@@ -163,7 +163,7 @@ template <bool REF, int MS, int MR, bool EX>
 __global__ void __launch_bounds__(32) nsm_advance_batch(NsmTraj* trajs, const NsmInstance* insts,
                                                         int ntraj, int step_end, double dt,
                                                         long long budget, long long max_ns,
-                                                        int* work) {
+                                                        int* work, const int* tlist) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31;
     const unsigned ltm = (1u << lane) - 1u;
@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(32) nsm_advance_batch(NsmTraj* trajs, const Ns
         if (lane == 0) jt = atomicAdd(work, 1);
         jt = __shfl_sync(SP_FULL, jt, 0);
         if (jt >= ntraj) return;
-        NsmTraj& T = trajs[jt];
+        NsmTraj& T = trajs[tlist ? tlist[jt] : jt];
         if (T.status != SP_TRAJ_OK || T.step >= step_end) continue;
         const NsmInstance& I = insts[T.inst];
         const int S = I.S, K = I.K, NN = I.num_nodes, N1 = I.level_size[1], L = I.levels;
@@ -538,7 +538,8 @@ __global__ void __launch_bounds__(32) nsm_advance_batch(NsmTraj* trajs, const Ns
     }
 }
 
-typedef void (*BatchFn)(NsmTraj*, const NsmInstance*, int, int, double, long long, long long, int*);
+typedef void (*BatchFn)(NsmTraj*, const NsmInstance*, int, int, double, long long, long long, int*,
+                        const int*);
 
 template <bool REF>
 static BatchFn pick_batch(int variant) {
@@ -553,7 +554,7 @@ static BatchFn pick_batch(int variant) {
 void launch_nsm_batch(bool ref, int variant, int warp_smem, NsmTraj* trajs,
                       const NsmInstance* insts, int ntraj, int step_end, double dt,
                       long long budget, long long max_ns, int* work, int num_sms,
-                      cudaStream_t st) {
+                      const int* tlist, cudaStream_t st) {
     cudaMemsetAsync(work, 0, sizeof(int), st);
     const int per_sm = (200 * 1024) / warp_smem > 0 ? (200 * 1024) / warp_smem : 1;
     int blocks = ntraj;
@@ -561,7 +562,8 @@ void launch_nsm_batch(bool ref, int variant, int warp_smem, NsmTraj* trajs,
     if (blocks > cap) blocks = cap;
     BatchFn fn = ref ? pick_batch<true>(variant) : pick_batch<false>(variant);
     cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    fn<<<blocks, 32, warp_smem, st>>>(trajs, insts, ntraj, step_end, dt, budget, max_ns, work);
+    fn<<<blocks, 32, warp_smem, st>>>(trajs, insts, ntraj, step_end, dt, budget, max_ns, work,
+                                      tlist);
 }
 
 }  // namespace spg

@@ -15,7 +15,8 @@ from . import abi
 from .abi import SpOptions, SpOutputs, SpRunArgs, SpTrajStatus, ptr
 
 
-KERNEL_NAMES = {1: "nsm_advance_generic", 2: "nsm_advance_small", 3: "nsm_advance_batch"}
+KERNEL_NAMES = {1: "nsm_advance_generic", 2: "nsm_advance_small", 3: "nsm_advance_batch",
+                4: "nsm_advance_batch+nsm_advance_small"}
 
 
 class EngineError(RuntimeError):

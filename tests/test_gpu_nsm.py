@@ -302,3 +302,22 @@ def test_exact_mode_matches_rescaled_reference_ensemble():
         gm, gv, gn = g[f"{tag}/total_mean"], g[f"{tag}/total_var"], int(g[f"{tag}/ntraj"])
         se = np.sqrt(v / n + gv / gn)
         assert np.all(np.abs(m - gm)[1:] <= 3.29 * se[1:] + 1e-9), (tag, m, gm)
+
+
+def test_mixed_kernel_groups_bitexact(oracle_lib):
+    """Domains of >= 2,048 voxels go to the speculative batch kernel and the
+    others to the sequential kernel, launched concurrently, each group in
+    descending order of total propensity; trajectories stay bit-exact."""
+    scs = [S.config_birth_death_2d(n=50, count=200, D=0.02, t_end=2.0, num_points=3, dt=1.0),
+           S.config_birth_death_2d(n=7, count=30, t_end=2.0, num_points=3, dt=1.0),
+           S.config_birth_death_2d(n=64, count=100, D=0.02, t_end=2.0, num_points=3, dt=1.0)]
+    inst = np.array([0, 1, 2, 1, 0, 2, 1], np.int32)
+    seeds = np.arange(70, 77, dtype=np.uint64)
+    with _engine(scs) as eng:
+        res = eng.run(seeds, instance=inst)
+        assert eng.profile()["kernel"] == "nsm_advance_batch+nsm_advance_small"
+    assert res["rc"] == abi.SP_OK, res.get("error")
+    for j, s in enumerate(seeds):
+        out, ev, _ = oracle_lib.nsm_trajectory(scs[inst[j]], int(s), 0)
+        np.testing.assert_array_equal(res["counts"][j], out, err_msg=f"trajectory {j}")
+        np.testing.assert_array_equal(res["events"][j], ev)
