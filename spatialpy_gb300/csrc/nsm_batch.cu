@@ -36,22 +36,26 @@ constexpr int kFront = 64;
 int nsm_batch_smem(const NsmInstance& d) {
     size_t b = (size_t)d.num_nodes * 8 + (size_t)d.level_size[1] * 8 + (size_t)d.num_nodes * 4;
     b += 2 * kFront * 4;
+    b += (size_t)(d.num_nodes - d.level_size[1]) * 4;   // repair flags, levels >= 2
     return (int)((b + 15) / 16 * 16);
 }
 
-// Level-1 nodes with time < thb, into lane-held (ct, ci, ct2).  Returns the
-// count, or -1 when more than 32 (or a frontier overflow).
+// Level-1 nodes with time < thb, into lane-held (ct, ci).  Returns the
+// count, or -1 when more than 32 (or a frontier overflow).  Levels above 2
+// are walked one frontier node at a time; the level-2 frontier (at most 32
+// nodes) is expanded in parallel, one node per lane, its 32 children read
+// in a lane-rotated order (no bank conflicts) and selected by bit masks.
 __device__ __forceinline__ int batch_extract(const NsmInstance& I, const long long* NT,
-                                             const int* NI, const long long* T2, int* fa,
-                                             int* fb, int lane, unsigned ltm, long long thb,
-                                             long long& ct, int& ci, long long& ct2) {
+                                             const int* NI, int* fa, int* fb, int lane,
+                                             unsigned ltm, long long thb, long long& ct,
+                                             int& ci) {
     const int L = I.levels;
     int nf = 1;
     if (lane == 0) fa[0] = 0;
     __syncwarp();
     int* cur = fa;
     int* nxt = fb;
-    for (int l = L; l >= 2; l--) {
+    for (int l = L; l >= 3; l--) {
         const int off = I.level_off[l - 1], sz = I.level_size[l - 1];
         int nn = 0;
         for (int f = 0; f < nf; f++) {
@@ -70,80 +74,168 @@ __device__ __forceinline__ int batch_extract(const NsmInstance& I, const long lo
         cur = nxt;
         nxt = tmp;
     }
-    if (nf > 32) return -1;
-    if (lane < nf) {
-        const int node = cur[lane];
-        ct = NT[I.level_off[1] + node];
-        ci = NI[I.level_off[1] + node];
-        ct2 = T2[node];
+    // level 2 -> level 1
+    const int off = I.level_off[1], sz = I.level_size[1];
+    int got = 0;
+    if (nf <= 32) {
+        unsigned mask = 0u;
+        int base = 0;
+        if (lane < nf) {
+            base = cur[lane] * 32;
+            if ((off & 1) == 0 && base + 32 <= sz) {
+                const longlong2* tp = (const longlong2*)(NT + off + base);
+#pragma unroll
+                for (int q = 0; q < 16; q++) {
+                    const int qq = (q + lane) & 15;
+                    const longlong2 u = tp[qq];
+                    mask |= (unsigned)(u.x < thb) << (2 * qq);
+                    mask |= (unsigned)(u.y < thb) << (2 * qq + 1);
+                }
+            } else {
+                for (int q = 0; q < 32; q++)
+                    if (base + q < sz && NT[off + base + q] < thb) mask |= 1u << q;
+            }
+        }
+        // exclusive prefix of the per-lane counts
+        const int n = __popc(mask);
+        int inc = n;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(SP_FULL, inc, o);
+            if (lane >= o) inc += u;
+        }
+        got = __shfl_sync(SP_FULL, inc, 31);
+        __syncwarp();
+        if (got <= 32) {
+            int pos = inc - n;
+            for (unsigned m = mask; m; m &= m - 1) nxt[pos++] = base + __ffs(m) - 1;
+        }
+    } else {
+        got = 33;
+    }
+    __syncwarp();
+    if (got > 32) return -1;
+    if (lane < got) {
+        const int node = nxt[lane];
+        ct = NT[off + node];
+        ci = NI[off + node];
     } else {
         ct = SP_INF_BITS;
         ci = INT_MAX;
-        ct2 = SP_INF_BITS;
     }
     __syncwarp();
-    return nf;
+    return got;
 }
 
-// ascending bitonic sort of 32 lanes by (t, i), carrying t2
-__device__ __forceinline__ void bitonic32(int lane, long long& ct, int& ci, long long& ct2) {
+// ascending bitonic sort of 32 lanes by (t, i)
+__device__ __forceinline__ void bitonic32(int lane, long long& ct, int& ci) {
 #pragma unroll
     for (int k = 2; k <= 32; k <<= 1) {
 #pragma unroll
         for (int jj = k >> 1; jj > 0; jj >>= 1) {
             const long long pt = __shfl_xor_sync(SP_FULL, ct, jj);
             const int pi = __shfl_xor_sync(SP_FULL, ci, jj);
-            const long long pt2 = __shfl_xor_sync(SP_FULL, ct2, jj);
             const bool up = (lane & k) == 0;
             const bool lower = (lane & jj) == 0;
             const bool take = (lower == up) ? kless(pt, pi, ct, ci) : kless(ct, ci, pt, pi);
             if (take) {
                 ct = pt;
                 ci = pi;
-                ct2 = pt2;
             }
         }
     }
 }
 
 // One lane: minimum and second minimum of leaf group g (32 contiguous leaf
-// times) -> level-1 node g and its second-smallest time.
-__device__ __forceinline__ void lane_rescan(const NsmInstance& I, const long long* LF,
-                                            long long* NT, int* NI, long long* T2, int g) {
-    const longlong2* p = (const longlong2*)(LF + (size_t)g * 32);
-    long long t1 = SP_INF_BITS, t2 = SP_INF_BITS;
-    int i1 = INT_MAX;
+// times) -> level-1 node g and its second-smallest time.  Two halves of 16
+// leaves, each reduced by a pairwise tree (the merges of one level are
+// independent, so their latencies overlap), then merged.
+struct MinPair {
+    long long m, s;   // smallest time (with its index) and the second-smallest time
+    int i;
+};
+
+__device__ __forceinline__ MinPair merge_pair(const MinPair& a, const MinPair& b) {
+    const bool x = kless(a.m, a.i, b.m, b.i);
+    MinPair r;
+    r.m = x ? a.m : b.m;
+    r.i = x ? a.i : b.i;
+    const long long hi = x ? b.m : a.m;
+    const long long s1 = x ? a.s : b.s;
+    r.s = hi < s1 ? hi : s1;
+    return r;
+}
+
+__device__ __forceinline__ MinPair rescan_half(const longlong2* p, int base) {
+    MinPair v[8];
 #pragma unroll
-    for (int q = 0; q < 16; q++) {
+    for (int q = 0; q < 8; q++) {
         const longlong2 u = p[q];
-        const int ia = g * 32 + 2 * q, ib = ia + 1;
-        if (kless(u.x, ia, t1, i1)) { t2 = t1; t1 = u.x; i1 = ia; }
-        else if (u.x < t2) t2 = u.x;
-        if (kless(u.y, ib, t1, i1)) { t2 = t1; t1 = u.y; i1 = ib; }
-        else if (u.y < t2) t2 = u.y;
+        const bool a = u.x <= u.y;               // ties: the lower index wins
+        v[q].m = a ? u.x : u.y;
+        v[q].i = a ? base + 2 * q : base + 2 * q + 1;
+        v[q].s = a ? u.y : u.x;
     }
-    NT[I.level_off[1] + g] = t1;
-    NI[I.level_off[1] + g] = i1;
-    T2[g] = t2;
+#pragma unroll
+    for (int w = 4; w >= 1; w >>= 1)
+#pragma unroll
+        for (int q = 0; q < w; q++) v[q] = merge_pair(v[q], v[q + w]);
+    return v[0];
+}
+
+// groups ga and gb (gb < 0: none), both groups' loads in flight together
+__device__ __forceinline__ void lane_rescan2(const NsmInstance& I, const long long* LF,
+                                             long long* NT, int* NI, long long* T2, int ga,
+                                             int gb) {
+    const int gq = gb >= 0 ? gb : ga;
+    const longlong2* pa = (const longlong2*)(LF + (size_t)ga * 32);
+    const longlong2* pb = (const longlong2*)(LF + (size_t)gq * 32);
+    const MinPair a0 = rescan_half(pa, ga * 32), b0 = rescan_half(pb, gq * 32);
+    const MinPair a1 = rescan_half(pa + 8, ga * 32 + 16), b1 = rescan_half(pb + 8, gq * 32 + 16);
+    const MinPair ra = merge_pair(a0, a1), rb = merge_pair(b0, b1);
+    NT[I.level_off[1] + ga] = ra.m;
+    NI[I.level_off[1] + ga] = ra.i;
+    T2[ga] = ra.s;
+    if (gb >= 0) {
+        NT[I.level_off[1] + gb] = rb.m;
+        NI[I.level_off[1] + gb] = rb.i;
+        T2[gb] = rb.s;
+    }
 }
 
 // One lane: node p of level l (>= 2) from its 32 children, read in an order
-// rotated by p so that lanes working on different nodes hit different banks.
+// rotated by p so that lanes working on different nodes hit different banks;
+// the argmin is a pairwise tree over each half of the children.
 __device__ __forceinline__ void lane_node(const NsmInstance& I, long long* NT, int* NI, int l, int p) {
     const int offc = I.level_off[l - 1], szc = I.level_size[l - 1];
-    long long t1 = SP_INF_BITS;
-    int i1 = INT_MAX;
+    long long bt = SP_INF_BITS;
+    int bi = INT_MAX;
     if ((offc & 1) == 0 && p * 32 + 32 <= szc) {
         // full node, 16-byte aligned children: two per load
         const longlong2* tp = (const longlong2*)(NT + offc + p * 32);
         const int2* ip = (const int2*)(NI + offc + p * 32);
-#pragma unroll 4
-        for (int q = 0; q < 16; q++) {
-            const int qq = (q + p) & 15;
-            const longlong2 t = tp[qq];
-            const int2 i = ip[qq];
-            if (kless(t.x, i.x, t1, i1)) { t1 = t.x; i1 = i.x; }
-            if (kless(t.y, i.y, t1, i1)) { t1 = t.y; i1 = i.y; }
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            long long t[8];
+            int id[8];
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const int qq = (h * 8 + q + p) & 15;
+                const longlong2 a = tp[qq];
+                const int2 b = ip[qq];
+                const bool x = kless(a.x, b.x, a.y, b.y);
+                t[q] = x ? a.x : a.y;
+                id[q] = x ? b.x : b.y;
+            }
+#pragma unroll
+            for (int w = 4; w >= 1; w >>= 1)
+#pragma unroll
+                for (int q = 0; q < w; q++) {
+                    const bool x = kless(t[q], id[q], t[q + w], id[q + w]);
+                    t[q] = x ? t[q] : t[q + w];
+                    id[q] = x ? id[q] : id[q + w];
+                }
+            if (kless(t[0], id[0], bt, bi)) { bt = t[0]; bi = id[0]; }
         }
     } else {
         for (int q = 0; q < 32; q++) {
@@ -151,16 +243,16 @@ __device__ __forceinline__ void lane_node(const NsmInstance& I, long long* NT, i
             if (c < szc) {
                 const long long t = NT[offc + c];
                 const int i = NI[offc + c];
-                if (kless(t, i, t1, i1)) { t1 = t; i1 = i; }
+                if (kless(t, i, bt, bi)) { bt = t; bi = i; }
             }
         }
     }
-    NT[I.level_off[l] + p] = t1;
-    NI[I.level_off[l] + p] = i1;
+    NT[I.level_off[l] + p] = bt;
+    NI[I.level_off[l] + p] = bi;
 }
 
 template <bool REF, int MS, int MR, bool EX>
-__global__ void __launch_bounds__(32) nsm_advance_batch(NsmTraj* trajs, const NsmInstance* insts,
+__global__ void __launch_bounds__(32, 1) nsm_advance_batch(NsmTraj* trajs, const NsmInstance* insts,
                                                         int ntraj, int step_end, double dt,
                                                         long long budget, long long max_ns,
                                                         int* work, const int* tlist) {
@@ -197,6 +289,9 @@ __global__ void __launch_bounds__(32) nsm_advance_batch(NsmTraj* trajs, const Ns
         int* NI = (int*)(T2 + N1);
         int* fa = (int*)(NI + NN);
         int* fb = fa + kFront;
+        int* flg = fb + kFront;     // repair flags of levels >= 2, all zero between batches
+        const int flg_base = I.level_off[2];
+        for (int e = lane; e < NN - I.level_size[1]; e += 32) flg[e] = 0;
         for (int e = lane; e < NN; e += 32) { NT[e] = T.node_t[e]; NI[e] = T.node_i[e]; }
         for (int e = lane; e < N1; e += 32) T2[e] = T.node_t2[e];
         __syncwarp();
@@ -245,16 +340,17 @@ __global__ void __launch_bounds__(32) nsm_advance_batch(NsmTraj* trajs, const Ns
                     long long thb = __double_as_longlong(th);
                     if (thb > t_end_bits + 1) thb = t_end_bits + 1;   // no event past t_end
                     if (thb <= rt) thb = rt + 1;
-                    count = batch_extract(I, NT, NI, T2, fa, fb, lane, ltm, thb, ct, ci, ct2);
+                    count = batch_extract(I, NT, NI, fa, fb, lane, ltm, thb, ct, ci);
                     if (count < 0) {
                         if (bsc > 1.0f) { bsc *= 0.5f; continue; }
                         count = 1;        // degenerate: the minimum alone
                         ct = lane == 0 ? rt : SP_INF_BITS;
                         ci = lane == 0 ? ri : INT_MAX;
-                        ct2 = lane == 0 ? T2[ri >> 5] : SP_INF_BITS;
                     } else {
-                        bitonic32(lane, ct, ci, ct2);
+                        bitonic32(lane, ct, ci);
                     }
+                    // the second-smallest time of each candidate's voxel group
+                    ct2 = lane < count ? T2[ci >> 5] : SP_INF_BITS;
                     if (count >= 28) bsc = bsc * 0.8f;
                     else if (count < 16 && bsc < 64.0f) bsc = bsc * 1.25f;
                 }
@@ -346,24 +442,38 @@ __global__ void __launch_bounds__(32) nsm_advance_batch(NsmTraj* trajs, const Ns
                             const int2* crow = I.cdfj + ((size_t)v * S + sp) * K;
                             int k = -1, lastk = -1, jk = -1, jlast = -1;
                             float prev = 0.0f;
-                            if (K <= 32) {
-                                // the whole row in one round (32 entries, 256 bytes)
+                            if (K <= 32 && (K & 1) == 0) {
+                                // the whole row in one round (32 entries, 256 bytes,
+                                // two per 16-byte load), then the scan of :359-367 as
+                                // bit masks: entry q is a candidate when its running
+                                // sum rises (positive weight) and a hit when it also
+                                // exceeds target2; the first hit, else the last
+                                // candidate, is the destination
                                 int2 c[32];
+                                const int4* crow4 = (const int4*)crow;
+#pragma unroll
+                                for (int q = 0; q < 16; q++) {
+                                    const int4 u = 2 * q < cnt ? crow4[q] : make_int4(0, -1, 0, -1);
+                                    c[2 * q] = make_int2(u.x, u.y);
+                                    c[2 * q + 1] = make_int2(u.z, u.w);
+                                }
+                                unsigned posm = 0u, hitm = 0u;
+#pragma unroll
+                                for (int q = 0; q < 32; q++) {
+                                    const float cq = __int_as_float(c[q].x);
+                                    const float cp = q == 0 ? 0.0f : __int_as_float(c[q - 1].x);
+                                    const bool pos = q < cnt && cq > cp;
+                                    posm |= (unsigned)pos << q;
+                                    hitm |= (unsigned)(pos && cq > target2) << q;
+                                }
+                                if (hitm) k = __ffs(hitm) - 1;
+                                else if (posm) lastk = 31 - __clz(posm);
+                                const int ks = hitm ? k : lastk;
 #pragma unroll
                                 for (int q = 0; q < 32; q++)
-                                    c[q] = q < cnt ? crow[q] : make_int2(0, -1);
-#pragma unroll
-                                for (int q = 0; q < 32; q++) {                  // :359-367
-                                    if (k < 0 && q < cnt) {
-                                        const float cq = __int_as_float(c[q].x);
-                                        if (cq > prev) {
-                                            lastk = q;
-                                            jlast = c[q].y;
-                                            if (cq > target2) { k = q; jk = c[q].y; }
-                                        }
-                                        prev = cq;
-                                    }
-                                }
+                                    if (q == ks) jk = c[q].y;
+                                jlast = jk;
+                                (void)prev;
                             } else {
                                 for (int q = 0; q < cnt && k < 0; q++) {
                                     const int2 cc = crow[q];
@@ -466,10 +576,7 @@ __global__ void __launch_bounds__(32) nsm_advance_batch(NsmTraj* trajs, const Ns
                 // differs, its destination group (32 contiguous leaves each)
                 const int gv = v >> 5;
                 const int gw = (w >= 0 && (w >> 5) != gv) ? w >> 5 : -1;
-                if (acc) {
-                    lane_rescan(I, LF, NT, NI, T2, gv);
-                    if (gw >= 0) lane_rescan(I, LF, NT, NI, T2, gw);
-                }
+                if (acc) lane_rescan2(I, LF, NT, NI, T2, gv, gw);
                 __syncwarp();
                 // parents of changed nodes, level by level: one lane per
                 // changed node on wide levels, the whole level by warp
@@ -492,21 +599,15 @@ __global__ void __launch_bounds__(32) nsm_advance_batch(NsmTraj* trajs, const Ns
                     }
                     pa = pa >= 0 ? pa >> 5 : -1;
                     pb = pb >= 0 ? pb >> 5 : -1;
-                    // one lane per distinct parent
-                    const unsigned ma = __match_any_sync(SP_FULL, pa);
-                    const bool lead_a = pa >= 0 && (ma & ltm) == 0;
-                    const unsigned mb = __match_any_sync(SP_FULL, pb);
-                    bool lead_b = pb >= 0 && (mb & ltm) == 0;
-                    const unsigned any_a = __ballot_sync(SP_FULL, lead_a);
-                    // a b-parent that some lane already recomputes as an a-parent
-                    for (unsigned bits = any_a; bits; bits &= bits - 1) {
-                        const int q = __ffs(bits) - 1;
-                        const int pq = __shfl_sync(SP_FULL, pa, q);
-                        if (pb == pq) lead_b = false;
-                    }
+                    // one lane per distinct parent: the first to raise its flag
+                    int* fl = flg + (I.level_off[l] - flg_base);
+                    const bool lead_a = pa >= 0 && atomicExch(&fl[pa], 1) == 0;
+                    const bool lead_b = pb >= 0 && atomicExch(&fl[pb], 1) == 0;
                     if (lead_a) lane_node(I, NT, NI, l, pa);
                     if (lead_b) lane_node(I, NT, NI, l, pb);
                     __syncwarp();
+                    if (lead_a) fl[pa] = 0;
+                    if (lead_b) fl[pb] = 0;
                     if (!lead_a) pa = -1;
                     if (!lead_b) pb = -1;
                 }
