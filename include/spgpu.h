@@ -127,7 +127,9 @@ typedef struct sp_options {
                                      two kernels, launched concurrently);
                                      1 = generic sequential warp kernel;
                                      2 = speculative batches wherever supported;
-                                     3 = sequential register kernel */
+                                     3 = sequential register kernel;
+                                     4 / 5 = speculative batches with 2 / 4 warps
+                                     per trajectory */
     int32_t reserved;
     int64_t event_budget;         /* max events per trajectory per launch (0 = default) */
 } sp_options;
@@ -233,6 +235,8 @@ typedef struct sp_profile {
 #define SP_KERNEL_BATCH 3        /* nsm_advance_batch: speculative 32-event batches */
 #define SP_KERNEL_MIXED 4        /* batch kernel for domains of >= 2,048 voxels and
                                     nsm_advance_small for the rest, concurrently */
+#define SP_KERNEL_BATCH_W2 5     /* nsm_advance_batchw: 2 warps per trajectory, 64-event batches */
+#define SP_KERNEL_BATCH_W4 6     /* nsm_advance_batchw: 4 warps per trajectory, 128-event batches */
 int sp_last_profile(sp_handle* h, sp_profile* p);
 
 /*

@@ -23,6 +23,7 @@ UNITS = {
     "engine.cu": [],
     "nsm.cu": ["-fmad=false"],
     "nsm_batch.cu": ["-fmad=false"],
+    "nsm_batchw.cu": ["-fmad=false"],
     "neighbors.cu": ["-fmad=false"],
     "sdpd.cu": ["-fmad=false"],
 }

@@ -30,6 +30,11 @@ void launch_nsm_advance(bool ref, bool smem_state, int variant, int warp_smem, i
                         double dt, long long budget, long long max_ns, int* work, int num_sms,
                         const int* tlist, cudaStream_t st);
 int nsm_batch_smem(const NsmInstance& d);
+int nsm_batchw_smem(const NsmInstance& d, int W);
+void launch_nsm_batchw(bool ref, int variant, int warps, int smem_bytes, NsmTraj* trajs,
+                       const NsmInstance* insts, int ntraj, int step_end, double dt,
+                       long long budget, long long max_ns, int* work, int num_sms,
+                       const int* tlist, cudaStream_t st);
 void launch_nsm_batch(bool ref, int variant, int warp_smem, NsmTraj* trajs,
                       const NsmInstance* insts, int ntraj, int step_end, double dt,
                       long long budget, long long max_ns, int* work, int num_sms,
@@ -76,8 +81,20 @@ struct Instance {
 struct KernelGroup {
     bool batch = false, smem_state = false;
     int variant = 0, warp_smem = 0, wpb = 1;
+    int warps = 1;             // batch kernel: warps per trajectory (1, 2 or 4)
     std::vector<int> list;     // trajectories, in launch order
     int* d_list = nullptr;     // device copy, or nullptr for 0..ntraj-1
+};
+
+// Warps-per-trajectory tuner of a batch group: the first output intervals
+// run with 4, 2 and 1 warps per trajectory in turn; the width with the
+// highest events/ms is kept.  Every width gives the same events, so the
+// choice changes speed only.
+struct WarpTuner {
+    bool on = false;
+    int stage = 0;
+    double rate[3] = {0, 0, 0};
+    static constexpr int widths[3] = {4, 2, 1};
 };
 
 struct RunState {
@@ -91,6 +108,7 @@ struct RunState {
     int next_out = 0, result = SP_OK;
     KernelGroup grp[2];
     int ngroups = 1;
+    WarpTuner tune;
     long long ctot = 0, mtot = 0;
     int32_t* d_counts = nullptr;
     long long *d_mom = nullptr, *d_coff = nullptr, *d_moff = nullptr;
@@ -482,6 +500,31 @@ static int net_variant(sp_handle* h, const std::vector<int>& js, const std::vect
     return 0;
 }
 
+// batch width of group G (falls back to fewer warps when shared memory is short)
+static void set_warps(sp_handle* h, const RunState& R, KernelGroup& G, int W) {
+    for (; W > 1; W >>= 1) {
+        int wb = 0;
+        for (int j : G.list) wb = std::max(wb, nsm_batchw_smem(h->inst[R.inst[j]].desc, W));
+        if (wb <= 200 * 1024) {
+            G.warps = W;
+            G.warp_smem = wb;
+            return;
+        }
+    }
+    int wb = 0;
+    for (int j : G.list) wb = std::max(wb, nsm_batch_smem(h->inst[R.inst[j]].desc));
+    G.warps = 1;
+    G.warp_smem = wb;
+}
+
+static int kernel_kind(const RunState& R) {
+    return R.ngroups == 2 ? SP_KERNEL_MIXED
+         : R.grp[0].batch && R.grp[0].warps == 2 ? SP_KERNEL_BATCH_W2
+         : R.grp[0].batch && R.grp[0].warps == 4 ? SP_KERNEL_BATCH_W4
+         : R.grp[0].batch ? SP_KERNEL_BATCH
+         : R.grp[0].variant != 0 ? SP_KERNEL_SEQUENTIAL : SP_KERNEL_GENERIC;
+}
+
 // kernel and launch shape for the trajectories `js`
 static int choose_group(sp_handle* h, const RunState& R, const std::vector<int>& js,
                         bool want_batch, KernelGroup& G) {
@@ -504,6 +547,14 @@ static int choose_group(sp_handle* h, const RunState& R, const std::vector<int>&
     // speculative batches need a register-resident network
     G.batch = want_batch && G.variant != 0 && batch_bytes <= 200 * 1024;
     if (G.batch) G.warp_smem = batch_bytes;
+    // warps per trajectory: forced by nsm_variant 4 (2 warps) or 5 (4 warps);
+    // by default 4 while the trajectories fit about three CTAs per SM, 2 up to
+    // six, else 1 (the tuner refines this on long runs)
+    const int n = (int)js.size();
+    const int W = h->opt.nsm_variant == 4 ? 2 : h->opt.nsm_variant == 5 ? 4
+                : h->opt.nsm_variant != 0 ? 1
+                : n <= 3 * h->num_sms ? 4 : n <= 6 * h->num_sms ? 2 : 1;
+    if (G.batch) set_warps(h, R, G, W);
     return SP_OK;
 }
 
@@ -521,7 +572,10 @@ static void launch_groups(sp_handle* h, bool ref, int step_end, long long budget
         }
         const int n = R.ngroups == 1 ? ntraj : (int)G.list.size();
         const int* tl = R.ngroups == 1 ? nullptr : G.d_list;
-        if (G.batch)
+        if (G.batch && G.warps > 1)
+            launch_nsm_batchw(ref, G.variant, G.warps, G.warp_smem, h->d_trajs, h->d_insts, n,
+                              step_end, h->dt, budget, max_ns, h->d_work + g, h->num_sms, tl, s);
+        else if (G.batch)
             launch_nsm_batch(ref, G.variant, G.warp_smem, h->d_trajs, h->d_insts, n, step_end,
                              h->dt, budget, max_ns, h->d_work + g, h->num_sms, tl, s);
         else
@@ -640,13 +694,20 @@ int sp_run_start(sp_handle* h, const sp_run_args* a, sp_outputs* out) {
         if (rc == SP_OK) rc = choose_group(h, R, small, false, R.grp[1]);
     } else {
         R.ngroups = 1;
-        const bool want_batch = h->opt.nsm_variant == 2 || (h->opt.nsm_variant == 0 && !big.empty());
+        const bool want_batch = h->opt.nsm_variant == 2 || h->opt.nsm_variant >= 4 ||
+                                (h->opt.nsm_variant == 0 && !big.empty());
         rc = choose_group(h, R, all, want_batch, R.grp[0]);
     }
     if (rc) { run_release(h); return rc; }
-    h->last_kernel = R.ngroups == 2 ? SP_KERNEL_MIXED
-                   : R.grp[0].batch ? SP_KERNEL_BATCH
-                   : R.grp[0].variant != 0 ? SP_KERNEL_SEQUENTIAL : SP_KERNEL_GENERIC;
+    // the tuner needs a few intervals to spare: one batch group, static
+    // domains, default policy, at least six output intervals
+    R.tune = WarpTuner{};
+    if (h->opt.nsm_variant == 0 && R.ngroups == 1 && R.grp[0].batch && !R.coupled &&
+        (int)h->output_steps.size() >= 7) {
+        R.tune.on = true;
+        set_warps(h, R, R.grp[0], WarpTuner::widths[0]);
+    }
+    h->last_kernel = kernel_kind(R);
     R.max_leaf = max_leaf;
     R.max_levels = max_levels;
     launch_nsm_init(h->d_trajs, h->d_insts, ntraj, max_leaf, max_levels, d_u0, !R.coupled, st);
@@ -801,6 +862,12 @@ int sp_run_continue(sp_handle* h, int32_t num_outputs) {
             done++;
         } else if (target > 0) {
             if (done >= num_outputs) break;
+            long long ev0 = 0;
+            double int_ms = 0;
+            if (R.tune.on) {
+                set_warps(h, R, R.grp[0], WarpTuner::widths[R.tune.stage]);
+                for (int j = 0; j < ntraj; j++) ev0 += h->h_trajs[j].nrx + h->h_trajs[j].ndf;
+            }
             for (;;) {
                 cudaEventRecord(h->ea, st);
                 launch_groups(h, ref, target, budget, max_ns);
@@ -815,6 +882,7 @@ int sp_run_continue(sp_handle* h, int32_t num_outputs) {
                 float ms = 0;
                 cudaEventElapsedTime(&ms, h->ea, h->eb);
                 h->adv_ms += ms;
+                int_ms += ms;
                 bool again = false;
                 for (int j = 0; j < ntraj; j++) {
                     NsmTraj& T = h->h_trajs[j];
@@ -834,6 +902,19 @@ int sp_run_continue(sp_handle* h, int32_t num_outputs) {
                 // resume: statuses were reset on the host copy
                 cudaMemcpyAsync(h->d_trajs, h->h_trajs.data(), sizeof(NsmTraj) * ntraj,
                                 cudaMemcpyHostToDevice, st);
+            }
+            if (R.tune.on && R.result == SP_OK) {
+                long long ev1 = 0;
+                for (int j = 0; j < ntraj; j++) ev1 += h->h_trajs[j].nrx + h->h_trajs[j].ndf;
+                R.tune.rate[R.tune.stage] = int_ms > 0 ? (double)(ev1 - ev0) / int_ms : 0.0;
+                if (++R.tune.stage == 3) {
+                    int best = 0;
+                    for (int k = 1; k < 3; k++)
+                        if (R.tune.rate[k] > R.tune.rate[best]) best = k;
+                    set_warps(h, R, R.grp[0], WarpTuner::widths[best]);
+                    R.tune.on = false;
+                    h->last_kernel = kernel_kind(R);
+                }
             }
             done++;
         }
@@ -924,6 +1005,7 @@ int sp_run(sp_handle* h, const sp_run_args* a, sp_outputs* out) {
     const double adv = h->adv_ms;
     h->last_ms += ms0;
     h->last_launches += l0;
+    if (!h->run.active) return rc2;   // released on a CUDA error; keep its message
     const int rc3 = sp_run_finish(h);
     h->adv_ms = adv;
     return rc2 != SP_OK ? rc2 : rc3;

@@ -1,0 +1,489 @@
+// nsm_batchw.cu — speculative batched NSM event loop with W warps (one CTA)
+// per trajectory: batches of up to 32*W candidates.
+//
+// The events, their order and their random numbers are those of the
+// sequential loop (nsm.cu) and of the one-warp batch kernel (nsm_batch.cu);
+// only the work of a batch is spread over more warps, so that one
+// trajectory keeps several schedulers of an SM busy:
+//
+//  1. candidates: warp 0 walks the shared-memory tree down to level 2; the
+//     level-2 frontier (up to 32*W nodes) is expanded by all warps, one node
+//     per lane; the level-1 nodes below the horizon are gathered, one per
+//     thread, and sorted by (time, voxel) with a CTA-wide bitonic network
+//     (shuffles within a warp, shared memory across warps).
+//  2. thread g executes candidate g as event number n+g.
+//  3. the accepted prefix: time bounds by prefix minima (warp shuffles, then
+//     the minima of earlier warps); voxel conflicts through a hashed table of
+//     the smallest candidate index touching each voxel (a collision only
+//     rejects more, which is safe: a rejected event is redone later).
+//  4. accepted events are written, their voxel groups rescanned, and the
+//     tree repaired level by level, one thread per changed node.
+//
+// Scalars that steer the loop (clock, counters, running propensity total)
+// are kept in every thread and updated from the same shared values in the
+// same order, so all warps take the same branches.  Compiled with
+// -fmad=false.
+#include "nsm_batch.cuh"
+
+namespace spg {
+
+constexpr int kHash = 2048;   // conflict table slots (power of two, > 2 * 32 * W)
+
+__device__ __forceinline__ int hslot(int v) { return (int)(((unsigned)v * 2654435761u) >> 21); }
+
+// conflict table: open addressing with linear probing, key = voxel, value =
+// the smallest candidate index touching it.  At most 2 * 32 * W keys per
+// batch, so a probe always ends at the key or at an empty slot.
+__device__ __forceinline__ void ctab_insert(int* key, int* val, int v, int g) {
+    int h = hslot(v);
+    for (int n = 0; n < kHash; n++) {
+        const int old = atomicCAS(&key[h], -1, v);
+        if (old == -1 || old == v) {
+            atomicMin(&val[h], g);
+            return;
+        }
+        h = (h + 1) & (kHash - 1);
+    }
+}
+
+__device__ __forceinline__ int ctab_find(const int* key, int v) {
+    int h = hslot(v);
+    for (int n = 0; n < kHash; n++) {
+        if (key[h] == v) return h;
+        h = (h + 1) & (kHash - 1);
+    }
+    return -1;
+}
+
+static size_t batchw_smem_bytes(const NsmInstance& d, int W) {
+    const size_t NN = d.num_nodes, N1 = d.level_size[1];
+    size_t b = NN * 8 + N1 * 8 + NN * 4;      // tree times, second minima, indices
+    b += 2 * (size_t)(64 * W) * 4;             // frontiers
+    b += (NN - N1) * 4;                        // repair flags, levels >= 2
+    b += (size_t)kHash * 8;                    // conflict table: keys, values
+    b += (size_t)(32 * W) * 4;                 // candidate list
+    b = (b + 15) / 16 * 16;
+    b += 2 * (size_t)(32 * W) * 12;            // sort exchange, double-buffered
+    return (b + 15) / 16 * 16;
+}
+
+int nsm_batchw_smem(const NsmInstance& d, int W) { return (int)batchw_smem_bytes(d, W); }
+
+template <bool REF, int MS, int MR, bool EX, int W>
+__global__ void __launch_bounds__(32 * W, 1)
+    nsm_advance_batchw(NsmTraj* trajs, const NsmInstance* insts, int ntraj, int step_end,
+                       double dt, long long budget, long long max_ns, int* work,
+                       const int* tlist) {
+    constexpr int NC = 32 * W;    // candidates per batch at most
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int s_jt, s_nf, s_tflag;
+    __shared__ int s_wcnt[W], s_wfi[W], s_werr[W], s_werrc[W], s_werrv[W], s_wnrx[W], s_wndf[W];
+    __shared__ long long s_wmin[W], s_tl;
+    __shared__ double s_wdA[W];
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const unsigned ltm = (1u << lane) - 1u;
+    for (;;) {
+        if (tid == 0) s_jt = atomicAdd(work, 1);
+        __syncthreads();
+        const int jt = s_jt;
+        __syncthreads();
+        if (jt >= ntraj) return;
+        NsmTraj& T = trajs[tlist ? tlist[jt] : jt];
+        if (T.status != SP_TRAJ_OK || T.step >= step_end) continue;
+        const NsmInstance& I = insts[T.inst];
+        const int NN = I.num_nodes, N1 = I.level_size[1], L = I.levels;
+        SmallNet<MS, MR> Q;
+        Q.S = I.S;
+        Q.R = I.R;
+#pragma unroll
+        for (int r = 0; r < MR; r++) {
+            const bool on = EX || r < I.R;
+            Q.kind[r] = on ? I.kind[r] : 0;
+            Q.ra[r] = on ? I.reac[2 * r] : 0;
+            Q.rb[r] = on ? I.reac[2 * r + 1] : 0;
+            Q.rate[r] = on ? I.rate[r] : 0.0f;
+            unsigned long long m = 0;
+            if (on)
+                for (int t = 0; t <= I.T && t < 64; t++)
+                    if (!I.allowed || I.allowed[r * (I.T + 1) + t]) m |= 1ull << t;
+            Q.allowed[r] = m;
+        }
+        // shared-memory layout (batchw_smem_bytes)
+        long long* NT = (long long*)smem;
+        long long* T2 = NT + NN;
+        int* NI = (int*)(T2 + N1);
+        int* fa = NI + NN;
+        int* fb = fa + 64 * W;
+        int* flg = fb + 64 * W;
+        int* hkey = flg + (NN - N1);
+        int* hval = hkey + kHash;
+        int* clist = hval + kHash;
+        unsigned char* xb = (unsigned char*)(((uintptr_t)(clist + NC) + 15) & ~(uintptr_t)15);
+        long long* xt = (long long*)xb;            // [2][NC]
+        int* xi = (int*)(xt + 2 * NC);             // [2][NC]
+        const int flg_base = I.level_off[2];
+        for (int e = tid; e < NN - N1; e += NC) flg[e] = 0;
+        for (int e = tid; e < kHash; e += NC) { hkey[e] = -1; hval[e] = INT_MAX; }
+        for (int e = tid; e < NN; e += NC) { NT[e] = T.node_t[e]; NI[e] = T.node_i[e]; }
+        for (int e = tid; e < N1; e += NC) T2[e] = T.node_t2[e];
+        __syncthreads();
+        long long* LF = T.leaf;
+        int32_t* X = T.x;
+        uint64_t evn = T.evn;
+        long long nrx = T.nrx, ndf = T.ndf;
+        int step = T.step;
+        int status = SP_TRAJ_OK, errv = -1;
+        double tlast = T.t_last;
+        double A = T.a_tot;
+        float bsc = T.bscale;
+        long long nev = 0;
+        int nbatch = 0;
+        long long stat_b = 0, stat_c = 0;
+        unsigned long long t_start;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_start));
+        long long rt = NT[I.level_off[L]];
+        int ri = NI[I.level_off[L]];
+        int xbuf = 0;
+        while (step < step_end && status == SP_TRAJ_OK) {
+            const double t_end = dt * (double)step + dt;   // simulate_rdme.cpp:67, 215
+            const long long t_end_bits = __double_as_longlong(t_end);
+            bool step_done = false;
+            for (;;) {
+                if (rt == SP_INF_BITS) { step_done = true; break; }
+                const bool over = rt > t_end_bits;
+                if (over && !REF) { step_done = true; break; }
+                if (nev >= budget) { status = SP_TRAJ_BUDGET_EXHAUSTED; break; }
+                if ((++nbatch & 15) == 0) {
+                    // one thread reads the clock; every thread takes its answer
+                    if (tid == 0) {
+                        unsigned long long now;
+                        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+                        s_tflag = (long long)(now - t_start) > max_ns;
+                    }
+                    __syncthreads();
+                    const int tf = s_tflag;
+                    __syncthreads();
+                    if (tf) { status = SP_TRAJ_BUDGET_EXHAUSTED; break; }
+                }
+                // ---- 1. candidates -------------------------------------------
+                long long ct = SP_INF_BITS, ct2 = SP_INF_BITS;
+                int ci = INT_MAX, count = 1;
+                if (over) {   // the reference's one event past the step end, alone
+                    if (tid == 0) { ct = rt; ci = ri; ct2 = T2[ri >> 5]; }
+                } else {
+                    float delta = A > 0.0 ? bsc / (float)A : 3.0e38f;
+                    if (!(delta > 0.0f)) delta = 3.0e38f;
+                    const double th = __longlong_as_double(rt) + (double)delta;
+                    long long thb = __double_as_longlong(th);
+                    if (thb > t_end_bits + 1) thb = t_end_bits + 1;   // no event past t_end
+                    if (thb <= rt) thb = rt + 1;
+                    // levels L..3 by warp 0: frontier of level-2 nodes in fa
+                    if (wid == 0) {
+                        int nf = 1;
+                        if (lane == 0) fa[0] = 0;
+                        __syncwarp();
+                        int* cur = fa;
+                        int* nxt = fb;
+                        for (int l = L; l >= 3 && nf >= 0; l--) {
+                            const int off = I.level_off[l - 1], sz = I.level_size[l - 1];
+                            int nn = 0;
+                            for (int f = 0; f < nf; f++) {
+                                const int c = cur[f] * 32 + lane;
+                                const long long t = c < sz ? NT[off + c] : SP_INF_BITS;
+                                const bool q = t < thb;
+                                const unsigned bal = __ballot_sync(SP_FULL, q);
+                                const int pos = nn + __popc(bal & ltm);
+                                if (q && pos < 64 * W) nxt[pos] = c;
+                                nn += __popc(bal);
+                            }
+                            __syncwarp();
+                            nf = nn > 64 * W ? -1 : nn;
+                            int* tmp = cur;
+                            cur = nxt;
+                            nxt = tmp;
+                        }
+                        if (nf > 0 && cur != fa)
+                            for (int e = lane; e < nf; e += 32) fa[e] = cur[e];
+                        if (lane == 0) s_nf = nf > NC ? -1 : nf;
+                    }
+                    __syncthreads();
+                    const int nf = s_nf;
+                    // level 2 -> level 1: frontier node `tid` per thread
+                    const int off1 = I.level_off[1], sz1 = I.level_size[1];
+                    unsigned mask = 0u;
+                    int base = 0;
+                    if (nf > 0 && tid < nf) {
+                        base = fa[tid] * 32;
+                        if ((off1 & 1) == 0 && base + 32 <= sz1) {
+                            const longlong2* tp = (const longlong2*)(NT + off1 + base);
+#pragma unroll
+                            for (int q = 0; q < 16; q++) {
+                                const int qq = (q + lane) & 15;
+                                const longlong2 u = tp[qq];
+                                mask |= (unsigned)(u.x < thb) << (2 * qq);
+                                mask |= (unsigned)(u.y < thb) << (2 * qq + 1);
+                            }
+                        } else {
+                            for (int q = 0; q < 32; q++)
+                                if (base + q < sz1 && NT[off1 + base + q] < thb) mask |= 1u << q;
+                        }
+                    }
+                    const int n = __popc(mask);
+                    int inc = n;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int u = __shfl_up_sync(SP_FULL, inc, o);
+                        if (lane >= o) inc += u;
+                    }
+                    if (lane == 31) s_wcnt[wid] = inc;
+                    __syncthreads();
+                    int wbase = 0, got = 0;
+#pragma unroll
+                    for (int u = 0; u < W; u++) {
+                        if (u < wid) wbase += s_wcnt[u];
+                        got += s_wcnt[u];
+                    }
+                    if (nf < 0) got = NC + 1;
+                    if (got <= NC) {
+                        int pos = wbase + inc - n;
+                        for (unsigned m = mask; m; m &= m - 1) clist[pos++] = base + __ffs(m) - 1;
+                    }
+                    __syncthreads();
+                    if (got > NC) {
+                        if (bsc > 1.0f) { bsc *= 0.5f; continue; }
+                        count = 1;        // degenerate: the minimum alone
+                        ct = tid == 0 ? rt : SP_INF_BITS;
+                        ci = tid == 0 ? ri : INT_MAX;
+                    } else {
+                        count = got;
+                        if (tid < got) {
+                            const int node = clist[tid];
+                            ct = NT[off1 + node];
+                            ci = NI[off1 + node];
+                        }
+                        // bitonic sort of NC keys (t, i), ascending
+#pragma unroll
+                        for (int k = 2; k <= NC; k <<= 1) {
+#pragma unroll
+                            for (int jj = k >> 1; jj > 0; jj >>= 1) {
+                                long long pt;
+                                int pi;
+                                if (jj >= 32) {
+                                    xt[xbuf * NC + tid] = ct;
+                                    xi[xbuf * NC + tid] = ci;
+                                    __syncthreads();
+                                    pt = xt[xbuf * NC + (tid ^ jj)];
+                                    pi = xi[xbuf * NC + (tid ^ jj)];
+                                    xbuf ^= 1;
+                                } else {
+                                    pt = __shfl_xor_sync(SP_FULL, ct, jj);
+                                    pi = __shfl_xor_sync(SP_FULL, ci, jj);
+                                }
+                                const bool up = (tid & k) == 0;
+                                const bool lower = (tid & jj) == 0;
+                                const bool take = (lower == up) ? kless(pt, pi, ct, ci)
+                                                                : kless(ct, ci, pt, pi);
+                                if (take) {
+                                    ct = pt;
+                                    ci = pi;
+                                }
+                            }
+                        }
+                    }
+                    ct2 = tid < count ? T2[ci >> 5] : SP_INF_BITS;
+                    if (count >= 28 * W) bsc = bsc * 0.8f;
+                    else if (count < 16 * W && bsc < 64.0f * W) bsc = bsc * 1.25f;
+                }
+                stat_b++;
+                stat_c += count;
+                // ---- 2. speculative execution, one candidate per thread -------
+                const bool act = tid < count;
+                Cand<MS> Cd;
+                batch_execute<REF, MS, MR, EX>(I, Q, X, act, ci, ct, evn + (uint64_t)tid, T.key0,
+                                               T.key1, Cd);
+                const int v = Cd.v, w = Cd.w, sp = Cd.sp, err = Cd.err;
+                // ---- 3. the accepted prefix ------------------------------------
+                long long bound = act ? ct2 : SP_INF_BITS;
+                if (Cd.tv < bound) bound = Cd.tv;
+                if (Cd.tw < bound) bound = Cd.tw;
+                long long pm = bound;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const long long u = __shfl_up_sync(SP_FULL, pm, o);
+                    if (lane >= o && u < pm) pm = u;
+                }
+                long long ex = __shfl_up_sync(SP_FULL, pm, 1);
+                if (lane == 0) ex = SP_INF_BITS;
+                if (lane == 31) s_wmin[wid] = pm;
+                if (act) {
+                    ctab_insert(hkey, hval, v, tid);
+                    if (w >= 0 && w != v) ctab_insert(hkey, hval, w, tid);
+                }
+                __syncthreads();
+#pragma unroll
+                for (int u = 0; u < W; u++)
+                    if (u < wid && s_wmin[u] < ex) ex = s_wmin[u];
+                // an earlier candidate touching v or w (the same rule as the
+                // one-warp kernel: two candidates never share a source voxel)
+                const int hv = act ? ctab_find(hkey, v) : -1;
+                const int hw = act && w >= 0 ? ctab_find(hkey, w) : -1;
+                const bool conf = act && ((hv >= 0 && hval[hv] < tid) || (hw >= 0 && hval[hw] < tid));
+                const bool valid = act && ct < ex && !conf && (nev + tid) < budget;
+                const unsigned vb = __ballot_sync(SP_FULL, valid);
+                const unsigned ebits = __ballot_sync(SP_FULL, act && err != 0);
+                if (lane == 0) {
+                    s_wfi[wid] = vb == SP_FULL ? 32 : __ffs(~vb) - 1;
+                    s_werr[wid] = ebits ? __ffs(ebits) - 1 : 32;
+                }
+                if (ebits && lane == __ffs(ebits) - 1) {
+                    s_werrc[wid] = err;
+                    s_werrv[wid] = v;
+                }
+                __syncthreads();
+                int m = NC;
+#pragma unroll
+                for (int u = W - 1; u >= 0; u--)
+                    if (s_wfi[u] < 32) m = 32 * u + s_wfi[u];
+                int me = NC, mu = -1;
+#pragma unroll
+                for (int u = W - 1; u >= 0; u--)
+                    if (s_werr[u] < 32) { me = 32 * u + s_werr[u]; mu = u; }
+                if (me < m) {
+                    status = s_werrc[mu];
+                    errv = s_werrv[mu];
+                    m = me;
+                }
+                if (hv >= 0) { hkey[hv] = -1; hval[hv] = INT_MAX; }   // read by all: clear
+                if (hw >= 0) { hkey[hw] = -1; hval[hw] = INT_MAX; }
+                // ---- 4. commit --------------------------------------------------
+                const bool acc = tid < m;
+                if (acc) {
+#pragma unroll
+                    for (int s = 0; s < MS; s++)
+                        if (EX || s < Q.S) X[(size_t)v * Q.S + s] = Cd.xv[s];
+                    LF[v] = Cd.tv;
+                    if (w >= 0) {
+#pragma unroll
+                        for (int s = 0; s < MS; s++)
+                            if (s == sp) X[(size_t)w * Q.S + s] = Cd.xw[s];
+                        LF[w] = Cd.tw;
+                    }
+                }
+                const int wr = __popc(__ballot_sync(SP_FULL, acc && Cd.rxn));
+                const int wd = __popc(__ballot_sync(SP_FULL, acc && !Cd.rxn));
+                double dsum = acc ? (double)Cd.dA : 0.0;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) dsum += __shfl_xor_sync(SP_FULL, dsum, o);
+                if (lane == 0) {
+                    s_wnrx[wid] = wr;
+                    s_wndf[wid] = wd;
+                    s_wdA[wid] = dsum;
+                }
+                if (m > 0 && tid == m - 1) s_tl = ct;
+                // ---- 5. rescan and tree repair ------------------------------------
+                const int gv = v >> 5;
+                const int gw = (w >= 0 && (w >> 5) != gv) ? w >> 5 : -1;
+                if (acc) lane_rescan2(I, LF, NT, NI, T2, gv, gw);
+                __syncthreads();
+#pragma unroll
+                for (int u = 0; u < W; u++) {
+                    nrx += s_wnrx[u];
+                    ndf += s_wndf[u];
+                    A += s_wdA[u];
+                }
+                evn += (uint64_t)m;
+                nev += m;
+                if (m > 0) tlast = __longlong_as_double(s_tl);
+                int pa = acc ? gv : -1, pb = acc ? gw : -1;
+                for (int l = 2; l <= L; l++) {
+                    if (I.level_size[l] <= 8) {
+                        if (wid == 0) {
+                            const int offc = I.level_off[l - 1], szc = I.level_size[l - 1];
+                            for (int p = 0; p < I.level_size[l]; p++) {
+                                const int c = p * 32 + lane;
+                                const long long t = c < szc ? NT[offc + c] : SP_INF_BITS;
+                                const int i = c < szc ? NI[offc + c] : INT_MAX;
+                                long long mt;
+                                int mi;
+                                argmin_redux(t, i, mt, mi);
+                                if (lane == 0) {
+                                    NT[I.level_off[l] + p] = mt;
+                                    NI[I.level_off[l] + p] = mi;
+                                }
+                            }
+                        }
+                        __syncthreads();
+                        continue;
+                    }
+                    pa = pa >= 0 ? pa >> 5 : -1;
+                    pb = pb >= 0 ? pb >> 5 : -1;
+                    int* fl = flg + (I.level_off[l] - flg_base);
+                    const bool lead_a = pa >= 0 && atomicExch(&fl[pa], 1) == 0;
+                    const bool lead_b = pb >= 0 && atomicExch(&fl[pb], 1) == 0;
+                    if (lead_a) lane_node(I, NT, NI, l, pa);
+                    if (lead_b) lane_node(I, NT, NI, l, pb);
+                    __syncthreads();
+                    if (lead_a) fl[pa] = 0;
+                    if (lead_b) fl[pb] = 0;
+                    if (!lead_a) pa = -1;
+                    if (!lead_b) pb = -1;
+                }
+                rt = NT[I.level_off[L]];
+                ri = NI[I.level_off[L]];
+                if (over) { step_done = true; break; }
+                if (status != SP_TRAJ_OK) break;
+            }
+            if (step_done) step++;
+            else break;
+        }
+        __syncthreads();
+        for (int e = tid; e < NN; e += NC) { T.node_t[e] = NT[e]; T.node_i[e] = NI[e]; }
+        for (int e = tid; e < N1; e += NC) T.node_t2[e] = T2[e];
+        if (tid == 0) {
+            T.evn = evn;
+            T.nrx = nrx;
+            T.ndf = ndf;
+            T.step = step;
+            T.status = status;
+            T.t_last = tlast;
+            T.a_tot = A;
+            T.bscale = bsc;
+            T.nbatch += stat_b;
+            T.ncand += stat_c;
+            if (errv >= 0) T.err_voxel = errv;
+        }
+        __syncthreads();
+    }
+}
+
+typedef void (*BatchWFn)(NsmTraj*, const NsmInstance*, int, int, double, long long, long long,
+                         int*, const int*);
+
+template <bool REF, int W>
+static BatchWFn pick_batchw(int variant) {
+    switch (variant) {
+        case 1: return nsm_advance_batchw<REF, 4, 8, false, W>;
+        case 2: return nsm_advance_batchw<REF, 8, 16, false, W>;
+        case 3: return nsm_advance_batchw<REF, 1, 2, true, W>;
+        default: return nsm_advance_batchw<REF, 3, 4, true, W>;
+    }
+}
+
+// warps: 2 or 4 per trajectory
+void launch_nsm_batchw(bool ref, int variant, int warps, int smem_bytes, NsmTraj* trajs,
+                       const NsmInstance* insts, int ntraj, int step_end, double dt,
+                       long long budget, long long max_ns, int* work, int num_sms,
+                       const int* tlist, cudaStream_t st) {
+    cudaMemsetAsync(work, 0, sizeof(int), st);
+    const int per_sm = (200 * 1024) / smem_bytes > 0 ? (200 * 1024) / smem_bytes : 1;
+    int blocks = ntraj;
+    const int cap = num_sms * (per_sm < 16 ? per_sm : 16);
+    if (blocks > cap) blocks = cap;
+    BatchWFn fn = warps == 4 ? (ref ? pick_batchw<true, 4>(variant) : pick_batchw<false, 4>(variant))
+                             : (ref ? pick_batchw<true, 2>(variant) : pick_batchw<false, 2>(variant));
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+    fn<<<blocks, 32 * warps, smem_bytes, st>>>(trajs, insts, ntraj, step_end, dt, budget, max_ns,
+                                               work, tlist);
+}
+
+}  // namespace spg

@@ -16,7 +16,8 @@ from .abi import SpOptions, SpOutputs, SpRunArgs, SpTrajStatus, ptr
 
 
 KERNEL_NAMES = {1: "nsm_advance_generic", 2: "nsm_advance_small", 3: "nsm_advance_batch",
-                4: "nsm_advance_batch+nsm_advance_small"}
+                4: "nsm_advance_batch+nsm_advance_small", 5: "nsm_advance_batchw2",
+                6: "nsm_advance_batchw4"}
 
 
 class EngineError(RuntimeError):
@@ -34,7 +35,8 @@ class Engine:
         Model instances (a list runs heterogeneous batches in one launch).
     sdpd_precision : "f32" or "f64"
     nsm_variant : 0 chosen per run, 1 generic sequential warp, 2 speculative batch
-        warp, 3 sequential register-resident warp
+        warp, 3 sequential register-resident warp, 4 / 5 speculative batches
+        with 2 / 4 warps per trajectory
     """
 
     def __init__(self, scenarios, device: int = 0, sdpd_precision: str = "f32",

@@ -100,34 +100,48 @@ def test_kernel_variants_bitexact(oracle_lib, case, variant):
         np.testing.assert_array_equal(res["events"][j], ev)
 
 
+_ORACLE_RUNS = {}
+
+
+def _oracle_run(oracle_lib, key, sc, seed, selection):
+    k = (key, seed, selection)
+    if k not in _ORACLE_RUNS:
+        _ORACLE_RUNS[k] = oracle_lib.nsm_trajectory(sc, seed, selection)
+    return _ORACLE_RUNS[k]
+
+
+@pytest.mark.parametrize("variant", [2, 4, 5])
 @pytest.mark.parametrize("selection", [abi.SP_SELECT_EXACT, abi.SP_SELECT_REFERENCE])
 @pytest.mark.parametrize("n,dims", [(16, 3), (64, 2)])
-def test_batch_kernel_bitexact_large_domain(oracle_lib, n, dims, selection):
-    """Speculative 32-event batches on 4,096-voxel domains equal the
+def test_batch_kernel_bitexact_large_domain(oracle_lib, n, dims, selection, variant):
+    """Speculative batches on 4,096-voxel domains (one warp and 32 events,
+    two warps and 64, four warps and 128 per trajectory) equal the
     sequential oracle event for event (both selection rules)."""
     t_end = 2.0 if dims == 3 else 0.2
     sc = S.config_rdme_3d(n=n, nA=3000, nB=2500, t_end=t_end, num_points=5, dt=t_end / 4,
                           dims=dims)
     seeds = np.arange(6, dtype=np.uint64) + 99173
-    with _engine(sc, nsm_variant=2) as eng:
+    with _engine(sc, nsm_variant=variant) as eng:
         res = eng.run(seeds, selection=selection)
+        kernel = eng.profile()["kernel"]
+    assert kernel == {2: "nsm_advance_batch", 4: "nsm_advance_batchw2",
+                      5: "nsm_advance_batchw4"}[variant]
     assert res["rc"] == abi.SP_OK, res.get("error")
     for j, s in enumerate(seeds):
-        out, ev, _ = oracle_lib.nsm_trajectory(sc, int(s), selection)
+        out, ev, _ = _oracle_run(oracle_lib, (n, dims), sc, int(s), selection)
         np.testing.assert_array_equal(res["events"][j], ev)
         np.testing.assert_array_equal(res["counts"][j], out)
 
 
-def test_batch_kernel_birth_death_large():
+@pytest.mark.parametrize("variant", [2, 4, 5])
+def test_batch_kernel_birth_death_large(oracle_lib, variant):
     sc = S.config_birth_death_2d(n=64, count=3000, k_birth=2000.0, D=1e-4, t_end=0.5,
                                  num_points=3, dt=0.25)
     seeds = np.arange(4, dtype=np.uint64) + 5
-
-    import oracle
-    with _engine(sc, nsm_variant=2) as eng:
+    with _engine(sc, nsm_variant=variant) as eng:
         res = eng.run(seeds)
     for j, s in enumerate(seeds):
-        out, ev, _ = oracle.nsm_trajectory(sc, int(s), 0)
+        out, ev, _ = _oracle_run(oracle_lib, "bd64", sc, int(s), 0)
         np.testing.assert_array_equal(res["events"][j], ev)
         np.testing.assert_array_equal(res["counts"][j], out)
 
@@ -321,3 +335,19 @@ def test_mixed_kernel_groups_bitexact(oracle_lib):
         out, ev, _ = oracle_lib.nsm_trajectory(scs[inst[j]], int(s), 0)
         np.testing.assert_array_equal(res["counts"][j], out, err_msg=f"trajectory {j}")
         np.testing.assert_array_equal(res["events"][j], ev)
+
+
+def test_warp_tuner_keeps_trajectories(oracle_lib):
+    """With the default policy a long run tries 4, 2 and 1 warps per
+    trajectory on its first intervals and keeps the fastest; the events are
+    those of the sequential oracle whichever width runs."""
+    sc = S.config_rdme_3d(n=16, nA=3000, nB=2500, t_end=1.0, num_points=11, dt=0.1)
+    seeds = np.arange(5, dtype=np.uint64) + 4242
+    with _engine(sc) as eng:
+        res = eng.run(seeds)
+        kernel = eng.profile()["kernel"]
+    assert kernel in ("nsm_advance_batch", "nsm_advance_batchw2", "nsm_advance_batchw4")
+    for j, s in enumerate(seeds):
+        out, ev, _ = oracle_lib.nsm_trajectory(sc, int(s), 0)
+        np.testing.assert_array_equal(res["events"][j], ev)
+        np.testing.assert_array_equal(res["counts"][j], out)
