@@ -43,10 +43,11 @@ SEED0 = 20260101
 # voxel + 4 |G_r| dependency entries for a reaction event
 B_DIFF = 2 * (8 * 3 + 16 * 4 + 24) + 8 * 32      # 480
 B_RXN = 8 * 3 + 16 * 4 + 24 + 4 * 5              # 132
-# DRAM bytes (read + write) per event of nsm_advance_batch on this workload,
-# from one ncu capture of the profile case (--profile-case: 6.388 GB over
-# 8,894,255 events in the captured launch; profiles/nsm_advance_batch_rdme40.txt)
-DRAM_BYTES_PER_EVENT = 718.0
+# DRAM bytes (read + write) per event of the event-loop kernel the default
+# policy runs here (nsm_advance_batchw, 4 warps per trajectory), from one ncu
+# capture of the profile case (--profile-case: 7.046 GB over 8,894,255 events
+# in the captured launch; profiles/nsm_advance_batchw4_rdme40.txt)
+DRAM_BYTES_PER_EVENT = 792.0
 
 
 def workload(intervals: int | None = None):
