@@ -40,7 +40,7 @@
 extern "C" {
 #endif
 
-#define SP_ABI_VERSION 1
+#define SP_ABI_VERSION 2
 
 /* ---- return codes ------------------------------------------------------ */
 #define SP_OK              0
@@ -66,6 +66,37 @@ extern "C" {
 #define SP_RXN_FIRST  1   /* k * x[a]                      (1st order)     */
 #define SP_RXN_SECOND 2   /* k * x[a] * x[b] / vol         (a != b)        */
 #define SP_RXN_DIMER  3   /* k * x[a] * (x[a] - 1) / vol   (2a -> ...)     */
+#define SP_RXN_CUSTOM 4   /* a custom propensity_function, evaluated from a
+                             stack program (see sp_scenario.rxn_code)        */
+
+/* ---- custom propensity programs -------------------------------------------
+ * A reaction's propensity_function (the expression the reference compiles
+ * into its generated C++, solver.py:344-373) as postfix code of int32 words,
+ * evaluated in double and rounded to float.  Operands follow their opcode.
+ * The engine checks every program (operands in range, stack depth at most
+ * SP_PROG_MAX_STACK, END reached) before use.                               */
+#define SP_OP_END    0
+#define SP_OP_CONST  1   /* k: push rxn_consts[k] */
+#define SP_OP_X      2   /* s: push the count of species s */
+#define SP_OP_VOL    3   /* push vol = m / rho */
+#define SP_OP_T      4   /* push the time */
+#define SP_OP_TYPE   5   /* push the particle type (sd) */
+#define SP_OP_DATA   6   /* i: push data function i at this particle */
+#define SP_OP_ADD   10
+#define SP_OP_SUB   11
+#define SP_OP_MUL   12
+#define SP_OP_DIV   13
+#define SP_OP_POW   14
+#define SP_OP_NEG   15
+#define SP_OP_POWI  16   /* n (|n| <= 64): integer power by repeated products */
+#define SP_OP_EXP   20   /* .. SP_OP_CEIL: exp log sqrt sin cos tan fabs log10 floor ceil */
+#define SP_OP_CEIL  29
+#define SP_OP_LT    30   /* .. SP_OP_NE: < <= > >= == != as 1.0 / 0.0 */
+#define SP_OP_NE    35
+#define SP_OP_AND   36
+#define SP_OP_OR    37
+#define SP_OP_NOT   38
+#define SP_PROG_MAX_STACK 16
 
 /* ---- NSM selection rule -------------------------------------------------- */
 #define SP_SELECT_EXACT     0  /* uniform rescaled for the channel choice; the
@@ -115,6 +146,14 @@ typedef struct sp_scenario {
     int32_t static_domain;        /* Model.staticDomain */
     int32_t num_outputs;          /* len(TimeSpan.output_steps) */
     const int32_t* output_steps;  /* [num_outputs] ascending step indices */
+
+    /* custom propensities (reactions of kind SP_RXN_CUSTOM); NULL if none */
+    const int32_t* rxn_code;      /* programs of all reactions, concatenated */
+    const int64_t* rxn_code_off;  /* [R+1]: reaction r's program is code[off[r] .. off[r+1]) */
+    const double*  rxn_consts;    /* [num_consts] constants the programs push */
+    int32_t num_consts;
+    int32_t num_data_fn;          /* DataFunction values at the initial positions */
+    const double*  data_fn;       /* [num_data_fn * N], function-major (solver.py:239-249) */
 } sp_scenario;
 
 typedef struct sp_options {

@@ -302,13 +302,81 @@ static void tables_free(nsm_tables_t *t) {
     free(t->rate);
 }
 
+/* a custom propensity program (SP_OP_* in spgpu.h) in double: the same
+   operations in the same order as the kernels' interpreter (nsm_prog.cuh);
+   the engine has checked the program before this runs */
+static double run_program(const sp_scenario *sc, int r, const int32_t *x, double vol, double tm,
+                          int type, int v) {
+    const int32_t *code = sc->rxn_code + sc->rxn_code_off[r];
+    double st[SP_PROG_MAX_STACK];
+    int sp = 0;
+    for (int pc = 0;;) {
+        const int op = code[pc];
+        if (op == SP_OP_END) return st[sp - 1];
+        switch (op) {
+            case SP_OP_CONST: st[sp++] = sc->rxn_consts[code[pc + 1]]; pc += 2; continue;
+            case SP_OP_X: st[sp++] = (double)x[code[pc + 1]]; pc += 2; continue;
+            case SP_OP_VOL: st[sp++] = vol; pc++; continue;
+            case SP_OP_T: st[sp++] = tm; pc++; continue;
+            case SP_OP_TYPE: st[sp++] = (double)type; pc++; continue;
+            case SP_OP_DATA:
+                st[sp++] = sc->data_fn[(size_t)code[pc + 1] * sc->num_particles + v];
+                pc += 2;
+                continue;
+            case SP_OP_NEG: st[sp - 1] = -st[sp - 1]; pc++; continue;
+            case SP_OP_NOT: st[sp - 1] = st[sp - 1] == 0.0 ? 1.0 : 0.0; pc++; continue;
+            case SP_OP_POWI: {
+                const int n = code[pc + 1], m = n < 0 ? -n : n;
+                double p = 1.0;
+                for (int q = 0; q < m; q++) p = p * st[sp - 1];
+                st[sp - 1] = n < 0 ? 1.0 / p : p;
+                pc += 2;
+                continue;
+            }
+            case SP_OP_EXP: st[sp - 1] = exp(st[sp - 1]); pc++; continue;
+            case SP_OP_EXP + 1: st[sp - 1] = log(st[sp - 1]); pc++; continue;
+            case SP_OP_EXP + 2: st[sp - 1] = sqrt(st[sp - 1]); pc++; continue;
+            case SP_OP_EXP + 3: st[sp - 1] = sin(st[sp - 1]); pc++; continue;
+            case SP_OP_EXP + 4: st[sp - 1] = cos(st[sp - 1]); pc++; continue;
+            case SP_OP_EXP + 5: st[sp - 1] = tan(st[sp - 1]); pc++; continue;
+            case SP_OP_EXP + 6: st[sp - 1] = fabs(st[sp - 1]); pc++; continue;
+            case SP_OP_EXP + 7: st[sp - 1] = log10(st[sp - 1]); pc++; continue;
+            case SP_OP_EXP + 8: st[sp - 1] = floor(st[sp - 1]); pc++; continue;
+            case SP_OP_CEIL: st[sp - 1] = ceil(st[sp - 1]); pc++; continue;
+            default: break;
+        }
+        const double b = st[sp - 1], a = st[sp - 2];
+        double res;
+        switch (op) {
+            case SP_OP_ADD: res = a + b; break;
+            case SP_OP_SUB: res = a - b; break;
+            case SP_OP_MUL: res = a * b; break;
+            case SP_OP_DIV: res = a / b; break;
+            case SP_OP_POW: res = pow(a, b); break;
+            case SP_OP_LT: res = a < b ? 1.0 : 0.0; break;
+            case SP_OP_LT + 1: res = a <= b ? 1.0 : 0.0; break;
+            case SP_OP_LT + 2: res = a > b ? 1.0 : 0.0; break;
+            case SP_OP_LT + 3: res = a >= b ? 1.0 : 0.0; break;
+            case SP_OP_LT + 4: res = a == b ? 1.0 : 0.0; break;
+            case SP_OP_NE: res = a != b ? 1.0 : 0.0; break;
+            case SP_OP_AND: res = (a != 0.0 && b != 0.0) ? 1.0 : 0.0; break;
+            default: res = (a != 0.0 || b != 0.0) ? 1.0 : 0.0; break;
+        }
+        st[sp - 2] = res;
+        sp--;
+        pc++;
+    }
+}
+
 /* mass-action propensity in float, the generated code's operator order with
    the second-order division by vol replaced by a product with 1/vol
-   (rounded from double): k*vol, k*A, (k*A*B)*(1/vol), (k*A*(A-1))*(1/vol) */
+   (rounded from double): k*vol, k*A, (k*A*B)*(1/vol), (k*A*(A-1))*(1/vol);
+   a custom propensity is its program's value at time tm, rounded to float */
 static inline float prop(const nsm_tables_t *t, int r, const int32_t *x, float vol, float ivol,
-                         int type) {
+                         int type, int v, double tm) {
     const sp_scenario *sc = t->sc;
     if (sc->rxn_allowed && !sc->rxn_allowed[(size_t)r * (sc->num_types + 1) + type]) return 0.0f;
+    if (sc->rxn_kind[r] == SP_RXN_CUSTOM) return (float)run_program(sc, r, x, (double)vol, tm, type, v);
     const float k = t->rate[r];
     const int a = sc->rxn_reactants[2 * r], b = sc->rxn_reactants[2 * r + 1];
     switch (sc->rxn_kind[r]) {
@@ -320,12 +388,13 @@ static inline float prop(const nsm_tables_t *t, int r, const int32_t *x, float v
 }
 
 /* the voxel whose volume a rate uses: its own, or (reference selection, for
-   a diffusion destination) the source voxel's */
+   a diffusion destination) the source voxel's; tm: the time custom
+   propensities see */
 static inline void voxel_rates(const nsm_tables_t *t, int v, const int32_t *x, int volv,
-                               float *srr, float *sdr) {
+                               float *srr, float *sdr, double tm) {
     const float vol = t->vol[volv], ivol = t->ivol[volv];
     float a = 0.0f;
-    for (int r = 0; r < t->R; r++) a = a + prop(t, r, x, vol, ivol, t->sc->type[v]);
+    for (int r = 0; r < t->R; r++) a = a + prop(t, r, x, vol, ivol, t->sc->type[v], v, tm);
     float d = 0.0f;
     for (int s = 0; s < t->S; s++) d = d + t->ddiag[(size_t)v * t->S + s] * (float)x[s];
     *srr = a;
@@ -404,7 +473,7 @@ static void nsm_build(const nsm_tables_t *t, nsm_state_t *st, double t0, uint32_
     heap_t *h = &st->h;
     for (int v = 0; v < N; v++) {
         float srr, sdr;
-        voxel_rates(t, v, st->x + (size_t)v * S, v, &srr, &sdr);
+        voxel_rates(t, v, st->x + (size_t)v * S, v, &srr, &sdr, 0.0);
         uint32_t ctr[4] = {(uint32_t)v, build_index, 1u, 0u}, r[4];
         spo_philox4x32_10(ctr, st->key, r);
         h->tau[v] = draw_time(t0, spo_neglog_f(u32f(r[0])), srr + sdr);
@@ -444,14 +513,14 @@ static void nsm_window(const nsm_tables_t *t, nsm_state_t *st, int step, int sel
         const float e0 = spo_neglog_f(u32f(r[2])), e1 = spo_neglog_f(u32f(r[3]));
         int32_t *xv = x + (size_t)v * S;
         float srr, sdr;
-        voxel_rates(t, v, xv, v, &srr, &sdr);
+        voxel_rates(t, v, xv, v, &srr, &sdr, tt);
         const float tot = srr + sdr;
         if (ua * tot <= srr) {                               /* :255 rand1 <= srrate/totrate */
             const float target = selection == SP_SELECT_EXACT ? ua * tot : ua * srr;
             float cum = 0.0f;
             int re = -1, last = -1;
             for (int q = 0; q < t->R; q++) {
-                const float a = prop(t, q, xv, t->vol[v], t->ivol[v], sc->type[v]);
+                const float a = prop(t, q, xv, t->vol[v], t->ivol[v], sc->type[v], v, tt);
                 cum = cum + a;
                 if (a > 0.0f) {
                     last = q;
@@ -465,7 +534,7 @@ static void nsm_window(const nsm_tables_t *t, nsm_state_t *st, int step, int sel
                 if (xv[sc->irN[i]] < 0) st->status = SP_TRAJ_NEG_COUNT;
             }
             if (st->status) break;
-            voxel_rates(t, v, xv, v, &srr, &sdr);
+            voxel_rates(t, v, xv, v, &srr, &sdr, tt);
             hp->tau[v] = draw_time(tt, e0, srr + sdr);
             hfix(hp, v);
             st->nrx++;
@@ -501,12 +570,12 @@ static void nsm_window(const nsm_tables_t *t, nsm_state_t *st, int step, int sel
             xv[sp] -= 1;                                          /* :394-402 */
             xw[sp] += 1;            /* w == v (a moving particle's own start-of-step
                                        point in its list): the count is unchanged */
-            voxel_rates(t, v, xv, v, &srr, &sdr);
+            voxel_rates(t, v, xv, v, &srr, &sdr, tt);
             hp->tau[v] = draw_time(tt, e0, srr + sdr);
             hfix(hp, v);
             /* the engine evaluates the destination's reactions with the
                source voxel's volume (simulate_rdme.cpp:431-433) */
-            voxel_rates(t, w, xw, selection == SP_SELECT_REFERENCE ? v : w, &srr, &sdr);
+            voxel_rates(t, w, xw, selection == SP_SELECT_REFERENCE ? v : w, &srr, &sdr, tt);
             hp->tau[w] = draw_time(tt, e1, srr + sdr);
             hfix(hp, w);
             st->ndf++;

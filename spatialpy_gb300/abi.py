@@ -25,11 +25,11 @@ SP_TRAJ_NAN_STATE = 2
 SP_TRAJ_SELECT_OVERFLOW = 3
 SP_TRAJ_BUDGET_EXHAUSTED = 4
 
-SP_RXN_ZERO, SP_RXN_FIRST, SP_RXN_SECOND, SP_RXN_DIMER = 0, 1, 2, 3
+SP_RXN_ZERO, SP_RXN_FIRST, SP_RXN_SECOND, SP_RXN_DIMER, SP_RXN_CUSTOM = 0, 1, 2, 3, 4
 SP_SELECT_EXACT, SP_SELECT_REFERENCE = 0, 1
 SP_PREC_F32, SP_PREC_F64 = 0, 1
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 
 _p = C.POINTER
 
@@ -66,6 +66,12 @@ class SpScenario(C.Structure):
         ("static_domain", C.c_int32),
         ("num_outputs", C.c_int32),
         ("output_steps", _p(C.c_int32)),
+        ("rxn_code", _p(C.c_int32)),
+        ("rxn_code_off", _p(C.c_int64)),
+        ("rxn_consts", _p(C.c_double)),
+        ("num_consts", C.c_int32),
+        ("num_data_fn", C.c_int32),
+        ("data_fn", _p(C.c_double)),
     ]
 
 
@@ -180,6 +186,14 @@ def scenario_struct(sc):
     s.static_domain = int(sc.static_domain)
     s.num_outputs = len(sc.output_steps)
     s.output_steps = ptr(sc.output_steps, C.c_int32)
+    if sc.rxn_code is not None:
+        s.rxn_code = ptr(sc.rxn_code, C.c_int32)
+        s.rxn_code_off = ptr(sc.rxn_code_off, C.c_int64)
+        s.rxn_consts = ptr(sc.rxn_consts, C.c_double)
+        s.num_consts = len(sc.rxn_consts)
+    if sc.data_fn is not None:
+        s.num_data_fn = sc.data_fn.shape[0]
+        s.data_fn = ptr(sc.data_fn, C.c_double)
     return s
 
 

@@ -172,6 +172,13 @@ struct NsmInstance {
     const int32_t* jcN;               // [R+1]
     const int32_t* irN;
     const int32_t* prN;
+    // custom propensities (SP_RXN_CUSTOM), or nullptr
+    const int32_t* code;              // programs, concatenated
+    const int32_t* code_off;          // [R+1]
+    const double* consts;
+    const double* data;               // [num_data * N] data function values
+    int32_t num_data;
+    int32_t has_custom;
 };
 
 // Per-trajectory mutable state (device resident for the whole run).

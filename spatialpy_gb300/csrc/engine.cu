@@ -70,6 +70,10 @@ struct Instance {
     double* diffusion = nullptr;
     int *kind = nullptr, *reac = nullptr, *jcN = nullptr, *irN = nullptr, *prN = nullptr;
     uint8_t* allowed = nullptr;
+    int *code = nullptr, *code_off = nullptr;
+    double *consts = nullptr, *data = nullptr;
+    int num_data = 0;
+    bool has_custom = false;
     uint32_t* u0 = nullptr;   // device copy for the current run
     NsmInstance desc{};
     SdpdState* sdpd = nullptr;
@@ -177,6 +181,50 @@ static int dev_alloc(sp_handle* h, T** dst, size_t n) {
     return dev_upload<T>(h, dst, nullptr, n);
 }
 
+// A custom propensity program must stay inside its reaction's slice, take
+// operands in range, never underflow, stay within SP_PROG_MAX_STACK values and
+// end at SP_OP_END with one value: then the kernels' interpreter cannot read
+// or write out of bounds.  Returns nullptr, or what is wrong.
+static const char* check_program(const sp_scenario& s, int r) {
+    const int64_t b = s.rxn_code_off[r], e = s.rxn_code_off[r + 1];
+    if (b < 0 || e < b || e > s.rxn_code_off[s.num_reactions]) return "program offsets out of order";
+    if (b == e) return "empty program";
+    int d = 0;
+    for (int64_t pc = b; pc < e;) {
+        const int op = s.rxn_code[pc];
+        const int64_t need = (op == SP_OP_CONST || op == SP_OP_X || op == SP_OP_DATA ||
+                              op == SP_OP_POWI) ? 2 : 1;
+        if (pc + need > e) return "operand past the end of the program";
+        const int a = need == 2 ? s.rxn_code[pc + 1] : 0;
+        if (op == SP_OP_END) return d == 1 ? nullptr : "program does not leave one value";
+        if (op == SP_OP_CONST) {
+            if (a < 0 || a >= s.num_consts) return "constant index out of range";
+            d++;
+        } else if (op == SP_OP_X) {
+            if (a < 0 || a >= s.num_species) return "species index out of range";
+            d++;
+        } else if (op == SP_OP_DATA) {
+            if (a < 0 || a >= s.num_data_fn || !s.data_fn) return "data function index out of range";
+            d++;
+        } else if (op == SP_OP_VOL || op == SP_OP_T || op == SP_OP_TYPE) {
+            d++;
+        } else if (op == SP_OP_POWI) {
+            if (a < -64 || a > 64) return "integer power out of range";
+            if (d < 1) return "stack underflow";
+        } else if (op == SP_OP_NEG || op == SP_OP_NOT || (op >= SP_OP_EXP && op <= SP_OP_CEIL)) {
+            if (d < 1) return "stack underflow";
+        } else if ((op >= SP_OP_ADD && op <= SP_OP_POW) || (op >= SP_OP_LT && op <= SP_OP_OR)) {
+            if (d < 2) return "stack underflow";
+            d--;
+        } else {
+            return "unknown opcode";
+        }
+        if (d > SP_PROG_MAX_STACK) return "program needs more than 16 stack values";
+        pc += need;
+    }
+    return "program without END";
+}
+
 static int validate(sp_handle* h, const sp_scenario& s, int i) {
     char b[256];
 #define REQ(cond, msg)                                           \
@@ -210,10 +258,21 @@ static int validate(sp_handle* h, const sp_scenario& s, int i) {
         }
         for (int r = 0; r < s.num_reactions; r++) {
             const int k = s.rxn_kind[r];
-            REQ(k >= SP_RXN_ZERO && k <= SP_RXN_DIMER, "unknown reaction kind");
-            const int a = s.rxn_reactants[2 * r], bb = s.rxn_reactants[2 * r + 1];
-            REQ(k == SP_RXN_ZERO || (a >= 0 && a < s.num_species), "reactant index out of range");
-            REQ(k != SP_RXN_SECOND || (bb >= 0 && bb < s.num_species), "second reactant out of range");
+            REQ(k >= SP_RXN_ZERO && k <= SP_RXN_CUSTOM, "unknown reaction kind");
+            if (k == SP_RXN_CUSTOM) {
+                REQ(s.rxn_code && s.rxn_code_off && (s.rxn_consts || s.num_consts == 0),
+                    "custom propensity programs must be set");
+                const char* why = check_program(s, r);
+                if (why) {
+                    snprintf(b, sizeof b, "scenario %d: reaction %d: %s", i, r, why);
+                    return fail(h, SP_E_INVALID, b);
+                }
+            } else {
+                const int a = s.rxn_reactants[2 * r], bb = s.rxn_reactants[2 * r + 1];
+                REQ(k == SP_RXN_ZERO || (a >= 0 && a < s.num_species), "reactant index out of range");
+                REQ(k != SP_RXN_SECOND || (bb >= 0 && bb < s.num_species),
+                    "second reactant out of range");
+            }
             REQ(s.jcN[r + 1] >= s.jcN[r], "jcN must be non-decreasing");
             for (int64_t q = s.jcN[r]; q < s.jcN[r + 1]; q++)
                 REQ(s.irN[q] >= 0 && s.irN[q] < s.num_species, "irN out of range");
@@ -288,6 +347,23 @@ static int setup_instance(sp_handle* h, const sp_scenario& s, Instance& I) {
         if ((rc = dev_upload(h, &I.prN, pr.data(), pr.size()))) return rc;
     }
     if (S > 0 && (rc = dev_upload(h, &I.diffusion, s.diffusion, (size_t)S * T))) return rc;
+    // custom propensity programs (checked by validate) and data functions
+    for (int r = 0; r < R; r++) I.has_custom |= s.rxn_kind[r] == SP_RXN_CUSTOM;
+    if (I.has_custom) {
+        const int64_t len = s.rxn_code_off[R];
+        std::vector<int> off(R + 1);
+        for (int r = 0; r <= R; r++) off[r] = (int)s.rxn_code_off[r];
+        if ((rc = dev_upload(h, &I.code, s.rxn_code, (size_t)len))) return rc;
+        if ((rc = dev_upload(h, &I.code_off, off.data(), off.size()))) return rc;
+        const double zero = 0.0;
+        if ((rc = dev_upload(h, &I.consts, s.num_consts > 0 ? s.rxn_consts : &zero,
+                             (size_t)(s.num_consts > 0 ? s.num_consts : 1))))
+            return rc;
+    }
+    if (s.num_data_fn > 0 && s.data_fn) {
+        I.num_data = s.num_data_fn;
+        if ((rc = dev_upload(h, &I.data, s.data_fn, (size_t)s.num_data_fn * N))) return rc;
+    }
 
     if (I.is_static) {
         // neighbour lists once (take_step1 at step 0, simulate.cpp:62-64)
@@ -373,6 +449,12 @@ static int setup_instance(sp_handle* h, const sp_scenario& s, Instance& I) {
     d.jcN = I.jcN;
     d.irN = I.irN;
     d.prN = I.prN;
+    d.code = I.code;
+    d.code_off = I.code_off;
+    d.consts = I.consts;
+    d.data = I.data;
+    d.num_data = I.num_data;
+    d.has_custom = I.has_custom ? 1 : 0;
     return SP_OK;
 }
 
@@ -486,6 +568,7 @@ static int net_variant(sp_handle* h, const std::vector<int>& js, const std::vect
     int minS = 1 << 30, minR = 1 << 30, maxS = 0, maxR = 0, maxT = 0;
     for (int j : js) {
         const Instance& I = h->inst[inst[j]];
+        if (I.has_custom) return 0;   // programs run in the generic kernel only
         minS = std::min(minS, I.S);
         minR = std::min(minR, I.R);
         maxS = std::max(maxS, I.S);

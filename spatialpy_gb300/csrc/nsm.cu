@@ -26,6 +26,7 @@
 #include <climits>
 
 #include "common.cuh"
+#include "nsm_prog.cuh"
 #include "nsm_small.cuh"
 
 namespace spg {
@@ -45,18 +46,32 @@ __device__ __forceinline__ float prop(const NsmInstance& I, int r, int xa, int x
     }
 }
 
+// Propensity of reaction r at voxel v, every lane of the warp alike: lane s
+// holds x[s].  Custom propensity programs are evaluated at time t (the
+// event's time; 0 at queue builds, as initialize_rxn_propensities passes,
+// simulate_rdme.cpp:123-124) with the voxel's volume and data functions.
+__device__ __forceinline__ float prop_w(const NsmInstance& I, int r, int xreg, float vol,
+                                        float ivol, int type, int v, double t) {
+    if (I.kind[r] == SP_RXN_CUSTOM) {
+        if (I.allowed && !I.allowed[r * (I.T + 1) + type]) return 0.0f;
+        auto xs = [&](int s) { return __shfl_sync(SP_FULL, xreg, s); };
+        return (float)run_program(I.code + I.code_off[r], I.consts, I.data, I.N, v, xs,
+                                  (double)vol, t, type);
+    }
+    const int ra = I.reac[2 * r], rb = I.reac[2 * r + 1];
+    const int xa = __shfl_sync(SP_FULL, xreg, ra < 0 ? 0 : ra);
+    const int xb = __shfl_sync(SP_FULL, xreg, rb < 0 ? 0 : rb);
+    return prop(I, r, xa, xb, vol, ivol, type);
+}
+
 // Sums of a voxel's reaction propensities and diffusion rates in the engine's
 // order (simulate_rdme.cpp:122-126, 142-150).  Lane s holds x[s] / Ddiag[s];
 // every lane computes the same sums.
 __device__ __forceinline__ void voxel_rates(const NsmInstance& I, int type, float vol, float ivol,
-                                            int xreg, float ddreg, float& srr, float& sdr) {
+                                            int xreg, float ddreg, float& srr, float& sdr,
+                                            int v, double t) {
     float a = 0.0f;
-    for (int r = 0; r < I.R; r++) {
-        const int ra = I.reac[2 * r], rb = I.reac[2 * r + 1];
-        const int xa = __shfl_sync(SP_FULL, xreg, ra < 0 ? 0 : ra);
-        const int xb = __shfl_sync(SP_FULL, xreg, rb < 0 ? 0 : rb);
-        a = a + prop(I, r, xa, xb, vol, ivol, type);
-    }
+    for (int r = 0; r < I.R; r++) a = a + prop_w(I, r, xreg, vol, ivol, type, v, t);
     float d = 0.0f;
     for (int s = 0; s < I.S; s++) {
         const int xs = __shfl_sync(SP_FULL, xreg, s);
@@ -82,6 +97,13 @@ __global__ void nsm_init_leaves(NsmTraj* trajs, const NsmInstance* insts, int nt
         float srr = 0.0f, sdr = 0.0f;
         const int* x = T.x + (size_t)v * I.S;
         for (int r = 0; r < I.R; r++) {
+            if (I.kind[r] == SP_RXN_CUSTOM) {
+                if (I.allowed && !I.allowed[r * (I.T + 1) + I.type[v]]) continue;
+                auto xs = [&](int s) { return x[s]; };
+                srr = srr + (float)run_program(I.code + I.code_off[r], I.consts, I.data, I.N, v,
+                                               xs, (double)I.vol[v], 0.0, I.type[v]);
+                continue;
+            }
             const int ra = I.reac[2 * r], rb = I.reac[2 * r + 1];
             srr = srr + prop(I, r, ra < 0 ? 0 : x[ra], rb < 0 ? 0 : x[rb], I.vol[v], I.ivol[v],
                              I.type[v]);
@@ -278,7 +300,7 @@ __global__ void __launch_bounds__(128) nsm_advance_generic(NsmTraj* trajs, const
                 }
                 long long lgv = LF[(v & ~31) + lane];
                 float srr, sdr;
-                voxel_rates(I, typev, volv, ivolv, xv, ddv, srr, sdr);
+                voxel_rates(I, typev, volv, ivolv, xv, ddv, srr, sdr, v, tt);
                 const float tot = srr + sdr;
                 tlast = tt;
                 if (ua * tot <= srr) {                           // :255 reaction
@@ -286,10 +308,7 @@ __global__ void __launch_bounds__(128) nsm_advance_generic(NsmTraj* trajs, const
                     float cum = 0.0f;
                     int re = -1, last = -1;
                     for (int q = 0; q < I.R; q++) {
-                        const int ra = I.reac[2 * q], rb2 = I.reac[2 * q + 1];
-                        const int xa = __shfl_sync(SP_FULL, xv, ra < 0 ? 0 : ra);
-                        const int xb = __shfl_sync(SP_FULL, xv, rb2 < 0 ? 0 : rb2);
-                        const float a = prop(I, q, xa, xb, volv, ivolv, typev);
+                        const float a = prop_w(I, q, xv, volv, ivolv, typev, v, tt);
                         cum = cum + a;
                         if (a > 0.0f) {
                             last = q;
@@ -304,7 +323,7 @@ __global__ void __launch_bounds__(128) nsm_advance_generic(NsmTraj* trajs, const
                         status = SP_TRAJ_NEG_COUNT; errv = v; break;
                     }
                     if (lane < S) X[(size_t)v * S + lane] = xv;
-                    voxel_rates(I, typev, volv, ivolv, xv, ddv, srr, sdr);
+                    voxel_rates(I, typev, volv, ivolv, xv, ddv, srr, sdr, v, tt);
                     const long long tv = draw_time(tt, e0, srr + sdr);
                     if (lane == (v & 31)) lgv = tv;
                     if (lane == 0) LF[v] = tv;
@@ -374,9 +393,9 @@ __global__ void __launch_bounds__(128) nsm_advance_generic(NsmTraj* trajs, const
                         X[(size_t)v * S + sp] = xv;
                         X[(size_t)w * S + sp] = xw;
                     }
-                    voxel_rates(I, typev, volv, ivolv, xv, ddv, srr, sdr);
+                    voxel_rates(I, typev, volv, ivolv, xv, ddv, srr, sdr, v, tt);
                     const long long tv = draw_time(tt, e0, srr + sdr);
-                    voxel_rates(I, typew, volw, ivolw, xw, ddw, srr, sdr);
+                    voxel_rates(I, typew, volw, ivolw, xw, ddw, srr, sdr, w, tt);
                     const long long tw = draw_time(tt, e1, srr + sdr);
                     if (lane == (v & 31)) lgv = tv;
                     if (samegrp) {

@@ -17,7 +17,8 @@ import math
 
 import numpy as np
 
-from .abi import SP_RXN_DIMER, SP_RXN_FIRST, SP_RXN_SECOND, SP_RXN_ZERO
+from . import propensity as prop
+from .abi import SP_RXN_CUSTOM, SP_RXN_DIMER, SP_RXN_FIRST, SP_RXN_SECOND, SP_RXN_ZERO
 
 
 @dataclasses.dataclass
@@ -51,6 +52,10 @@ class Scenario:
     v: np.ndarray | None = None   # [N,3] float64
     u0: np.ndarray | None = None  # [N,S] uint32 (voxel-major)
     name: str = "scenario"
+    rxn_code: np.ndarray | None = None      # custom propensity programs (int32)
+    rxn_code_off: np.ndarray | None = None  # [R+1] int64
+    rxn_consts: np.ndarray | None = None    # float64
+    data_fn: np.ndarray | None = None       # [num_data_fn, N] float64
 
     def __post_init__(self):
         self.x = np.ascontiguousarray(self.x, dtype=np.float64).reshape(-1, 3)
@@ -79,6 +84,14 @@ class Scenario:
             self.v = np.ascontiguousarray(self.v, dtype=np.float64).reshape(n, 3)
         if self.u0 is not None:
             self.u0 = np.ascontiguousarray(self.u0, dtype=np.uint32).reshape(n, len(self.species))
+        if self.rxn_code is not None:
+            self.rxn_code = np.ascontiguousarray(self.rxn_code, dtype=np.int32)
+            self.rxn_code_off = np.ascontiguousarray(self.rxn_code_off, dtype=np.int64)
+            self.rxn_consts = np.ascontiguousarray(self.rxn_consts, dtype=np.float64)
+            if self.rxn_consts.size == 0:
+                self.rxn_consts = np.zeros(1)
+        if self.data_fn is not None:
+            self.data_fn = np.ascontiguousarray(self.data_fn, dtype=np.float64).reshape(-1, n)
 
     @property
     def num_particles(self) -> int:
@@ -109,12 +122,18 @@ class Scenario:
 # reaction network helpers (mass action, reaction.py:260-313)
 # ----------------------------------------------------------------------------
 
-def mass_action(species: list, reactions: list, num_types: int):
+def mass_action(species: list, reactions: list, num_types: int, params: dict | None = None,
+                data_names: list = (), programs: dict | None = None):
     """Encode ``[(rate, {reactant: stoich}, {product: stoich}, restrict_types|None)]``.
 
     Returns (rate, kind, reactants, allowed, jcN, irN, prN).  The stoichiometry
     CSC matches ``Model.__create_stoichiometric_matrix`` (model.py:252-268):
     per reaction column, rows in ascending species order.
+
+    A rate given as a string is a custom propensity function: the reaction
+    gets kind SP_RXN_CUSTOM and its program (propensity.compile_expression
+    over ``params`` and ``data_names``).  Pass a dict as ``programs`` to
+    receive ``code``, ``off`` and ``consts`` (see :func:`custom_fields`).
     """
     S, R = len(species), len(reactions)
     idx = {s: i for i, s in enumerate(species)}
@@ -125,12 +144,19 @@ def mass_action(species: list, reactions: list, num_types: int):
     allowed[:, 0] = 0
     restricted = False
     dense = np.zeros((S, R), np.int64)
+    progs, consts = [None] * R, []
     for r, (k, reactants, products, types) in enumerate(reactions):
-        rate[r] = float(k)
         order = sum(reactants.values())
-        if order > 2:
+        if isinstance(k, str):
+            kind[r] = SP_RXN_CUSTOM
+            progs[r] = prop.compile_expression(k, species, params or {}, consts, data_names)
+        elif order > 2:
             raise ValueError("mass-action reactions are at most second order")
-        if order == 0:
+        else:
+            rate[r] = float(k)
+        if kind[r] == SP_RXN_CUSTOM:
+            pass
+        elif order == 0:
             kind[r] = SP_RXN_ZERO
         elif len(reactants) == 1 and order == 1:
             kind[r] = SP_RXN_FIRST
@@ -159,8 +185,19 @@ def mass_action(species: list, reactions: list, num_types: int):
                 irN.append(s)
                 prN.append(int(dense[s, r]))
         jcN.append(len(irN))
+    if programs is not None:
+        programs.update(custom_fields(progs, consts))
     return (rate, kind, reac, allowed if restricted else None,
             np.array(jcN, np.int64), np.array(irN, np.int64), np.array(prN, np.int32))
+
+
+def custom_fields(progs: list, consts: list) -> dict:
+    """Scenario fields for custom propensity programs (all None without any)."""
+    if not any(p is not None for p in progs):
+        return {"rxn_code": None, "rxn_code_off": None, "rxn_consts": None}
+    code, off = prop.pack(progs)
+    return {"rxn_code": code, "rxn_code_off": off,
+            "rxn_consts": np.array(consts if consts else [0.0], np.float64)}
 
 
 def find_h(x: np.ndarray) -> float:
@@ -363,7 +400,10 @@ def from_model(model, h: float | None = None) -> Scenario:
     ``restrict_to`` (solver.py:269-286), mass-action propensities
     (reaction.py:260-313; custom propensities raise NotImplementedError),
     ``h = find_h()`` unless given (solver.py:406-410), dimension from the
-    vertex columns (solver.py:404-410)."""
+    vertex columns (solver.py:404-410).  Custom propensity functions become
+    stack programs (propensity.py) over the model's parameters and data
+    functions, the latter evaluated at the initial positions
+    (solver.py:239-249)."""
     stoich, _dep = model.compile_prep()
     dom = model.domain
     tmap = dom.typeNdxMapping
@@ -371,10 +411,18 @@ def from_model(model, h: float | None = None) -> Scenario:
     species = list(model.listOfSpecies.keys())
     type_idx = np.array([tmap[t] for t in dom.type_id], np.int32)
     params = {n: p.value for n, p in model.listOfParameters.items()}
+    data_names = list(getattr(model, "listOfDataFunctions", {}).keys())
     rxns = []
     for rname, r in model.listOfReactions.items():
         if not r.massaction:
-            raise NotImplementedError(f"reaction {rname}: custom propensities are not supported")
+            types = None
+            if r.restrict_to:
+                types = [tmap[t if str(t).startswith("type_") else f"type_{t}"]
+                         for t in r.restrict_to]
+            reactants = {s.name if hasattr(s, "name") else s: n for s, n in r.reactants.items()}
+            products = {s.name if hasattr(s, "name") else s: n for s, n in r.products.items()}
+            rxns.append((str(r.propensity_function), reactants, products, types))
+            continue
         k = r.marate
         if hasattr(k, "value"):
             k = k.value
@@ -386,7 +434,17 @@ def from_model(model, h: float | None = None) -> Scenario:
         if r.restrict_to:
             types = [tmap[t if str(t).startswith("type_") else f"type_{t}"] for t in r.restrict_to]
         rxns.append((float(k), reactants, products, types))
-    rate, kind, reac, allowed, jcN, irN, prN = mass_action(species, rxns, T)
+    programs = {}
+    try:
+        rate, kind, reac, allowed, jcN, irN, prN = mass_action(species, rxns, T, params,
+                                                               data_names, programs)
+    except prop.PropensityError as err:
+        raise NotImplementedError(str(err)) from err
+    data_fn = None
+    if data_names:
+        coords = np.asarray(dom.coordinates(), np.float64)
+        data_fn = np.array([[float(f.map([c[0], c[1], c[2]])) for c in coords]
+                            for f in model.listOfDataFunctions.values()])
     # the stoichiometry must agree with compile_prep's CSC
     if stoich is not None and min(stoich.shape) > 0:
         assert np.array_equal(np.asarray(stoich.indptr), jcN)
@@ -418,4 +476,4 @@ def from_model(model, h: float | None = None) -> Scenario:
                     static_domain=bool(model.staticDomain), rho0=float(dom.rho0),
                     c0=float(dom.c0), P0=float(dom.P0),
                     gravity=tuple(dom.gravity) if dom.gravity is not None else (0.0, 0.0, 0.0),
-                    u0=u0, name=model.name)
+                    u0=u0, name=model.name, data_fn=data_fn, **programs)
