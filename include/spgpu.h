@@ -40,7 +40,7 @@
 extern "C" {
 #endif
 
-#define SP_ABI_VERSION 2
+#define SP_ABI_VERSION 3
 
 /* ---- return codes ------------------------------------------------------ */
 #define SP_OK              0
@@ -154,7 +154,28 @@ typedef struct sp_scenario {
     int32_t num_consts;
     int32_t num_data_fn;          /* DataFunction values at the initial positions */
     const double*  data_fn;       /* [num_data_fn * N], function-major (solver.py:239-249) */
+
+    /* deterministic chemistry (Model.enable_pde): concentrations C[N*S] that
+       start at u0 and follow the reactions' ode_propensity_function and SPH
+       diffusion (model.cpp:151-189, simulate.cpp:81-85, 167-169) */
+    int32_t enable_pde;
+    const int32_t* ode_code;      /* programs as rxn_code, one per reaction; SP_OP_X reads C */
+    const int64_t* ode_code_off;  /* [R+1] */
+    const double*  ode_consts;
+    int32_t num_ode_consts;
+    /* boundary conditions (BoundaryCondition.expression, boundarycondition.py:121-167),
+       applied in order after the predictor and after the corrector */
+    int32_t num_bcs;
+    const double*  bc_box;        /* [num_bcs*6] xmin xmax ymin ymax zmin zmax (+-inf: none) */
+    const int32_t* bc_type;       /* [num_bcs] particle type the condition needs, 0 = any */
+    const int32_t* bc_target;     /* [num_bcs] SP_BC_V, SP_BC_NU, SP_BC_RHO or SP_BC_C + s */
+    const double*  bc_value;      /* [num_bcs*3] value (v uses all three) */
 } sp_scenario;
+
+#define SP_BC_V   0
+#define SP_BC_NU  1
+#define SP_BC_RHO 2
+#define SP_BC_C   3   /* + species index: a deterministic concentration */
 
 typedef struct sp_options {
     int32_t device;               /* CUDA device ordinal */
@@ -188,6 +209,7 @@ typedef struct sp_run_args {
     int32_t want_counts;          /* write per-output counts */
     int32_t want_moments;         /* write per-instance moment sums over trajectories */
     int32_t want_particles;       /* write per-output particle state (non-static) */
+    int32_t want_chem;            /* write per-output deterministic concentrations */
     double  timeout_s;            /* 0 = none; else SP_E_TIMEOUT once exceeded */
 } sp_run_args;
 
@@ -204,6 +226,9 @@ typedef struct sp_outputs {
     /* [ntraj*2] (reaction events, diffusion events) — the engine counters
        total_reactions / total_diffusion (simulate_rdme.cpp:310, 445) */
     int64_t* event_counts;
+    /* [sum_i num_outputs_i * N_i * S_i] deterministic concentrations C of the
+       instances with enable_pde (written when want_chem), instance-major */
+    double* chem;
 } sp_outputs;
 
 typedef struct sp_traj_status {

@@ -67,14 +67,20 @@ def lib():
                                        _p(C.c_int64), _p(C.c_int32)]
         for fn in (L.spo_sdpd_f64, L.spo_sdpd_f32):
             fn.argtypes = [_p(SpScenario), C.c_int32, C.c_int32, C.c_int32, C.c_int32] + \
-                [_p(C.c_double)] * 7 + [_p(C.c_int32), C.c_void_p]
+                [_p(C.c_double)] * 7 + [_p(C.c_int32), C.c_void_p, C.c_void_p]
         L.spo_coupled_ensemble.argtypes = [_p(SpScenario), _p(C.c_uint32), _p(C.c_uint64),
                                            C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                            C.c_int32, C.c_int32, _p(C.c_int32),
                                            _p(C.c_int64), _p(C.c_int32), _p(C.c_double),
-                                           _p(C.c_double)]
+                                           _p(C.c_double), _p(C.c_double)]
+        L.spo_chem_static.argtypes = [_p(SpScenario), _p(C.c_uint32), C.c_int32,
+                                      _p(C.c_double)]
         _lib = L
     return _lib
+
+
+class SpoChem(C.Structure):
+    _fields_ = [("C", _p(C.c_double)), ("Q", _p(C.c_double)), ("nu", _p(C.c_double))]
 
 
 def _ptr(a, t):
@@ -166,6 +172,7 @@ class SdpdState:
         self.Frho = np.zeros(n)
         self.step = 0
         self.nbr_count = np.zeros(n, np.int32)
+        self.nu = sc.nu.copy()      # boundary conditions may change it
 
 
 def sdpd(sc, state: SdpdState, nsteps: int, precision: str = "f64", mode: int = 2,
@@ -177,16 +184,29 @@ def sdpd(sc, state: SdpdState, nsteps: int, precision: str = "f64", mode: int = 
     rc = fn(C.byref(s), state.step, nsteps, mode, kmax, _ptr(state.x, C.c_double),
             _ptr(state.v, C.c_double), _ptr(state.vt, C.c_double), _ptr(state.rho, C.c_double),
             _ptr(state.F, C.c_double), _ptr(state.Fbp, C.c_double), _ptr(state.Frho, C.c_double),
-            _ptr(state.nbr_count, C.c_int32), None)
+            _ptr(state.nbr_count, C.c_int32), None,
+            C.byref(SpoChem(None, None, _ptr(state.nu, C.c_double))))
     if rc != 0:
         raise RuntimeError(f"SDPD oracle failed (rc={rc})")
     state.step += nsteps
     return state
 
 
+def chem_static(sc, kmax: int = 64, u0=None):
+    """Deterministic concentrations of a static domain (enable_pde) at every
+    output: [T, N, S]."""
+    u0 = np.ascontiguousarray(sc.u0 if u0 is None else u0, np.uint32)
+    s = scenario_struct(sc)
+    out = np.zeros((len(sc.output_steps), sc.num_particles, sc.num_species))
+    rc = lib().spo_chem_static(C.byref(s), _ptr(u0, C.c_uint32), kmax, _ptr(out, C.c_double))
+    if rc != 0:
+        raise RuntimeError(f"chemistry oracle failed (rc={rc})")
+    return out
+
+
 def coupled_ensemble(sc, seeds, selection: int = 0, precision: str = "f32", mode: int = 6,
                      kmax: int = 48, u0=None, want_particles: bool = True, threads: int = 0,
-                     want_counts: bool = True):
+                     want_counts: bool = True, want_chem: bool = False):
     """Moving domain with species: the SDPD flow plus, every step, new
     diffusion tables, volumes and event queues for each trajectory.
     Returns (counts [ntraj,T,N,S], events [ntraj,2], status [ntraj],
@@ -200,13 +220,16 @@ def coupled_ensemble(sc, seeds, selection: int = 0, precision: str = "f32", mode
     st = np.zeros(nt, np.int32)
     px = np.zeros((T, n, 3)) if want_particles else None
     pr = np.zeros((T, n)) if want_particles else None
+    ch = np.zeros((T, n, sc.num_species)) if want_chem else None
     rc = lib().spo_coupled_ensemble(C.byref(s), _ptr(u0, C.c_uint32), _ptr(seeds, C.c_uint64),
                                     nt, selection, 64 if precision == "f64" else 32, mode, kmax,
                                     threads, _ptr(out, C.c_int32), _ptr(ev, C.c_int64),
                                     _ptr(st, C.c_int32), _ptr(px, C.c_double),
-                                    _ptr(pr, C.c_double))
+                                    _ptr(pr, C.c_double), _ptr(ch, C.c_double))
     if rc != 0:
         raise RuntimeError(f"coupled oracle failed (rc={rc})")
+    if want_chem:
+        return out, ev, st, px, pr, ch
     return out, ev, st, px, pr
 
 

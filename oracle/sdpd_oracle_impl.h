@@ -115,7 +115,8 @@ static int SPO_NB(int n, int dim, const REAL *xq, const REAL *xt, REAL h, const 
 
 int SPO_FN(const sp_scenario *sc, int32_t step0, int32_t nsteps, int32_t mode, int32_t kmax,
            double *x_io, double *v_io, double *vt_io, double *rho_io, double *F_io,
-           double *Fbp_io, double *Frho_io, int32_t *nbr_count, spo_sdpd_lists *lists) {
+           double *Fbp_io, double *Frho_io, int32_t *nbr_count, spo_sdpd_lists *lists,
+           spo_chem *chem) {
     const int n = sc->num_particles, dim = sc->dimension;
     const REAL h = (REAL)sc->h, dt = (REAL)sc->dt, rho0 = (REAL)sc->rho0, P0 = (REAL)sc->P0;
     const REAL g[3] = {(REAL)sc->gravity[0], (REAL)sc->gravity[1], (REAL)sc->gravity[2]};
@@ -133,13 +134,20 @@ int SPO_FN(const sp_scenario *sc, int32_t step0, int32_t nsteps, int32_t mode, i
     int32_t *nidx = (int32_t *)malloc(sizeof(int32_t) * (size_t)n * kmax);
     int32_t *ncnt = (int32_t *)malloc(sizeof(int32_t) * n);
     REAL *ndij = lists ? (REAL *)malloc(sizeof(REAL) * (size_t)n * kmax) : NULL;
+    /* double copies for the chemistry and the boundary conditions */
+    double *pd = (double *)malloc(sizeof(double) * 3 * n);
+    double *dd = chem ? (double *)malloc(sizeof(double) * (size_t)n * kmax) : NULL;
+    double *wd = chem ? (double *)malloc(sizeof(double) * (size_t)n * kmax) : NULL;
+    double *md = chem ? (double *)malloc(sizeof(double) * n) : NULL;
+    double *rd = chem ? (double *)malloc(sizeof(double) * n) : NULL;
+    const int do_chem = chem && chem->C && sc->enable_pde && sc->num_species > 0;
     for (int i = 0; i < 3 * n; i++) {
         x[i] = (REAL)x_io[i]; v[i] = (REAL)v_io[i]; vt[i] = (REAL)vt_io[i];
         F[i] = (REAL)F_io[i]; Fbp[i] = (REAL)Fbp_io[i];
     }
     for (int i = 0; i < n; i++) {
         rho[i] = (REAL)rho_io[i]; Frho[i] = (REAL)Frho_io[i];
-        m[i] = (REAL)sc->mass[i]; nu[i] = (REAL)sc->nu[i];
+        m[i] = (REAL)sc->mass[i]; nu[i] = (REAL)(chem && chem->nu ? chem->nu[i] : sc->nu[i]);
     }
     int rc = 0;
     for (int step = step0; step < step0 + nsteps && !rc; step++) {
@@ -158,11 +166,24 @@ int SPO_FN(const sp_scenario *sc, int32_t step0, int32_t nsteps, int32_t mode, i
                 }
                 rho[i] = rho[i] + K_(0.5) * dt * Frho[i];
             }
+            if (sc->num_bcs) {   /* applyBoundaryConditions after the predictor */
+                double p[3] = {(double)x[3 * i], (double)x[3 * i + 1], (double)x[3 * i + 2]};
+                double vv[3] = {(double)v[3 * i], (double)v[3 * i + 1], (double)v[3 * i + 2]};
+                double nn = (double)nu[i], rr = (double)rho[i];
+                spo_flow_bcs(sc, i, p, vv, &nn, &rr);
+                for (int d = 0; d < 3; d++) v[3 * i + d] = (REAL)vv[d];
+                nu[i] = (REAL)nn;
+                rho[i] = (REAL)rr;
+            }
             for (int d = 0; d < 3; d++) { F[3 * i + d] = g[d]; Fbp[3 * i + d] = 0; }
             Frho[i] = 0;
             orho[i] = rho[i];
         }
         if (rc) break;
+        if (do_chem) {
+            for (int e = 0; e < 3 * n; e++) pd[e] = (double)x[e];
+            spo_chem_half(sc, chem->C, chem->Q, pd, 3, step == 0, 1);
+        }
         /* neighbour lists used by substeps 1-2 (particle.cpp:240-294): at step 0
            from the unmoved points; later from moved queries against the
            start-of-step points (mode 2) or against moved points */
@@ -242,6 +263,15 @@ int SPO_FN(const sp_scenario *sc, int32_t step0, int32_t nsteps, int32_t mode, i
             for (int d = 0; d < 3; d++) { F[3 * i + d] = Fi[d]; Fbp[3 * i + d] = Fb[d]; }
             Frho[i] = Fr;
         }
+        if (do_chem) {   /* the chemistry part of pairwiseForce (model.cpp:151-189) */
+            for (size_t e = 0; e < (size_t)n * kmax; e++) {
+                dd[e] = (double)ndist[e];
+                wd[e] = (double)ndw[e];
+            }
+            for (int i = 0; i < n; i++) { md[i] = (double)m[i]; rd[i] = (double)rho[i]; }
+            spo_chem_flux(sc, chem->C, chem->Q, ncnt, nidx, dd, wd, kmax, md, rd,
+                          sc->dt * (double)step);
+        }
         /* substep 2: take_step2 (simulate.cpp:132-173) */
         const REAL *rb = (mode & 1) ? rho : orho;   /* density read by the BVF pass */
         for (int i = 0; i < n; i++) {
@@ -296,6 +326,19 @@ int SPO_FN(const sp_scenario *sc, int32_t step0, int32_t nsteps, int32_t mode, i
                     for (int d = 0; d < dim; d++)
                         v[3 * i + d] = -v[3 * i + d] + K_(2.0) * FMAX(K_(0.0), vdn) * nrm[3 * i + d];
             }
+            if (sc->num_bcs) {   /* applyBoundaryConditions after the corrector */
+                double p[3] = {(double)x[3 * i], (double)x[3 * i + 1], (double)x[3 * i + 2]};
+                double vv[3] = {(double)v[3 * i], (double)v[3 * i + 1], (double)v[3 * i + 2]};
+                double nn = (double)nu[i], rr = (double)rho[i];
+                spo_flow_bcs(sc, i, p, vv, &nn, &rr);
+                for (int d = 0; d < 3; d++) v[3 * i + d] = (REAL)vv[d];
+                nu[i] = (REAL)nn;
+                rho[i] = (REAL)rr;
+            }
+        }
+        if (do_chem) {
+            for (int e = 0; e < 3 * n; e++) pd[e] = (double)x[e];
+            spo_chem_half(sc, chem->C, chem->Q, pd, 3, 0, 0);
         }
     }
     for (int i = 0; i < 3 * n; i++) {
@@ -309,7 +352,9 @@ int SPO_FN(const sp_scenario *sc, int32_t step0, int32_t nsteps, int32_t mode, i
         memcpy(lists->idx, nidx, sizeof(int32_t) * (size_t)n * kmax);
         for (size_t e = 0; e < (size_t)n * kmax; e++) lists->dij[e] = (double)ndij[e];
     }
-    free(ndij);
+    if (chem && chem->nu)
+        for (int i = 0; i < n; i++) chem->nu[i] = (double)nu[i];
+    free(ndij); free(pd); free(dd); free(wd); free(md); free(rd);
     free(x); free(xt); free(v); free(vt); free(F); free(Fbp); free(rho); free(orho); free(Frho);
     free(m); free(nu); free(nrm); free(ndist); free(ndw); free(nidx); free(ncnt); free(sd2);
     return rc;

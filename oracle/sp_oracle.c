@@ -305,17 +305,31 @@ static void tables_free(nsm_tables_t *t) {
 /* a custom propensity program (SP_OP_* in spgpu.h) in double: the same
    operations in the same order as the kernels' interpreter (nsm_prog.cuh);
    the engine has checked the program before this runs */
+static double run_program_x(const sp_scenario *sc, const int32_t *code, const double *consts,
+                            const int32_t *xi, const double *xd, double vol, double tm, int type,
+                            int v);
+
 static double run_program(const sp_scenario *sc, int r, const int32_t *x, double vol, double tm,
                           int type, int v) {
-    const int32_t *code = sc->rxn_code + sc->rxn_code_off[r];
+    return run_program_x(sc, sc->rxn_code + sc->rxn_code_off[r], sc->rxn_consts, x, NULL, vol,
+                         tm, type, v);
+}
+
+/* xi: integer counts, or xd: concentrations (exactly one is set) */
+static double run_program_x(const sp_scenario *sc, const int32_t *code, const double *consts,
+                            const int32_t *xi, const double *xd, double vol, double tm, int type,
+                            int v) {
     double st[SP_PROG_MAX_STACK];
     int sp = 0;
     for (int pc = 0;;) {
         const int op = code[pc];
         if (op == SP_OP_END) return st[sp - 1];
         switch (op) {
-            case SP_OP_CONST: st[sp++] = sc->rxn_consts[code[pc + 1]]; pc += 2; continue;
-            case SP_OP_X: st[sp++] = (double)x[code[pc + 1]]; pc += 2; continue;
+            case SP_OP_CONST: st[sp++] = consts[code[pc + 1]]; pc += 2; continue;
+            case SP_OP_X:
+                st[sp++] = xd ? xd[code[pc + 1]] : (double)xi[code[pc + 1]];
+                pc += 2;
+                continue;
             case SP_OP_VOL: st[sp++] = vol; pc++; continue;
             case SP_OP_T: st[sp++] = tm; pc++; continue;
             case SP_OP_TYPE: st[sp++] = (double)type; pc++; continue;
@@ -693,7 +707,7 @@ static void *coupled_worker(void *arg) {
 int spo_coupled_ensemble(const sp_scenario *sc, const uint32_t *u0, const uint64_t *seeds,
                          int32_t ntraj, int32_t selection, int32_t precision, int32_t mode,
                          int32_t kmax, int32_t threads, int32_t *out, int64_t *ev,
-                         int32_t *status, double *px, double *prho) {
+                         int32_t *status, double *px, double *prho, double *chem_out) {
     const int N = sc->num_particles, S = sc->num_species, R = sc->num_reactions;
     int nth = threads <= 0 ? (int)sysconf(_SC_NPROCESSORS_ONLN) : threads;
     if (nth > ntraj) nth = ntraj;
@@ -729,6 +743,13 @@ int spo_coupled_ensemble(const sp_scenario *sc, const uint32_t *u0, const uint64
     for (int r = 0; r < R; r++) t.rate[r] = (float)sc->rxn_rate[r];
     nsm_state_t *st = (nsm_state_t *)malloc(sizeof(nsm_state_t) * ntraj);
     for (int j = 0; j < ntraj; j++) nsm_state_init(&st[j], &t, u0, seeds[j]);
+    spo_chem ch;
+    ch.C = sc->enable_pde ? (double *)calloc(NS, sizeof(double)) : NULL;
+    ch.Q = sc->enable_pde ? (double *)calloc(NS, sizeof(double)) : NULL;
+    ch.nu = (double *)malloc(sizeof(double) * N);
+    memcpy(ch.nu, sc->nu, sizeof(double) * N);
+    if (ch.C)
+        for (size_t e = 0; e < NS; e++) ch.C[e] = (double)u0[e];
     int rc = 0, oi = 0;
     const int nout = sc->num_outputs;
     for (int step = 0; step < sc->num_steps && !rc; step++) {
@@ -737,11 +758,12 @@ int spo_coupled_ensemble(const sp_scenario *sc, const uint32_t *u0, const uint64
                 memcpy(out + ((size_t)j * nout + oi) * NS, st[j].x, sizeof(int32_t) * NS);
             if (px) memcpy(px + (size_t)oi * 3 * N, x, sizeof(double) * 3 * N);
             if (prho) memcpy(prho + (size_t)oi * N, rho, sizeof(double) * N);
+            if (chem_out && ch.C) memcpy(chem_out + (size_t)oi * NS, ch.C, sizeof(double) * NS);
             oi++;
         }
         rc = precision == 64
-                 ? spo_sdpd_f64(sc, step, 1, mode, kmax, x, v, vt, rho, F, Fbp, Frho, NULL, &L)
-                 : spo_sdpd_f32(sc, step, 1, mode, kmax, x, v, vt, rho, F, Fbp, Frho, NULL, &L);
+                 ? spo_sdpd_f64(sc, step, 1, mode, kmax, x, v, vt, rho, F, Fbp, Frho, NULL, &L, &ch)
+                 : spo_sdpd_f32(sc, step, 1, mode, kmax, x, v, vt, rho, F, Fbp, Frho, NULL, &L, &ch);
         if (rc) break;
         /* nsm_core__initialize_rxn/diff_propensities (simulate_rdme.cpp:113-152)
            with this step's lists and the end-of-step densities */
@@ -765,8 +787,10 @@ int spo_coupled_ensemble(const sp_scenario *sc, const uint32_t *u0, const uint64
             memcpy(out + ((size_t)j * nout + oi) * NS, st[j].x, sizeof(int32_t) * NS);
         if (px) memcpy(px + (size_t)oi * 3 * N, x, sizeof(double) * 3 * N);
         if (prho) memcpy(prho + (size_t)oi * N, rho, sizeof(double) * N);
+        if (chem_out && ch.C) memcpy(chem_out + (size_t)oi * NS, ch.C, sizeof(double) * NS);
         oi++;
     }
+    free(ch.C); free(ch.Q); free(ch.nu);
     for (int j = 0; j < ntraj; j++) {
         ev[2 * j] = st[j].nrx;
         ev[2 * j + 1] = st[j].ndf;
@@ -778,5 +802,115 @@ int spo_coupled_ensemble(const sp_scenario *sc, const uint32_t *u0, const uint64
     free(t.cdf); free(t.ddiag); free(t.vol); free(t.ivol); free(t.rate);
     free(L.count); free(L.idx); free(L.dij);
     free(x); free(v); free(vt); free(F); free(Fbp); free(rho); free(Frho);
+    return rc;
+}
+
+/* ------------------------------------------------------------------------
+ * Deterministic chemistry and boundary conditions
+ * ------------------------------------------------------------------------ */
+static int bc_hit(const sp_scenario *sc, int b, int i, const double p[3]) {
+    const double *bx = sc->bc_box + 6 * b;
+    return p[0] >= bx[0] && p[0] <= bx[1] && p[1] >= bx[2] && p[1] <= bx[3] && p[2] >= bx[4] &&
+           p[2] <= bx[5] && (sc->bc_type[b] == 0 || sc->bc_type[b] == sc->type[i]);
+}
+
+void spo_flow_bcs(const sp_scenario *sc, int i, const double p[3], double v[3], double *nu,
+                  double *rho) {
+    for (int b = 0; b < sc->num_bcs; b++) {
+        const int tg = sc->bc_target[b];
+        if (tg >= SP_BC_C || !bc_hit(sc, b, i, p)) continue;
+        const double *val = sc->bc_value + 3 * b;
+        if (tg == SP_BC_V) { v[0] = val[0]; v[1] = val[1]; v[2] = val[2]; }
+        else if (tg == SP_BC_NU) *nu = val[0];
+        else *rho = val[0];
+    }
+}
+
+void spo_chem_half(const sp_scenario *sc, double *C, double *Q, const double *pos, int pstride,
+                   int first, int clear_q) {
+    const int N = sc->num_particles, S = sc->num_species;
+    const double coef = first ? 0.0 : 0.5 * sc->dt;
+    for (int i = 0; i < N; i++) {
+        double *c = C + (size_t)i * S, *q = Q + (size_t)i * S;
+        if (coef != 0.0)
+            for (int s = 0; s < S; s++) c[s] = c[s] + q[s] * coef;
+        if (sc->num_bcs) {
+            const double *p = pos + (size_t)i * pstride;
+            for (int b = 0; b < sc->num_bcs; b++) {
+                const int tg = sc->bc_target[b];
+                if (tg >= SP_BC_C && bc_hit(sc, b, i, p)) c[tg - SP_BC_C] = sc->bc_value[3 * b];
+            }
+        }
+        if (clear_q)
+            for (int s = 0; s < S; s++) q[s] = 0.0;
+    }
+}
+
+void spo_chem_flux(const sp_scenario *sc, const double *C, double *Q, const int32_t *cnt,
+                   const int32_t *idx, const double *dist, const double *dwdr, int kstride,
+                   const double *mass, const double *rho, double t) {
+    const int N = sc->num_particles, S = sc->num_species, R = sc->num_reactions,
+              T = sc->num_types;
+    const double h = sc->h;
+    int *dense = (int *)calloc((size_t)S * (R > 0 ? R : 1), sizeof(int));
+    for (int r = 0; r < R; r++)
+        for (int64_t q = sc->jcN[r]; q < sc->jcN[r + 1]; q++)
+            dense[(size_t)sc->irN[q] * R + r] += sc->prN[q];
+    for (int i = 0; i < N; i++) {
+        const double *ci = C + (size_t)i * S;
+        double *q = Q + (size_t)i * S;
+        const double mi = mass[i], ri = rho[i];
+        const int ti = sc->type[i];
+        for (int k = 0; k < cnt[i]; k++) {
+            const size_t o = (size_t)i * kstride + k;
+            const double r = dist[o];
+            if (r / h > 1.0 || r == 0.0) continue;
+            const int j = idx[o];
+            const double mj = mass[j], rj = rho[j];
+            const double wfd = (1.0 / (r + 0.001 * h)) * dwdr[o];
+            const double base = 2.0 * ((mi * mj) / (mi + mj)) * ((ri + rj) / (ri * rj)) * (r * r) *
+                                wfd / ((r * r) + 0.01 * h * h);
+            const double *cj = C + (size_t)j * S;
+            for (int s = 0; s < S; s++)
+                q[s] = q[s] + sc->diffusion[s * T + (ti - 1)] * (ci[s] - cj[s]) * base;
+        }
+        const double vol = mi / ri;
+        for (int r = 0; r < R; r++) {
+            if (sc->rxn_allowed && !sc->rxn_allowed[(size_t)r * (T + 1) + ti]) continue;
+            const double flux = run_program_x(sc, sc->ode_code + sc->ode_code_off[r], sc->ode_consts,
+                                              NULL, ci, vol, t, ti, i);
+            for (int s = 0; s < S; s++) q[s] = q[s] + (double)dense[(size_t)s * R + r] * flux;
+        }
+    }
+    free(dense);
+}
+
+int spo_chem_static(const sp_scenario *sc, const uint32_t *u0, int32_t kmax, double *out) {
+    const int N = sc->num_particles, S = sc->num_species;
+    int32_t *cnt = (int32_t *)malloc(sizeof(int32_t) * N);
+    int32_t *idx = (int32_t *)malloc(sizeof(int32_t) * (size_t)N * kmax);
+    double *dist = (double *)malloc(sizeof(double) * (size_t)N * kmax);
+    double *dw = (double *)malloc(sizeof(double) * (size_t)N * kmax);
+    int rc = spo_neighbors(N, sc->dimension, sc->x, sc->x, sc->h, sc->mass, sc->rho, kmax, cnt, idx,
+                           dist, dw, NULL);
+    double *C = (double *)calloc((size_t)N * S, sizeof(double));
+    double *Q = (double *)calloc((size_t)N * S, sizeof(double));
+    for (size_t e = 0; e < (size_t)N * S; e++) C[e] = (double)u0[e];   /* C = u0 */
+    int oi = 0;
+    const int nout = sc->num_outputs;
+    for (int step = 0; step < sc->num_steps && !rc; step++) {
+        while (oi < nout && sc->output_steps[oi] <= step) {
+            memcpy(out + (size_t)oi * N * S, C, sizeof(double) * N * S);
+            oi++;
+        }
+        spo_chem_half(sc, C, Q, sc->x, 3, step == 0, 1);
+        spo_chem_flux(sc, C, Q, cnt, idx, dist, dw, kmax, sc->mass, sc->rho, sc->dt * (double)step);
+        spo_chem_half(sc, C, Q, sc->x, 3, 0, 0);
+    }
+    while (!rc && oi < nout) {
+        memcpy(out + (size_t)oi * N * S, C, sizeof(double) * N * S);
+        oi++;
+    }
+    free(cnt); free(idx); free(dist); free(dw); free(C); free(Q);
     return rc;
 }

@@ -76,12 +76,40 @@ typedef struct spo_sdpd_lists {
     int32_t *idx;
     double *dij;
 } spo_sdpd_lists;
+/* chem: deterministic concentrations C and fluxes Q ([N*S] double each) to
+ * advance with the flow when sc->enable_pde (NULL: none); nu: the particle
+ * viscosities [N], updated by boundary conditions (NULL: sc->nu). */
+typedef struct spo_chem {
+    double *C;
+    double *Q;
+    double *nu;
+} spo_chem;
 int spo_sdpd_f64(const sp_scenario *sc, int32_t step0, int32_t nsteps, int32_t mode, int32_t kmax,
                  double *x, double *v, double *vt, double *rho, double *F, double *Fbp,
-                 double *Frho, int32_t *nbr_count, spo_sdpd_lists *lists);
+                 double *Frho, int32_t *nbr_count, spo_sdpd_lists *lists, spo_chem *chem);
 int spo_sdpd_f32(const sp_scenario *sc, int32_t step0, int32_t nsteps, int32_t mode, int32_t kmax,
                  double *x, double *v, double *vt, double *rho, double *F, double *Fbp,
-                 double *Frho, int32_t *nbr_count, spo_sdpd_lists *lists);
+                 double *Frho, int32_t *nbr_count, spo_sdpd_lists *lists, spo_chem *chem);
+
+/* Deterministic chemistry (Model.enable_pde; model.cpp:151-189,
+ * simulate.cpp:81-88, 166-171) with the layouts the matrices are written in
+ * (species-major diffusion, N[s][r]).
+ * spo_chem_half: C += Q dt/2 (not when first), the boundary conditions on
+ * concentrations (positions [N*pstride]), then Q = 0 when clear_q.
+ * spo_chem_flux: Q from neighbour lists (skipping r = 0 and r > h) and the
+ * reactions' ODE rate programs at time t.
+ * spo_chem_static: a static domain from C = u0 over the time span, with the
+ * oracle's fixed neighbour lists; out [num_outputs][N][S]. */
+void spo_chem_half(const sp_scenario *sc, double *C, double *Q, const double *pos, int pstride,
+                   int first, int clear_q);
+void spo_chem_flux(const sp_scenario *sc, const double *C, double *Q, const int32_t *cnt,
+                   const int32_t *idx, const double *dist, const double *dwdr, int kstride,
+                   const double *mass, const double *rho, double t);
+int spo_chem_static(const sp_scenario *sc, const uint32_t *u0, int32_t kmax, double *out);
+/* boundary conditions on v, nu, rho of particle i at position p (after the
+ * predictor and after the corrector, simulate.cpp:88, 171) */
+void spo_flow_bcs(const sp_scenario *sc, int i, const double p[3], double v[3], double *nu,
+                  double *rho);
 
 /*
  * Moving domain with stochastic species (simulate_threads.cpp:232-281 with
@@ -94,12 +122,14 @@ int spo_sdpd_f32(const sp_scenario *sc, int32_t step0, int32_t nsteps, int32_t m
  * step on `threads` POSIX threads (0 = all cores).
  * out: [ntraj][num_outputs][N][S] counts or NULL; px/prho:
  * [num_outputs][N*3] / [num_outputs][N] flow state or NULL; ev: [ntraj*2];
- * status: [ntraj].  Returns 0, -1 on a list overflow, 2 on NaN state.
+ * status: [ntraj]; chem_out: [num_outputs][N][S] deterministic
+ * concentrations (enable_pde) or NULL.  Returns 0, -1 on a list overflow,
+ * 2 on NaN state.
  */
 int spo_coupled_ensemble(const sp_scenario *sc, const uint32_t *u0, const uint64_t *seeds,
                          int32_t ntraj, int32_t selection, int32_t precision, int32_t mode,
                          int32_t kmax, int32_t threads, int32_t *out, int64_t *ev,
-                         int32_t *status, double *px, double *prho);
+                         int32_t *status, double *px, double *prho, double *chem_out);
 
 #ifdef __cplusplus
 }

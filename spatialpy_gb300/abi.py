@@ -26,10 +26,11 @@ SP_TRAJ_SELECT_OVERFLOW = 3
 SP_TRAJ_BUDGET_EXHAUSTED = 4
 
 SP_RXN_ZERO, SP_RXN_FIRST, SP_RXN_SECOND, SP_RXN_DIMER, SP_RXN_CUSTOM = 0, 1, 2, 3, 4
+SP_BC_V, SP_BC_NU, SP_BC_RHO, SP_BC_C = 0, 1, 2, 3
 SP_SELECT_EXACT, SP_SELECT_REFERENCE = 0, 1
 SP_PREC_F32, SP_PREC_F64 = 0, 1
 
-ABI_VERSION = 2
+ABI_VERSION = 3
 
 _p = C.POINTER
 
@@ -72,6 +73,16 @@ class SpScenario(C.Structure):
         ("num_consts", C.c_int32),
         ("num_data_fn", C.c_int32),
         ("data_fn", _p(C.c_double)),
+        ("enable_pde", C.c_int32),
+        ("ode_code", _p(C.c_int32)),
+        ("ode_code_off", _p(C.c_int64)),
+        ("ode_consts", _p(C.c_double)),
+        ("num_ode_consts", C.c_int32),
+        ("num_bcs", C.c_int32),
+        ("bc_box", _p(C.c_double)),
+        ("bc_type", _p(C.c_int32)),
+        ("bc_target", _p(C.c_int32)),
+        ("bc_value", _p(C.c_double)),
     ]
 
 
@@ -96,6 +107,7 @@ class SpRunArgs(C.Structure):
         ("want_counts", C.c_int32),
         ("want_moments", C.c_int32),
         ("want_particles", C.c_int32),
+        ("want_chem", C.c_int32),
         ("timeout_s", C.c_double),
     ]
 
@@ -108,6 +120,7 @@ class SpOutputs(C.Structure):
         ("particle_v", _p(C.c_double)),
         ("particle_rho", _p(C.c_double)),
         ("event_counts", _p(C.c_int64)),
+        ("chem", _p(C.c_double)),
     ]
 
 
@@ -194,6 +207,18 @@ def scenario_struct(sc):
     if sc.data_fn is not None:
         s.num_data_fn = sc.data_fn.shape[0]
         s.data_fn = ptr(sc.data_fn, C.c_double)
+    s.enable_pde = int(bool(sc.enable_pde))
+    if sc.ode_code is not None:
+        s.ode_code = ptr(sc.ode_code, C.c_int32)
+        s.ode_code_off = ptr(sc.ode_code_off, C.c_int64)
+        s.ode_consts = ptr(sc.ode_consts, C.c_double)
+        s.num_ode_consts = len(sc.ode_consts)
+    if sc.bc_target is not None and len(sc.bc_target):
+        s.num_bcs = len(sc.bc_target)
+        s.bc_box = ptr(sc.bc_box, C.c_double)
+        s.bc_type = ptr(sc.bc_type, C.c_int32)
+        s.bc_target = ptr(sc.bc_target, C.c_int32)
+        s.bc_value = ptr(sc.bc_value, C.c_double)
     return s
 
 

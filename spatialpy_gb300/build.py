@@ -26,6 +26,7 @@ UNITS = {
     "nsm_batchw.cu": ["-fmad=false"],
     "neighbors.cu": ["-fmad=false"],
     "sdpd.cu": ["-fmad=false"],
+    "chem.cu": ["-fmad=false"],
 }
 
 

@@ -14,6 +14,7 @@
 #include <string>
 #include <vector>
 
+#include "chem.cuh"
 #include "common.cuh"
 #include "neighbors.cuh"
 #include "sdpd.cuh"
@@ -77,6 +78,9 @@ struct Instance {
     uint32_t* u0 = nullptr;   // device copy for the current run
     NsmInstance desc{};
     SdpdState* sdpd = nullptr;
+    // deterministic chemistry (enable_pde)
+    bool pde = false;
+    ChemDev chem{};
 };
 
 }  // namespace
@@ -119,6 +123,11 @@ struct RunState {
     // moving domain with species: one flow (instance cinst) shared by every
     // trajectory, stepped here; particle outputs of that instance
     bool coupled = false, want_part = false;
+    bool chem = false, want_chem = false;   // some instance has enable_pde
+    int chem_step = 0;                      // static domains: chemistry steps taken
+    double* d_chem = nullptr;               // chemistry outputs
+    long long chem_tot = 0;
+    std::vector<long long> chem_off;        // per instance, in doubles
     int cinst = -1, step = 0, max_leaf = 0, max_levels = 0;
     long long poff = 0, ptot = 0;   // offset of cinst / total, in particles x outputs
     double *d_px = nullptr, *d_pv = nullptr, *d_prho = nullptr;
@@ -185,20 +194,21 @@ static int dev_alloc(sp_handle* h, T** dst, size_t n) {
 // operands in range, never underflow, stay within SP_PROG_MAX_STACK values and
 // end at SP_OP_END with one value: then the kernels' interpreter cannot read
 // or write out of bounds.  Returns nullptr, or what is wrong.
-static const char* check_program(const sp_scenario& s, int r) {
-    const int64_t b = s.rxn_code_off[r], e = s.rxn_code_off[r + 1];
-    if (b < 0 || e < b || e > s.rxn_code_off[s.num_reactions]) return "program offsets out of order";
+static const char* check_program_in(const sp_scenario& s, const int32_t* code,
+                                    const int64_t* offs, int num_consts, int r) {
+    const int64_t b = offs[r], e = offs[r + 1];
+    if (b < 0 || e < b || e > offs[s.num_reactions]) return "program offsets out of order";
     if (b == e) return "empty program";
     int d = 0;
     for (int64_t pc = b; pc < e;) {
-        const int op = s.rxn_code[pc];
+        const int op = code[pc];
         const int64_t need = (op == SP_OP_CONST || op == SP_OP_X || op == SP_OP_DATA ||
                               op == SP_OP_POWI) ? 2 : 1;
         if (pc + need > e) return "operand past the end of the program";
-        const int a = need == 2 ? s.rxn_code[pc + 1] : 0;
+        const int a = need == 2 ? code[pc + 1] : 0;
         if (op == SP_OP_END) return d == 1 ? nullptr : "program does not leave one value";
         if (op == SP_OP_CONST) {
-            if (a < 0 || a >= s.num_consts) return "constant index out of range";
+            if (a < 0 || a >= num_consts) return "constant index out of range";
             d++;
         } else if (op == SP_OP_X) {
             if (a < 0 || a >= s.num_species) return "species index out of range";
@@ -223,6 +233,10 @@ static const char* check_program(const sp_scenario& s, int r) {
         pc += need;
     }
     return "program without END";
+}
+
+static const char* check_program(const sp_scenario& s, int r) {
+    return check_program_in(s, s.rxn_code, s.rxn_code_off, s.num_consts, r);
 }
 
 static int validate(sp_handle* h, const sp_scenario& s, int i) {
@@ -277,6 +291,24 @@ static int validate(sp_handle* h, const sp_scenario& s, int i) {
             for (int64_t q = s.jcN[r]; q < s.jcN[r + 1]; q++)
                 REQ(s.irN[q] >= 0 && s.irN[q] < s.num_species, "irN out of range");
         }
+    }
+    if (s.enable_pde && s.num_species > 0) {
+        REQ(s.num_reactions == 0 || (s.ode_code && s.ode_code_off && s.ode_consts),
+            "enable_pde needs the reactions' ODE rate programs");
+        for (int r = 0; r < s.num_reactions; r++) {
+            const char* why = check_program_in(s, s.ode_code, s.ode_code_off, s.num_ode_consts, r);
+            if (why) {
+                snprintf(b, sizeof b, "scenario %d: ODE rate of reaction %d: %s", i, r, why);
+                return fail(h, SP_E_INVALID, b);
+            }
+        }
+    }
+    REQ(s.num_bcs >= 0, "num_bcs must be >= 0");
+    if (s.num_bcs > 0) {
+        REQ(s.bc_box && s.bc_type && s.bc_target && s.bc_value, "boundary condition arrays must be set");
+        for (int q = 0; q < s.num_bcs; q++)
+            REQ(s.bc_target[q] >= SP_BC_V && s.bc_target[q] < SP_BC_C + s.num_species,
+                "boundary condition target out of range");
     }
 #undef REQ
     return SP_OK;
@@ -455,6 +487,58 @@ static int setup_instance(sp_handle* h, const sp_scenario& s, Instance& I) {
     d.data = I.data;
     d.num_data = I.num_data;
     d.has_custom = I.has_custom ? 1 : 0;
+    if (s.enable_pde && S > 0) {
+        ChemDev& D = I.chem;
+        I.pde = true;
+        D.N = N;
+        D.S = S;
+        D.R = R;
+        D.T = T;
+        D.dt = s.dt;
+        D.h = s.h;
+        if ((rc = dev_alloc(h, &D.C, (size_t)N * S))) return rc;
+        if ((rc = dev_alloc(h, &D.Q, (size_t)N * S))) return rc;
+        D.type = I.type;
+        D.diffusion = I.diffusion;
+        D.allowed = I.allowed;
+        D.data = I.data;
+        if (R > 0) {
+            std::vector<int> dense((size_t)S * R, 0), off(R + 1);
+            for (int r = 0; r < R; r++)
+                for (int64_t q = s.jcN[r]; q < s.jcN[r + 1]; q++)
+                    dense[(size_t)s.irN[q] * R + r] += s.prN[q];
+            int* st = nullptr;
+            if ((rc = dev_upload(h, &st, dense.data(), dense.size()))) return rc;
+            D.stoich = st;
+            const int64_t len = s.ode_code_off[R];
+            for (int r = 0; r <= R; r++) off[r] = (int)s.ode_code_off[r];
+            int *code = nullptr, *co = nullptr;
+            double* cs = nullptr;
+            if ((rc = dev_upload(h, &code, s.ode_code, (size_t)len))) return rc;
+            if ((rc = dev_upload(h, &co, off.data(), off.size()))) return rc;
+            const double zero = 0.0;
+            if ((rc = dev_upload(h, &cs, s.num_ode_consts > 0 ? s.ode_consts : &zero,
+                                 (size_t)(s.num_ode_consts > 0 ? s.num_ode_consts : 1))))
+                return rc;
+            D.code = code;
+            D.code_off = co;
+            D.consts = cs;
+        }
+        if (s.num_bcs > 0) {
+            const int nb = s.num_bcs;
+            double *box = nullptr, *val = nullptr;
+            int *ty = nullptr, *tg = nullptr;
+            if ((rc = dev_upload(h, &box, s.bc_box, 6 * (size_t)nb))) return rc;
+            if ((rc = dev_upload(h, &val, s.bc_value, 3 * (size_t)nb))) return rc;
+            if ((rc = dev_upload(h, &ty, s.bc_type, (size_t)nb))) return rc;
+            if ((rc = dev_upload(h, &tg, s.bc_target, (size_t)nb))) return rc;
+            D.nbc = nb;
+            D.bc_box = box;
+            D.bc_value = val;
+            D.bc_type = ty;
+            D.bc_target = tg;
+        }
+    }
     return SP_OK;
 }
 
@@ -749,6 +833,26 @@ int sp_run_start(sp_handle* h, const sp_run_args* a, sp_outputs* out) {
     }
     for (int j = 0; j < ntraj; j++)
         if (!u0ptr[R.inst[j]]) { run_release(h); return fail(h, SP_E_INVALID, "u0 missing for an instance in use"); }
+    // deterministic chemistry: C = u0, Q = 0 for every instance in use with enable_pde
+    {
+        std::vector<char> used(ninst, 0);
+        for (int j = 0; j < ntraj; j++) used[R.inst[j]] = 1;
+        for (int i = 0; i < ninst; i++) {
+            Instance& I = h->inst[i];
+            if (!used[i] || !I.pde) continue;
+            R.chem = true;
+            std::vector<double> c0((size_t)I.N * I.S);
+            std::vector<uint32_t> u(c0.size());
+            if (a->buffers_on_device)
+                cudaMemcpy(u.data(), u0ptr[i], sizeof(uint32_t) * u.size(), cudaMemcpyDeviceToHost);
+            else
+                std::memcpy(u.data(), a->u0[i], sizeof(uint32_t) * u.size());
+            for (size_t e = 0; e < c0.size(); e++) c0[e] = (double)u[e];   // C = u0 (template :77-80)
+            cudaMemcpy(I.chem.C, c0.data(), sizeof(double) * c0.size(), cudaMemcpyHostToDevice);
+            cudaMemsetAsync(I.chem.Q, 0, sizeof(double) * c0.size(), st);
+        }
+    }
+    R.chem_step = 0;
     const uint32_t** d_u0 = nullptr;
     if ((rc = dmalloc((void**)&d_u0, sizeof(void*) * ninst))) return rc;
     cudaMemcpyAsync(d_u0, u0ptr.data(), sizeof(void*) * ninst, cudaMemcpyHostToDevice, st);
@@ -858,6 +962,18 @@ int sp_run_start(sp_handle* h, const sp_run_args* a, sp_outputs* out) {
             if (out->particle_rho && (rc = dmalloc((void**)&R.d_prho, sizeof(double) * R.ptot))) return rc;
         }
     }
+    R.want_chem = R.chem && a->want_chem && out && out->chem;
+    if (R.want_chem) {
+        R.chem_off.assign(ninst, 0);
+        R.chem_tot = 0;
+        for (int i = 0; i < ninst; i++) {
+            R.chem_off[i] = R.chem_tot;
+            R.chem_tot += (long long)nout * h->inst[i].N * h->inst[i].S;
+        }
+        if (a->buffers_on_device) R.d_chem = out->chem;
+        else if ((rc = dmalloc((void**)&R.d_chem, sizeof(double) * R.chem_tot))) return rc;
+        cudaMemsetAsync(R.d_chem, 0, sizeof(double) * R.chem_tot, st);
+    }
     R.step = 0;
     R.next_out = 0;
     R.result = SP_OK;
@@ -865,6 +981,66 @@ int sp_run_start(sp_handle* h, const sp_run_args* a, sp_outputs* out) {
     if (e != cudaSuccess) { run_release(h); return spg_set_cuda_error(h, e, "sp_run_start", __FILE__, __LINE__); }
     // outputs at step 0 need no events
     return sp_run_continue(h, 0);
+}
+
+// Deterministic chemistry of the static-domain instances of the run, steps
+// R.chem_step .. target-1: per step the half step from the previous step's
+// fluxes with the boundary conditions (take_step1, simulate.cpp:81-88), the
+// fluxes from the fixed neighbour lists (model.cpp:151-189, at t = step*dt),
+// and the second half step (take_step2, simulate.cpp:166-171).
+static void chem_steps_static(sp_handle* h, int target) {
+    RunState& R = h->run;
+    if (!R.chem || R.coupled) return;
+    std::vector<char> used(h->inst.size(), 0);
+    for (int j : R.inst) used[j] = 1;
+    for (size_t i = 0; i < h->inst.size(); i++) {
+        Instance& I = h->inst[i];
+        if (!used[i] || !I.pde || !I.is_static) continue;
+        for (int step = R.chem_step; step < target; step++) {
+            chem_launch_half(I.chem, I.x, step == 0, true, h->st);
+            chem_launch_flux_d(I.chem, I.nbr_cnt, I.nbr_idx, I.nbr_dist, I.nbr_dwdr, I.K, I.mass,
+                               I.rho, h->dt * (double)step, h->st);
+            chem_launch_half(I.chem, I.x, false, false, h->st);
+            h->launches += 3;
+        }
+    }
+    if (target > R.chem_step) R.chem_step = target;
+}
+
+// the concentrations of every instance with chemistry into output k
+static void chem_snapshot(sp_handle* h, int k) {
+    RunState& R = h->run;
+    if (!R.want_chem) return;
+    std::vector<char> used(h->inst.size(), 0);
+    for (int j : R.inst) used[j] = 1;
+    for (size_t i = 0; i < h->inst.size(); i++) {
+        const Instance& I = h->inst[i];
+        if (!used[i] || !I.pde) continue;
+        const size_t n = (size_t)I.N * I.S;
+        cudaMemcpyAsync(R.d_chem + R.chem_off[i] + (size_t)k * n, I.chem.C, sizeof(double) * n,
+                        cudaMemcpyDeviceToDevice, h->st);
+    }
+}
+
+// one flow step with the chemistry interleaved as the reference's substeps
+static void flow_chem_step(sp_handle* h, Instance& I) {
+    const SdpdLists L = sdpd_lists(I.sdpd);
+    const int step = L.step;
+    sdpd_enqueue_phase(I.sdpd, 0);
+    if (L.f64) chem_launch_half4d(I.chem, (const double*)L.pos, step == 0, true, h->st);
+    else chem_launch_half4f(I.chem, (const float*)L.pos, step == 0, true, h->st);
+    sdpd_enqueue_phase(I.sdpd, 1);
+    if (L.f64)
+        chem_launch_flux_d(I.chem, L.count, L.idx, (const double*)L.dist, (const double*)L.dwdr,
+                           L.kcap, (const double*)L.mass, (const double*)L.rho,
+                           h->dt * (double)step, h->st);
+    else
+        chem_launch_flux_f(I.chem, L.count, L.idx, (const float*)L.dist, (const float*)L.dwdr,
+                           L.kcap, (const float*)L.mass, (const float*)L.rho,
+                           h->dt * (double)step, h->st);
+    sdpd_enqueue_phase(I.sdpd, 2);
+    if (L.f64) chem_launch_half4d(I.chem, (const double*)L.pos, false, false, h->st);
+    else chem_launch_half4f(I.chem, (const float*)L.pos, false, false, h->st);
 }
 
 // Moving domain with species, steps R.step .. target-1 (simulate_threads.cpp:
@@ -880,7 +1056,8 @@ static int coupled_steps(sp_handle* h, int target, bool ref, long long budget, l
     const int ntraj = R.args.num_trajectories;
     cudaEventRecord(h->ea, st);
     while (R.step < target) {
-        sdpd_enqueue_step(I.sdpd);
+        if (I.pde) flow_chem_step(h, I);
+        else sdpd_enqueue_step(I.sdpd);
         const SdpdLists L = sdpd_lists(I.sdpd);
         if (L.f64)
             launch_diffusion_tables(I.N, I.S, I.T, I.K, I.type, L.count, L.idx,
@@ -1002,6 +1179,8 @@ int sp_run_continue(sp_handle* h, int32_t num_outputs) {
             done++;
         }
         if (R.result != SP_OK) break;
+        chem_steps_static(h, target);
+        chem_snapshot(h, R.next_out);
         if (R.want_counts || R.want_mom) {
             launch_nsm_snapshot(h->d_trajs, h->d_insts, ntraj, R.want_counts ? R.d_counts : nullptr,
                                 R.d_coff, R.want_mom ? R.d_mom : nullptr, R.d_moff, R.next_out, st);
@@ -1050,6 +1229,9 @@ int sp_run_finish(sp_handle* h) {
             cudaMemcpyAsync(R.out.counts, R.d_counts, sizeof(int32_t) * R.ctot, cudaMemcpyDeviceToHost, st);
         if (R.want_mom)
             cudaMemcpyAsync(R.out.moments, R.d_mom, sizeof(long long) * 2 * R.mtot, cudaMemcpyDeviceToHost, st);
+        if (R.want_chem)
+            cudaMemcpyAsync(R.out.chem, R.d_chem, sizeof(double) * R.chem_tot,
+                            cudaMemcpyDeviceToHost, st);
         if (R.want_part) {
             const long long n = (long long)h->output_steps.size() * h->inst[R.cinst].N;
             if (R.d_px)

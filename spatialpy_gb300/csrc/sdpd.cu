@@ -62,7 +62,41 @@ struct SdpdDev {
     int kcap;
     CellGrid g;
     int* flag;   // bit 1: list overflow, bit 2: NaN state, bit 4: cell overflow
+    // boundary conditions on v, nu, rho (boundarycondition.py:121-167)
+    const int* type;
+    int nbc;
+    const double* bc_box;
+    const int* bc_type;
+    const int* bc_target;
+    const double* bc_value;
 };
+
+// The boundary conditions that target v, nu or rho, in order: a particle
+// inside the condition's box (and of its type) takes the value
+// (applyBoundaryConditions, called after the predictor and after the
+// corrector, simulate.cpp:88, 171).  Concentration targets are chem.cu's.
+template <typename R, typename V>
+__device__ __forceinline__ void flow_bcs(const SdpdDev<R>& D, int i, const V& p, V& v, R& rho) {
+    for (int b = 0; b < D.nbc; b++) {
+        const int tg = D.bc_target[b];
+        if (tg >= SP_BC_C) continue;
+        const double* bx = D.bc_box + 6 * b;
+        const double px = (double)p.x, py = (double)p.y, pz = (double)p.z;
+        if (!(px >= bx[0] && px <= bx[1] && py >= bx[2] && py <= bx[3] && pz >= bx[4] &&
+              pz <= bx[5] && (D.bc_type[b] == 0 || D.bc_type[b] == D.type[i])))
+            continue;
+        const double* val = D.bc_value + 3 * b;
+        if (tg == SP_BC_V) {
+            v.x = (R)val[0];
+            v.y = (R)val[1];
+            v.z = (R)val[2];
+        } else if (tg == SP_BC_NU) {
+            D.nu[i] = (R)val[0];
+        } else {
+            rho = (R)val[0];
+        }
+    }
+}
 
 constexpr int kCellCap = 16;
 
@@ -115,6 +149,11 @@ __global__ void sdpd_begin(SdpdDev<R> D) {
         D.vel[i] = v;
         D.vt[i] = t;
         D.pos[i] = p;
+        D.rho[i] = rho;
+    }
+    if (D.nbc) {
+        flow_bcs(D, i, p, v, rho);
+        D.vel[i] = v;
         D.rho[i] = rho;
     }
     auto F = D.F[i];
@@ -345,6 +384,7 @@ __global__ void sdpd_corrector(SdpdDev<R> D) {
             if (D.dim > 2) v.z = -v.z + (R)2.0 * mx * n2;
         }
     }
+    if (D.nbc) flow_bcs(D, i, D.pos[i], v, rho);   // applyBoundaryConditions, simulate.cpp:171
     D.vel[i] = v;
     D.rho[i] = rho;
 }
@@ -366,7 +406,11 @@ struct SdpdState {
     int *ccnt = nullptr, *cidx = nullptr, *ncnt = nullptr, *nidx = nullptr, *flag = nullptr;
     void* ndij = nullptr;
     // initial state (REAL-typed 4-vectors and densities) for sdpd_reset
-    std::vector<unsigned char> init_pos, init_vel, init_rho;
+    std::vector<unsigned char> init_pos, init_vel, init_rho, init_nu;
+    int* type = nullptr;
+    int nbc = 0;
+    double *bc_box = nullptr, *bc_value = nullptr;
+    int *bc_type = nullptr, *bc_target = nullptr;
     CellGrid grid{};
     cudaGraphExec_t graph20 = nullptr;   // 20 steps starting at a multiple of 20 (>= 20)
 };
@@ -406,6 +450,12 @@ static SdpdDev<R> dev_view(SdpdState* s) {
     D.ccnt = s->ccnt; D.cidx = s->cidx;
     D.ncnt = s->ncnt; D.nidx = s->nidx; D.ndist = (R*)s->ndist; D.ndw = (R*)s->ndw;
     D.ndij = (R*)s->ndij;
+    D.type = s->type;
+    D.nbc = s->nbc;
+    D.bc_box = s->bc_box;
+    D.bc_type = s->bc_type;
+    D.bc_target = s->bc_target;
+    D.bc_value = s->bc_value;
     D.kcap = s->kcap;
     D.g = s->grid;
     D.flag = s->flag;
@@ -439,6 +489,7 @@ static bool upload(SdpdState* s, const sp_scenario& sc, std::string* err) {
     s->init_pos.assign((unsigned char*)pos.data(), (unsigned char*)pos.data() + v4);
     s->init_vel.assign((unsigned char*)vel.data(), (unsigned char*)vel.data() + v4);
     s->init_rho.assign((unsigned char*)rho.data(), (unsigned char*)rho.data() + r1);
+    s->init_nu.assign((unsigned char*)nu.data(), (unsigned char*)nu.data() + r1);
     // F, Fbp, vt start at zero: the engine reads them before first writing
     // them (particle.cpp:70-83), the oracle zero-initialises them
     cudaMemcpyAsync(s->pos, pos.data(), v4, cudaMemcpyHostToDevice, s->st);
@@ -484,12 +535,28 @@ SdpdState* sdpd_create(const sp_scenario& sc, int precision, cudaStream_t st, st
     s->grid.ncell = s->grid.nc[0] * s->grid.nc[1] * s->grid.nc[2];
     const int N = s->N;
     bool ok = sd_alloc(s, (void**)&s->fixed, N, err) &&
+              sd_alloc(s, (void**)&s->type, sizeof(int) * N, err) &&
               sd_alloc(s, (void**)&s->ccnt, sizeof(int) * s->grid.ncell, err) &&
               sd_alloc(s, (void**)&s->cidx, sizeof(int) * (size_t)s->grid.ncell * kCellCap, err) &&
               sd_alloc(s, (void**)&s->ncnt, sizeof(int) * N, err) &&
               sd_alloc(s, (void**)&s->nidx, sizeof(int) * (size_t)N * s->kcap, err) &&
               sd_alloc(s, (void**)&s->flag, sizeof(int), err);
+    if (ok && sc.num_bcs > 0) {
+        const int nb = sc.num_bcs;
+        s->nbc = nb;
+        ok = sd_alloc(s, (void**)&s->bc_box, sizeof(double) * 6 * nb, err) &&
+             sd_alloc(s, (void**)&s->bc_value, sizeof(double) * 3 * nb, err) &&
+             sd_alloc(s, (void**)&s->bc_type, sizeof(int) * nb, err) &&
+             sd_alloc(s, (void**)&s->bc_target, sizeof(int) * nb, err);
+        if (ok) {
+            cudaMemcpyAsync(s->bc_box, sc.bc_box, sizeof(double) * 6 * nb, cudaMemcpyHostToDevice, st);
+            cudaMemcpyAsync(s->bc_value, sc.bc_value, sizeof(double) * 3 * nb, cudaMemcpyHostToDevice, st);
+            cudaMemcpyAsync(s->bc_type, sc.bc_type, sizeof(int) * nb, cudaMemcpyHostToDevice, st);
+            cudaMemcpyAsync(s->bc_target, sc.bc_target, sizeof(int) * nb, cudaMemcpyHostToDevice, st);
+        }
+    }
     if (ok) {
+        cudaMemcpyAsync(s->type, sc.type, sizeof(int) * N, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(s->fixed, sc.fixed, N, cudaMemcpyHostToDevice, st);
         cudaMemsetAsync(s->ncnt, 0, sizeof(int) * N, st);
         ok = s->prec == SP_PREC_F64 ? upload<double>(s, sc, err) : upload<float>(s, sc, err);
@@ -668,6 +735,7 @@ int sdpd_reset(SdpdState* s, std::string* err) {
     cudaMemsetAsync(s->Fbp, 0, v4, s->st);
     cudaMemcpyAsync(s->rho, s->init_rho.data(), r1, cudaMemcpyHostToDevice, s->st);
     cudaMemcpyAsync(s->orho, s->init_rho.data(), r1, cudaMemcpyHostToDevice, s->st);
+    cudaMemcpyAsync(s->nu, s->init_nu.data(), r1, cudaMemcpyHostToDevice, s->st);
     cudaMemsetAsync(s->ncnt, 0, sizeof(int) * s->N, s->st);
     cudaMemsetAsync(s->flag, 0, sizeof(int), s->st);
     cudaError_t e = cudaStreamSynchronize(s->st);   // host staging buffers stay valid
@@ -685,12 +753,38 @@ void sdpd_enqueue_step(SdpdState* s) {
     s->step++;
 }
 
+template <typename R>
+static void enqueue_phase_t(SdpdState* s, int phase) {
+    const int N = s->N, tb = 128, nb = (N + tb - 1) / tb;
+    SdpdDev<R> D = dev_view<R>(s);
+    D.step = s->step;
+    if (phase == 0) {
+        cudaMemsetAsync(s->ccnt, 0, sizeof(int) * s->grid.ncell, s->st);
+        sdpd_begin<R><<<nb, tb, 0, s->st>>>(D);
+    } else if (phase == 1) {
+        constexpr int TP = sizeof(R) == 4 ? 128 : 64;
+        sdpd_pairs<R, 48, TP><<<(N + TP - 1) / TP, TP, 0, s->st>>>(D, s->step == 0 ? 1 : 0);
+    } else {
+        sdpd_corrector<R><<<nb, tb, 0, s->st>>>(D);
+        s->step++;
+    }
+}
+
+void sdpd_enqueue_phase(SdpdState* s, int phase) {
+    if (s->prec == SP_PREC_F64) enqueue_phase_t<double>(s, phase);
+    else enqueue_phase_t<float>(s, phase);
+}
+
 SdpdLists sdpd_lists(SdpdState* s) {
     SdpdLists L;
     L.count = s->ncnt;
     L.idx = s->nidx;
     L.dij = s->ndij;
     L.rho = s->rho;
+    L.dist = s->ndist;
+    L.dwdr = s->ndw;
+    L.mass = s->mass;
+    L.pos = s->pos;
     L.kcap = s->kcap;
     L.f64 = s->prec == SP_PREC_F64;
     L.step = s->step;

@@ -27,6 +27,10 @@ struct SdpdLists {
     int* idx;        // [N][kcap]
     void* dij;       // [N][kcap] REAL (float, or double when f64)
     void* rho;       // [N] REAL
+    void* dist;      // [N][kcap] REAL
+    void* dwdr;      // [N][kcap] REAL
+    void* mass;      // [N] REAL
+    void* pos;       // [N] 4-vectors of REAL
     int kcap;
     bool f64;
     int step;        // steps taken
@@ -34,6 +38,9 @@ struct SdpdLists {
 int sdpd_enable_dij(SdpdState* s, std::string* err);            // lists carry D_ij from now on
 int sdpd_reset(SdpdState* s, std::string* err);                 // back to the initial state, step 0
 void sdpd_enqueue_step(SdpdState* s);                           // one step, no host sync
+// one step in three parts: 0 predictor (take_step1), 1 lists + forces,
+// 2 corrector (take_step2; advances the step counter)
+void sdpd_enqueue_phase(SdpdState* s, int phase);
 SdpdLists sdpd_lists(SdpdState* s);
 // vol = m / rho, 1/vol = rho / m from the current densities (float)
 void sdpd_launch_volumes(SdpdState* s, const double* mass, float* vol, float* ivol);

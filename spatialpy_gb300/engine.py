@@ -88,7 +88,7 @@ class Engine:
 
     # -- runs ----------------------------------------------------------------
     def _prepare(self, seeds, instance, selection, want_counts, want_moments, u0, timeout,
-                 want_particles=False):
+                 want_particles=False, want_chem=False):
         seeds = np.ascontiguousarray(seeds, dtype=np.uint64).reshape(-1)
         nt = seeds.shape[0]
         inst = None
@@ -130,6 +130,11 @@ class Engine:
         pv = np.zeros(3 * np_tot)
         prho = np.zeros(np_tot)
         args.want_particles = int(want_particles)
+        csizes = [T[i] * sc.num_particles * sc.num_species for i, sc in enumerate(self.scenarios)]
+        chem = np.zeros(int(sum(csizes)) if want_chem else 0)
+        args.want_chem = int(want_chem)
+        if want_chem:
+            out.chem = ptr(chem, C.c_double)
         if want_particles:
             out.particle_x = ptr(px, C.c_double)
             out.particle_v = ptr(pv, C.c_double)
@@ -138,7 +143,8 @@ class Engine:
         self._run = dict(seeds=seeds, inst=inst, u0s=u0s, u0p=u0p, args=args, out=out, T=T,
                          idx=idx, sizes=sizes, counts=counts, msizes=msizes, moments=moments,
                          events=events, want_counts=want_counts, want_moments=want_moments,
-                         want_particles=want_particles, psizes=psizes, px=px, pv=pv, prho=prho)
+                         want_particles=want_particles, psizes=psizes, px=px, pv=pv, prho=prho,
+                         want_chem=want_chem, csizes=csizes, chem=chem)
         return self._run
 
     def _collect(self, rc):
@@ -176,11 +182,19 @@ class Engine:
                 rs.append(r["prho"][o:o + n].reshape(T[i], sc.num_particles))
                 o += n
             res["particles"] = list(zip(xs, vs, rs))
+        if r["want_chem"]:
+            parts, o = [], 0
+            for i, sc in enumerate(self.scenarios):
+                n = r["csizes"][i]
+                parts.append(r["chem"][o:o + n].reshape(T[i], sc.num_particles, sc.num_species))
+                o += n
+            res["chem"] = parts
         return res
 
     def run(self, seeds, instance=None, selection: int = abi.SP_SELECT_EXACT,
             want_counts: bool = True, want_moments: bool = False, u0=None,
-            timeout: float | None = None, want_particles: bool = False):
+            timeout: float | None = None, want_particles: bool = False,
+            want_chem: bool = False):
         """Run one trajectory per seed over the whole time span.
 
         Returns a dict with ``counts`` (list per trajectory of [T,N,S] int32
@@ -189,10 +203,11 @@ class Engine:
         ([ntraj,2] reaction/diffusion counts) and ``status`` codes.  On a
         moving domain every trajectory shares the flow; ``want_particles``
         adds ``particles`` (per instance: positions [T,N,3], velocities
-        [T,N,3], densities [T,N] at the outputs).
+        [T,N,3], densities [T,N] at the outputs); ``want_chem`` adds
+        ``chem`` (per instance with enable_pde: concentrations [T,N,S]).
         """
         r = self._prepare(seeds, instance, selection, want_counts, want_moments, u0, timeout,
-                          want_particles)
+                          want_particles, want_chem)
         rc = self.lib.sp_run(self._h, C.byref(r["args"]), C.byref(r["out"]))
         return self._collect(rc)
 

@@ -247,6 +247,24 @@ def _powi(a: float, n: int) -> float:
     return 1.0 / r if n < 0 else r
 
 
+def mass_action_ode(k: float, reactants: list, consts: list) -> list:
+    """The deterministic rate of a mass-action reaction (reaction.py:283-300):
+    ``k * A * B`` or ``k * A * A``, left to right; reactants: (species
+    index, stoichiometry) pairs."""
+    code = []
+    v = float(k)
+    if v in consts:
+        code.extend([CONST, consts.index(v)])
+    else:
+        consts.append(v)
+        code.extend([CONST, len(consts) - 1])
+    for s, n in reactants:
+        for _ in range(n):
+            code.extend([X, s, MUL])
+    code.append(END)
+    return code
+
+
 def pack(programs: list):
     """Concatenate per-reaction programs: (code int32, offsets int64 [R+1])."""
     off = [0]

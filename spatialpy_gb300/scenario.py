@@ -56,6 +56,14 @@ class Scenario:
     rxn_code_off: np.ndarray | None = None  # [R+1] int64
     rxn_consts: np.ndarray | None = None    # float64
     data_fn: np.ndarray | None = None       # [num_data_fn, N] float64
+    enable_pde: bool = False                # deterministic concentrations C
+    ode_code: np.ndarray | None = None      # ODE propensity programs, one per reaction
+    ode_code_off: np.ndarray | None = None
+    ode_consts: np.ndarray | None = None
+    bc_box: np.ndarray | None = None        # [nbc, 6] xmin xmax ymin ymax zmin zmax
+    bc_type: np.ndarray | None = None       # [nbc] int32, 0 = any
+    bc_target: np.ndarray | None = None     # [nbc] int32 SP_BC_*
+    bc_value: np.ndarray | None = None      # [nbc, 3]
 
     def __post_init__(self):
         self.x = np.ascontiguousarray(self.x, dtype=np.float64).reshape(-1, 3)
@@ -92,6 +100,18 @@ class Scenario:
                 self.rxn_consts = np.zeros(1)
         if self.data_fn is not None:
             self.data_fn = np.ascontiguousarray(self.data_fn, dtype=np.float64).reshape(-1, n)
+        if self.ode_code is not None:
+            self.ode_code = np.ascontiguousarray(self.ode_code, dtype=np.int32)
+            self.ode_code_off = np.ascontiguousarray(self.ode_code_off, dtype=np.int64)
+            self.ode_consts = np.ascontiguousarray(self.ode_consts, dtype=np.float64)
+            if self.ode_consts.size == 0:
+                self.ode_consts = np.zeros(1)
+        if self.bc_target is not None:
+            nb = len(self.bc_target)
+            self.bc_target = np.ascontiguousarray(self.bc_target, dtype=np.int32)
+            self.bc_type = np.ascontiguousarray(self.bc_type, dtype=np.int32).reshape(nb)
+            self.bc_box = np.ascontiguousarray(self.bc_box, dtype=np.float64).reshape(nb, 6)
+            self.bc_value = np.ascontiguousarray(self.bc_value, dtype=np.float64).reshape(nb, 3)
 
     @property
     def num_particles(self) -> int:
@@ -145,15 +165,23 @@ def mass_action(species: list, reactions: list, num_types: int, params: dict | N
     restricted = False
     dense = np.zeros((S, R), np.int64)
     progs, consts = [None] * R, []
-    for r, (k, reactants, products, types) in enumerate(reactions):
+    oprogs, oconsts = [None] * R, []
+    for r, entry in enumerate(reactions):
+        k, reactants, products, types = entry[:4]
         order = sum(reactants.values())
         if isinstance(k, str):
             kind[r] = SP_RXN_CUSTOM
             progs[r] = prop.compile_expression(k, species, params or {}, consts, data_names)
+            ode = entry[4] if len(entry) > 4 and entry[4] else k
+            oprogs[r] = prop.compile_expression(ode, species, params or {}, oconsts, data_names)
         elif order > 2:
             raise ValueError("mass-action reactions are at most second order")
         else:
             rate[r] = float(k)
+            # the ODE form of a mass-action propensity: k times each reactant
+            # (reaction.py:283-300), no volume factor
+            oprogs[r] = prop.mass_action_ode(float(k), [(idx[sp], n) for sp, n in
+                                                        reactants.items()], oconsts)
         if kind[r] == SP_RXN_CUSTOM:
             pass
         elif order == 0:
@@ -187,6 +215,9 @@ def mass_action(species: list, reactions: list, num_types: int, params: dict | N
         jcN.append(len(irN))
     if programs is not None:
         programs.update(custom_fields(progs, consts))
+        ocode, ooff = prop.pack(oprogs)
+        programs.update({"ode_code": ocode, "ode_code_off": ooff,
+                         "ode_consts": np.array(oconsts if oconsts else [0.0], np.float64)})
     return (rate, kind, reac, allowed if restricted else None,
             np.array(jcN, np.int64), np.array(irN, np.int64), np.array(prN, np.int32))
 
@@ -421,7 +452,8 @@ def from_model(model, h: float | None = None) -> Scenario:
                          for t in r.restrict_to]
             reactants = {s.name if hasattr(s, "name") else s: n for s, n in r.reactants.items()}
             products = {s.name if hasattr(s, "name") else s: n for s, n in r.products.items()}
-            rxns.append((str(r.propensity_function), reactants, products, types))
+            rxns.append((str(r.propensity_function), reactants, products, types,
+                         str(r.ode_propensity_function or r.propensity_function)))
             continue
         k = r.marate
         if hasattr(k, "value"):
@@ -440,6 +472,26 @@ def from_model(model, h: float | None = None) -> Scenario:
                                                                data_names, programs)
     except prop.PropensityError as err:
         raise NotImplementedError(str(err)) from err
+    # boundary conditions (boundarycondition.py:121-167)
+    bcs = {}
+    blist = list(getattr(model, "listOfBoundaryConditions", []))
+    if blist:
+        box, btype, btarget, bval = [], [], [], []
+        for bc in blist:
+            lim = [bc.xmin, bc.xmax, bc.ymin, bc.ymax, bc.zmin, bc.zmax]
+            box.append([(-np.inf if q % 2 == 0 else np.inf) if v is None else float(v)
+                        for q, v in enumerate(lim)])
+            tid = bc.type_id
+            btype.append(0 if tid is None else tmap[tid if str(tid).startswith("type_")
+                                                    else f"type_{tid}"])
+            tg = bc.target.name if hasattr(bc.target, "name") else bc.target
+            if tg in species:
+                btarget.append(3 + species.index(tg))
+            else:
+                btarget.append({"v": 0, "nu": 1, "rho": 2}[tg])
+            val = bc.value
+            bval.append(list(val) if isinstance(val, (list, tuple)) else [float(val), 0.0, 0.0])
+        bcs = {"bc_box": box, "bc_type": btype, "bc_target": btarget, "bc_value": bval}
     data_fn = None
     if data_names:
         coords = np.asarray(dom.coordinates(), np.float64)
@@ -476,4 +528,5 @@ def from_model(model, h: float | None = None) -> Scenario:
                     static_domain=bool(model.staticDomain), rho0=float(dom.rho0),
                     c0=float(dom.c0), P0=float(dom.P0),
                     gravity=tuple(dom.gravity) if dom.gravity is not None else (0.0, 0.0, 0.0),
-                    u0=u0, name=model.name, data_fn=data_fn, **programs)
+                    u0=u0, name=model.name, data_fn=data_fn,
+                    enable_pde=bool(getattr(model, "enable_pde", False)), **programs, **bcs)

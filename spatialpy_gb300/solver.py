@@ -47,7 +47,7 @@ class GpuResult(_RefResult):
     """One trajectory held in memory; ``read_step`` returns what the
     reference reads from ``outputN.vtk`` (result.py:270-321)."""
 
-    def __init__(self, model, scenario, counts, times, particles=None):
+    def __init__(self, model, scenario, counts, times, particles=None, chem=None):
         self.model = model
         self.tspan = None
         self.success = True
@@ -61,6 +61,7 @@ class GpuResult(_RefResult):
         self.counts = counts                      # [T, N, S] int32
         self.times = np.asarray(times, np.float64)
         self.particles = particles                # optional (x [T,N,3], v [T,N,3], rho [T,N])
+        self.chem = chem                          # optional [T,N,S] deterministic concentrations
 
     # -- ensemble container (result.py:161-171)
     def __len__(self):
@@ -100,6 +101,8 @@ class GpuResult(_RefResult):
         data = {"id": np.arange(n), "type": sc.type.copy(), "v": v, "rho": rho,
                 "mass": sc.mass.copy(), "bvf_phi": np.zeros(n), "nu": sc.nu.copy()}
         for s, name in enumerate(sc.species):
+            if self.chem is not None:
+                data[f"C[{name}]"] = self.chem[step_num][:, s].copy()
             data[f"D[{name}]"] = self.counts[step_num][:, s].astype(np.float64)
         return x, data
 
@@ -115,7 +118,12 @@ class GpuResult(_RefResult):
             return super().get_species(species, timepoints, concentration, deterministic, debug)
         name = species if isinstance(species, str) else species.name
         s = self.scenario.species.index(name)
-        out = self.counts[:, :, s].astype(np.float64)
+        if deterministic:
+            if self.chem is None:
+                raise ValueError("deterministic concentrations need a model with enable_pde")
+            out = self.chem[:, :, s].copy()
+        else:
+            out = self.counts[:, :, s].astype(np.float64)
         if concentration:
             out = out / self.scenario.vol
         if timepoints is not None:
@@ -131,7 +139,7 @@ class GpuResult(_RefResult):
         else:
             x, v, rho = sc.x, None, sc.rho
         return write_outputs(directory, x, sc.type, sc.mass, rho, sc.nu, sc.species,
-                             self.counts, v=v)
+                             self.counts, v=v, chem=self.chem)
 
 
 class GpuSolver(_RefSolver):
@@ -193,14 +201,15 @@ class GpuSolver(_RefSolver):
             return self._run_flow(seeds, times, timeout)
         try:
             res = self.engine.run(seeds, selection=self.selection, want_counts=True,
-                                  timeout=timeout)
+                                  timeout=timeout, want_chem=bool(sc.enable_pde))
         except EngineError as err:
             raise SimulationError(f"Solver execution failed: {err}") from err
         if res["rc"] == abi.SP_E_TRAJECTORY:
             raise SimulationError(f"Solver execution failed: {res.get('error')}")
+        chem = res["chem"][0] if sc.enable_pde else None
         first = None
         for j in range(number_of_trajectories):
-            r = GpuResult(self.model, sc, res["counts"][j], times)
+            r = GpuResult(self.model, sc, res["counts"][j], times, chem=chem)
             r.timeout = res["rc"] == abi.SP_E_TIMEOUT
             if first is None:
                 first = r
@@ -216,15 +225,18 @@ class GpuSolver(_RefSolver):
         if sc.num_species > 0 and sc.u0 is not None:
             try:
                 res = self.engine.run(seeds, selection=self.selection, want_counts=True,
-                                      timeout=timeout, want_particles=True)
+                                      timeout=timeout, want_particles=True,
+                                      want_chem=bool(sc.enable_pde))
             except EngineError as err:
                 raise SimulationError(f"Solver execution failed: {err}") from err
             if res["rc"] not in (abi.SP_OK, abi.SP_E_TIMEOUT):
                 raise SimulationError(f"Solver execution failed: {res.get('error')}")
             particles = res["particles"][0]
+            chem = res["chem"][0] if sc.enable_pde else None
             first = None
             for j in range(len(seeds)):
-                r = GpuResult(self.model, sc, res["counts"][j], times, particles=particles)
+                r = GpuResult(self.model, sc, res["counts"][j], times, particles=particles,
+                              chem=chem)
                 r.timeout = res["rc"] == abi.SP_E_TIMEOUT
                 if first is None:
                     first = r

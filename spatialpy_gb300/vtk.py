@@ -36,15 +36,17 @@ def _vec_rows(arr, fmt):
     return "".join(out)
 
 
-def format_step(points, types, v, rho, mass, bvf_phi, nu, species, counts, index):
-    """One output file as text.  counts: [N, S] copy numbers."""
+def format_step(points, types, v, rho, mass, bvf_phi, nu, species, counts, index, chem=None):
+    """One output file as text.  counts: [N, S] copy numbers; chem: [N, S]
+    deterministic concentrations or None (output.cpp writes them as C[s])."""
     n = points.shape[0]
     parts = ["# vtk DataFile Version 4.1\n", "Generated by SpatialPy\n", "ASCII\n",
              "DATASET POLYDATA\n", f"POINTS {n} float\n",
              _vec_rows(points, "%.10e"), "\n",
              f"VERTICES {n} {2 * n}\n", "".join(f"1 {i}\n" for i in range(n)), "\n",
              f"POINT_DATA {n}\n"]
-    nfields = 7 + (len(species) if index > 0 else 0)
+    nc = len(species) if chem is not None else 0
+    nfields = 7 + nc + (len(species) if index > 0 else 0)
     parts.append(f"FIELD FieldData {nfields}\n")
     parts += [f"id 1 {n} int\n", _rows(range(n), 9, "%u "), "\n"]
     parts += [f"type 1 {n} int\n", _rows(types, 9, "%u "), "\n"]
@@ -53,13 +55,16 @@ def format_step(points, types, v, rho, mass, bvf_phi, nu, species, counts, index
     parts += [f"mass 1 {n} double\n", _rows(mass, 9, "%f "), "\n"]
     parts += [f"bvf_phi 1 {n} double\n", _rows(bvf_phi, 9, "%f "), "\n"]
     parts += [f"nu 1 {n} double\n", _rows(nu, 9, "%f "), "\n"]
+    if chem is not None:
+        for s, name in enumerate(species):
+            parts += [f"C[{name}] 1 {n} double\n", _rows(chem[:, s], 9, "%f "), "\n"]
     for s, name in enumerate(species):
         parts += [f"D[{name}] 1 {n} int\n", _rows(counts[:, s], 9, "%u "), "\n"]
     return "".join(parts)
 
 
 def write_outputs(directory, points, types, mass, rho, nu, species, counts, v=None,
-                  bvf_phi=None, bbox=None):
+                  bvf_phi=None, bbox=None, chem=None):
     """Write output0.vtk ... output{T-1}.vtk (and output0_boundingBox.vtk
     when ``bbox`` = (xlo, xhi, ylo, yhi, zlo, zhi) is given).
 
@@ -84,7 +89,8 @@ def write_outputs(directory, points, types, mass, rho, nu, species, counts, v=No
         pk = points[k] if points.ndim == 3 else points
         vk = v[k] if v.ndim == 3 else v
         rk = rho[k] if rho.ndim == 2 else rho
-        text = format_step(pk, types, vk, rk, mass, bvf_phi, nu, species, counts[k], k)
+        text = format_step(pk, types, vk, rk, mass, bvf_phi, nu, species, counts[k], k,
+                           None if chem is None else chem[k])
         path = os.path.join(directory, f"output{k}.vtk")
         with open(path, "w") as f:
             f.write(text)

@@ -184,3 +184,26 @@ def test_coupled_oracle_flow_and_species(oracle_lib):
     out2, ev2, _, _, _ = oracle_lib.coupled_ensemble(sc, seeds)
     np.testing.assert_array_equal(out, out2)
     np.testing.assert_array_equal(ev, ev2)
+
+
+def test_chem_oracle_conserves_and_integrates(oracle_lib):
+    """Deterministic chemistry (model.cpp:151-189): SPH diffusion alone keeps
+    the total of C; a zero-order ODE rate k adds k*dt per step to every
+    particle of its type; a boundary condition pins its concentrations.""" 
+    from .chem_cases import static_chem
+    sc = static_chem(reactions="none", bcs=False)
+    out = oracle_lib.chem_static(sc)
+    tot = out.sum(axis=1)
+    np.testing.assert_allclose(tot, np.broadcast_to(tot[0], tot.shape), rtol=1e-12)
+    assert np.abs(out[-1] - out[0]).max() > 0.1           # it diffused
+    sc2 = static_chem(reactions="birth")
+    sc2 = sc2.copy(u0=np.zeros_like(sc2.u0))
+    out2 = oracle_lib.chem_static(sc2)
+    n1 = int((sc2.type == 1).sum())
+    steps = sc2.output_steps
+    # the first half step of step 0 has no fluxes yet (simulate.cpp:81), so
+    # the total lags k*N1*t by half a step
+    want = np.where(steps > 0, 3.0 * n1 * (sc2.dt * steps - 0.5 * sc2.dt), 0.0)
+    np.testing.assert_allclose(out2[:, :, 0].sum(axis=1), want, rtol=1e-9)
+    top = sc2.x[:, 1] > 0.8
+    assert np.all(out2[1:, top, 1] == 4.0)
