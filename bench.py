@@ -326,6 +326,39 @@ def run_uneven(args):
                        "host_setup_s": round(build_s, 1)}}
 
 
+def run_surrogate(args):
+    """Surrogate + SSA fallback against the plain GPU SSA over a held-out
+    parameter sweep (reduced sizes: 2-D 32 x 32 lattice, t in [0, 4] with 8
+    output times, 32 trajectories per point, 256 training and 64 held-out
+    points).  Errors are relative L2 of the ensemble mean and variance
+    fields coarse-grained to whole-domain species totals per output time,
+    next to the same metric between two independent SSA ensembles (the
+    noise floor of the reference answer)."""
+    from spatialpy_gb300 import surrogate as SG
+    cfg = SG.SweepConfig(n=32, molecules=1000, t_end=4.0, num_times=8, trajectories=32)
+    rng = np.random.default_rng(7)
+    tp, hp = SG.sample_parameters(256, rng), SG.sample_parameters(64, rng)
+    tm, tv, train_s = SG.ssa_moments(tp, cfg, 10)
+    hm, hv, ssa_s = SG.ssa_moments(hp, cfg, 10 ** 6)
+    hm2, hv2, _ = SG.ssa_moments(hp, cfg, 2 * 10 ** 6)
+    sur = SG.Surrogate(cfg, width=32, modes=12, layers=4)
+    t0 = time.perf_counter()
+    loss = sur.fit(tp, tm, tv, epochs=300)
+    fit_s = time.perf_counter() - t0
+    out = {"metric": "sweep seconds (surrogate + SSA fallback vs plain GPU SSA)",
+           "config": {"workload": "2-D 32x32 RDME sweep, 5 parameters log-uniform +-1 decade, "
+                                  "64 held-out points x 32 trajectories, 8 output times",
+                      "train_points": 256, "fno": "4 layers, width 32, 12 modes, FiLM, bf16"},
+           "ssa_train_s": train_s, "fit_s": fit_s, "train_loss": loss}
+    for name, block in (("totals", cfg.n), ("blocks8", 8)):
+        summ = SG.sweep(sur, hp, hm, hv, ssa_s, threshold=0.02, block=block)
+        summ["ssa_noise_mean"] = float(np.median(SG.rel_error(hm2, hm, cfg.n, block)))
+        summ["ssa_noise_var"] = float(np.median(SG.rel_error(hv2, hv, cfg.n, block)))
+        out[name] = {k: float(v) if isinstance(v, (np.floating, float)) else v
+                     for k, v in summ.items()}
+    return out
+
+
 def run_ours(args, world, rank, local, pg):
     import __graft_entry__ as g
     g.build()
@@ -381,6 +414,7 @@ def run_ours(args, world, rank, local, pg):
     coupled = (run_coupled(args, rank == 0 and not args.skip_cpu)
                if not args.skip_sdpd and args.coupled_steps > 0 else None)
     uneven = run_uneven(args) if args.uneven_intervals > 0 else None
+    surrogate = run_surrogate(args) if args.surrogate else None
 
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -407,6 +441,8 @@ def run_ours(args, world, rank, local, pg):
         out["secondary_coupled"] = coupled
     if uneven is not None:
         out["secondary_uneven"] = uneven
+    if surrogate is not None:
+        out["secondary_surrogate"] = surrogate
     if rank == 0 and not args.skip_cpu:
         out["cpu_baseline"] = cpu_baseline()
     return out
@@ -421,6 +457,8 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-sdpd", action="store_true")
     ap.add_argument("--sdpd-steps", type=int, default=200)
+    ap.add_argument("--surrogate", action="store_true",
+                    help="add the learned-surrogate sweep line (about four minutes)")
     ap.add_argument("--uneven-intervals", type=int, default=1,
                     help="timed intervals of the 4,096-instance uneven ensemble (0 = skip)")
     ap.add_argument("--coupled-steps", type=int, default=100,
