@@ -898,7 +898,7 @@ int sp_run_start(sp_handle* h, const sp_run_args* a, sp_outputs* out) {
     R.max_leaf = max_leaf;
     R.max_levels = max_levels;
     launch_nsm_init(h->d_trajs, h->d_insts, ntraj, max_leaf, max_levels, d_u0, !R.coupled, st);
-    h->launches += R.coupled ? 1 : 2 + max_levels;
+    h->launches += R.coupled ? 1 : 3;
     if (R.ngroups == 2) {
         // largest total propensity first, so the longest trajectories start
         // first (longest-processing-time order)
@@ -1070,7 +1070,7 @@ static int coupled_steps(sp_handle* h, int target, bool ref, long long budget, l
         launch_nsm_rebuild(h->d_trajs, h->d_insts, ntraj, R.max_leaf, R.max_levels,
                            h->dt * (double)R.step, (uint32_t)R.step, st);
         launch_groups(h, ref, R.step + 1, budget, max_ns);
-        h->launches += 3 + 1 + 1 + 2 + R.max_levels + 1;
+        h->launches += 3 + 1 + 1 + 3 + 1;
         R.step++;
     }
     cudaEventRecord(h->eb, st);

@@ -91,63 +91,68 @@ __global__ void nsm_init_leaves(NsmTraj* trajs, const NsmInstance* insts, int nt
     if (j >= ntraj) return;
     NsmTraj& T = trajs[j];
     const NsmInstance& I = insts[T.inst];
-    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < I.leaf_stride;
-         v += gridDim.x * blockDim.x) {
-        if (v >= I.N) { T.leaf[v] = SP_INF_BITS; continue; }
-        float srr = 0.0f, sdr = 0.0f;
-        const int* x = T.x + (size_t)v * I.S;
-        for (int r = 0; r < I.R; r++) {
-            if (I.kind[r] == SP_RXN_CUSTOM) {
-                if (I.allowed && !I.allowed[r * (I.T + 1) + I.type[v]]) continue;
-                auto xs = [&](int s) { return x[s]; };
-                srr = srr + (float)run_program(I.code + I.code_off[r], I.consts, I.data, I.N, v,
-                                               xs, (double)I.vol[v], 0.0, I.type[v]);
-                continue;
-            }
-            const int ra = I.reac[2 * r], rb = I.reac[2 * r + 1];
-            srr = srr + prop(I, r, ra < 0 ? 0 : x[ra], rb < 0 ? 0 : x[rb], I.vol[v], I.ivol[v],
-                             I.type[v]);
-        }
-        for (int s = 0; s < I.S; s++) sdr = sdr + I.ddiag[(size_t)v * I.S + s] * (float)x[s];
-        const u32x4 rr = philox4x32_10((uint32_t)v, build_index, 1u, 0u, T.key0, T.key1);
-        T.leaf[v] = draw_time(t0, neglog_f(u32f(rr.x)), srr + sdr);
-        if (srr + sdr > 0.0f) atomicAdd(&T.a_tot, (double)(srr + sdr));
-    }
-}
-
-// one warp per parent node of level l+1
-__global__ void nsm_build_level(NsmTraj* trajs, const NsmInstance* insts, int ntraj, int l) {
-    const int j = blockIdx.y;
-    if (j >= ntraj) return;
-    NsmTraj& T = trajs[j];
-    const NsmInstance& I = insts[T.inst];
-    if (l >= I.levels) return;
+    // the instance and trajectory fields the loop reads, held in registers
+    // (the leaf stores below could otherwise alias them for the compiler)
+    const int N = I.N, S = I.S, R = I.R, NT1 = I.level_off[1], stride = I.leaf_stride;
+    const bool tree1 = I.levels >= 1;
+    const int* __restrict__ X = T.x;
+    long long* __restrict__ leaf = T.leaf;
+    long long* __restrict__ nt = T.node_t;
+    int* __restrict__ ni = T.node_i;
+    long long* __restrict__ n2 = T.node_t2;
+    const uint32_t k0 = T.key0, k1 = T.key1;
+    const float* __restrict__ ddiag = I.ddiag;
     const int lane = threadIdx.x & 31;
-    const int wpb = blockDim.x >> 5;
-    const int nparent = I.level_size[l + 1];
-    for (int p = blockIdx.x * wpb + (threadIdx.x >> 5); p < nparent; p += gridDim.x * wpb) {
-        const int c = p * 32 + lane;
-        long long t = SP_INF_BITS;
-        int i = INT_MAX;
-        if (l == 0) {
-            if (c < I.leaf_stride) { t = T.leaf[c]; i = c; }
-        } else if (c < I.level_size[l]) {
-            t = T.node_t[I.level_off[l] + c];
-            i = T.node_i[I.level_off[l] + c];
+    // leaf_stride is a multiple of 32 and blocks hold whole warps, so every
+    // lane of a warp runs the same iterations, over one voxel group
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < stride; v += gridDim.x * blockDim.x) {
+        float a = 0.0f;
+        long long tv = SP_INF_BITS;
+        if (v < N) {
+            float srr = 0.0f, sdr = 0.0f;
+            const int* x = X + (size_t)v * S;
+            const int type = I.type[v];
+            for (int r = 0; r < R; r++) {
+                if (I.kind[r] == SP_RXN_CUSTOM) {
+                    if (I.allowed && !I.allowed[r * (I.T + 1) + type]) continue;
+                    auto xs = [&](int s) { return x[s]; };
+                    srr = srr + (float)run_program(I.code + I.code_off[r], I.consts, I.data, N, v,
+                                                   xs, (double)I.vol[v], 0.0, type);
+                    continue;
+                }
+                const int ra = I.reac[2 * r], rb = I.reac[2 * r + 1];
+                srr = srr + prop(I, r, ra < 0 ? 0 : x[ra], rb < 0 ? 0 : x[rb], I.vol[v],
+                                 I.ivol[v], type);
+            }
+            for (int s = 0; s < S; s++) sdr = sdr + ddiag[(size_t)v * S + s] * (float)x[s];
+            a = srr + sdr;
+            // a voxel without propensity gets an infinite time whatever its
+            // draw, so its Philox block is skipped (sparse systems rebuild fast)
+            if (a > 0.0f) {
+                const u32x4 rr = philox4x32_10((uint32_t)v, build_index, 1u, 0u, k0, k1);
+                tv = draw_time(t0, neglog_f(u32f(rr.x)), a);
+            }
         }
-        const long long tc = t;
-        const int ic = i;
-        warp_argmin(t, i);
-        if (lane == 0) {
-            T.node_t[I.level_off[l + 1] + p] = t;
-            T.node_i[I.level_off[l + 1] + p] = i;
-        }
-        if (l == 0) {   // second-smallest leaf time of the group
-            long long t2 = ic == i ? SP_INF_BITS : tc;
-            int i2 = ic == i ? INT_MAX : ic;
+        leaf[v] = tv;
+        // the group's level-1 node (minimum) and second-smallest time, here
+        // instead of a second pass over the leaves
+        if (tree1) {
+            long long t = tv;
+            int i = v;
+            warp_argmin(t, i);
+            long long t2 = i == v ? SP_INF_BITS : tv;
+            int i2 = i == v ? INT_MAX : v;
             warp_argmin(t2, i2);
-            if (lane == 0) T.node_t2[p] = t2;
+            if (lane == 0) {
+                nt[NT1 + (v >> 5)] = t;
+                ni[NT1 + (v >> 5)] = i;
+                n2[v >> 5] = t2;
+            }
         }
+        // running total (steers speculation only): one atomic per warp
+        double ad = a > 0.0f ? (double)a : 0.0;
+        for (int o = 16; o > 0; o >>= 1) ad += __shfl_xor_sync(SP_FULL, ad, o);
+        if (lane == 0 && ad > 0.0) atomicAdd(&T.a_tot, ad);
     }
 }
 
@@ -787,16 +792,41 @@ __global__ void nsm_reset_totals(NsmTraj* trajs, int ntraj) {
     if (j < ntraj) trajs[j].a_tot = 0.0;
 }
 
+// levels 2..L of every trajectory's tree, one block per trajectory (these
+// levels hold few nodes: a launch per level would cost more than the work)
+__global__ void nsm_build_upper(NsmTraj* trajs, const NsmInstance* insts, int ntraj) {
+    const int j = blockIdx.x;
+    if (j >= ntraj) return;
+    NsmTraj& T = trajs[j];
+    const NsmInstance& I = insts[T.inst];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int l = 1; l < I.levels; l++) {
+        const int nparent = I.level_size[l + 1];
+        for (int p = wid; p < nparent; p += nw) {
+            const int c = p * 32 + lane;
+            long long t = SP_INF_BITS;
+            int i = INT_MAX;
+            if (c < I.level_size[l]) {
+                t = T.node_t[I.level_off[l] + c];
+                i = T.node_i[I.level_off[l] + c];
+            }
+            warp_argmin(t, i);
+            if (lane == 0) {
+                T.node_t[I.level_off[l + 1] + p] = t;
+                T.node_i[I.level_off[l + 1] + p] = i;
+            }
+        }
+        __syncthreads();
+    }
+}
+
 void launch_nsm_rebuild(NsmTraj* trajs, const NsmInstance* insts, int ntraj, int max_leaf,
                         int max_levels, double t0, uint32_t build_index, cudaStream_t st) {
     const int gx = (max_leaf + 255) / 256 < 64 ? (max_leaf + 255) / 256 : 64;
     dim3 g(gx, ntraj);
     nsm_reset_totals<<<(ntraj + 127) / 128, 128, 0, st>>>(trajs, ntraj);
-    nsm_init_leaves<<<g, 256, 0, st>>>(trajs, insts, ntraj, t0, build_index);
-    for (int l = 0; l < max_levels; l++) {
-        const int gbx = (max_leaf / 32 + 3) / 4 + 1 < 64 ? (max_leaf / 32 + 3) / 4 + 1 : 64;
-        nsm_build_level<<<dim3(gbx, ntraj), 128, 0, st>>>(trajs, insts, ntraj, l);
-    }
+    nsm_init_leaves<<<g, 256, 0, st>>>(trajs, insts, ntraj, t0, build_index);   // + level 1
+    if (max_levels > 1) nsm_build_upper<<<ntraj, 256, 0, st>>>(trajs, insts, ntraj);
 }
 
 // u0 copy, then (build_queue) the queue at t = 0 with build index 0; a
@@ -808,11 +838,8 @@ void launch_nsm_init(NsmTraj* trajs, const NsmInstance* insts, int ntraj, int ma
     dim3 g(gx, ntraj);
     if (u0) nsm_copy_u0<<<g, 256, 0, st>>>(trajs, insts, ntraj, u0);
     if (!build_queue) return;
-    nsm_init_leaves<<<g, 256, 0, st>>>(trajs, insts, ntraj, 0.0, 0u);
-    for (int l = 0; l < max_levels; l++) {
-        const int gbx = (max_leaf / 32 + 3) / 4 + 1 < 64 ? (max_leaf / 32 + 3) / 4 + 1 : 64;
-        nsm_build_level<<<dim3(gbx, ntraj), 128, 0, st>>>(trajs, insts, ntraj, l);
-    }
+    nsm_init_leaves<<<g, 256, 0, st>>>(trajs, insts, ntraj, 0.0, 0u);   // + level 1
+    if (max_levels > 1) nsm_build_upper<<<ntraj, 256, 0, st>>>(trajs, insts, ntraj);
 }
 
 // Per-warp shared memory: the tree (12 bytes per node) and, for small
