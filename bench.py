@@ -170,7 +170,7 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def cpu_baseline(threads: int | None = None, ntraj: int = 128, intervals: int = 8):
+def cpu_baseline(threads: int | None = None, ntraj: int = 128, intervals: int = 16):
     """The oracle (CPU restatement of the reference algorithm) on the host
     cores, a bounded sample of the same workload."""
     import oracle
