@@ -59,6 +59,7 @@ struct SdpdDev {
     int *ncnt, *nidx;
     R *ndist, *ndw;
     R* ndij;     // D_ij per list entry, or nullptr when no species diffuse
+    R *pr, *wv;  // per particle after the predictor: P/rho^2 and m/rho (read by pairs)
     int kcap;
     CellGrid g;
     int* flag;   // bit 1: list overflow, bit 2: NaN state, bit 4: cell overflow
@@ -163,6 +164,11 @@ __global__ void sdpd_begin(SdpdDev<R> D) {
     Fb.x = 0; Fb.y = 0; Fb.z = 0; Fb.w = 0;
     D.Fbp[i] = Fb;
     D.orho[i] = rho;
+    // the pressure term P/rho^2 and the volume m/rho of this particle, as the
+    // force pass evaluates them for every pair it is in (model.cpp:105-120)
+    const R P = D.P0 * (rho / D.rho0 - (R)1.0);
+    D.pr[i] = P / (rho * rho);
+    D.wv[i] = D.mass[i] / rho;
 }
 
 // find_neighbors against the step's tree points + pairwiseForce (model.cpp:39-191)
@@ -238,6 +244,7 @@ __global__ void __launch_bounds__(TB) sdpd_pairs(SdpdDev<R> D, int first_step) {
     const R rhoi = D.rho[i], mi = D.mass[i], nui = D.nu[i];
     const R P0 = D.P0, rho0 = D.rho0;
     const R Pi = P0 * (rhoi / rho0 - (R)1.0);
+    const R pri = Pi / (rhoi * rhoi), npri = -Pi / (rhoi * rhoi), wi = D.wv[i];
     R Fx = D.g0, Fy = D.g1, Fz = D.g2, Bx = 0, By = 0, Bz = 0, Fr = 0;
     for (int k = 0; k < m; k++) {
         const int j = cj[k * TB];
@@ -269,13 +276,13 @@ __global__ void __launch_bounds__(TB) sdpd_pairs(SdpdDev<R> D, int first_step) {
         if (dim > 1) { dx1 = xi.y - xj.y; dv1 = vi.y - vj4.y; dvdx = dvdx + dv1 * dx1; }
         if (dim > 2) { dx2 = xi.z - xj.z; dv2 = vi.z - vj4.z; dvdx = dvdx + dv2 * dx2; }
         const R rhoj = D.rho[j], mj = D.mass[j], nuj = D.nu[j];
-        const R Pj = P0 * (rhoj / rho0 - (R)1.0);
-        R pg = Pi / (rhoi * rhoi) + Pj / (rhoj * rhoj);
-        if (pg < 0) pg = -Pi / (rhoi * rhoi) + Pj / (rhoj * rhoj);
+        const R prj = D.pr[j];                 // Pj / (rhoj * rhoj)
+        R pg = pri + prj;
+        if (pg < 0) pg = npri + prj;
         const R rh = r + (R)0.001 * h;
         const R fp = (R)-1.0 * mj * pg * dWdr / rh;
         const R fv = mj * ((R)2.0 * (nui * nuj) / (nui + nuj)) * ((R)1 / rh) * dWdr / (rhoi * rhoj);
-        const R wi = mi / rhoi, wj = mj / rhoj;
+        const R wj = D.wv[j];                   // mj / rhoj
         const R ss = wi * wi + wj * wj;
         const R fbp = (R)-10.0 * P0 * ((R)1.0 / mi) * ss * dWdr / rh;
         const R a0 = ti.x - vi.x, a1 = ti.y - vi.y, a2 = ti.z - vi.z;
@@ -401,7 +408,7 @@ struct SdpdState {
     std::vector<void*> allocs;
     void *pos = nullptr, *vel = nullptr, *vt = nullptr, *F = nullptr, *Fbp = nullptr,
          *pold = nullptr, *cpos = nullptr, *rho = nullptr, *orho = nullptr, *mass = nullptr,
-         *nu = nullptr, *ndist = nullptr, *ndw = nullptr;
+         *nu = nullptr, *ndist = nullptr, *ndw = nullptr, *pr = nullptr, *wv = nullptr;
     uint8_t* fixed = nullptr;
     int *ccnt = nullptr, *cidx = nullptr, *ncnt = nullptr, *nidx = nullptr, *flag = nullptr;
     void* ndij = nullptr;
@@ -450,6 +457,8 @@ static SdpdDev<R> dev_view(SdpdState* s) {
     D.ccnt = s->ccnt; D.cidx = s->cidx;
     D.ncnt = s->ncnt; D.nidx = s->nidx; D.ndist = (R*)s->ndist; D.ndw = (R*)s->ndw;
     D.ndij = (R*)s->ndij;
+    D.pr = (R*)s->pr;
+    D.wv = (R*)s->wv;
     D.type = s->type;
     D.nbc = s->nbc;
     D.bc_box = s->bc_box;
@@ -471,7 +480,7 @@ static bool upload(SdpdState* s, const sp_scenario& sc, std::string* err) {
     for (void** p : four)
         if (!sd_alloc(s, p, v4, err)) return false;
     if (!sd_alloc(s, &s->cpos, sizeof(V) * (size_t)s->grid.ncell * kCellCap, err)) return false;
-    void** ones[] = {&s->rho, &s->orho, &s->mass, &s->nu};
+    void** ones[] = {&s->rho, &s->orho, &s->mass, &s->nu, &s->pr, &s->wv};
     for (void** p : ones)
         if (!sd_alloc(s, p, r1, err)) return false;
     std::vector<V> pos(N), zero(N), vel(N);
