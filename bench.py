@@ -470,6 +470,9 @@ def main():
                     help="small case for ncu: the bench workload over two 0.05 intervals")
     ap.add_argument("--profile-sdpd", action="store_true",
                     help="small case for ncu: 30 SDPD steps of the dam break (FP32)")
+    ap.add_argument("--profile-coupled", action="store_true",
+                    help="small case for ncu: 5 + 20 steps of the dam break with 64 species "
+                         "trajectories")
     args = ap.parse_args()
     if args.profile_sdpd:
         import __graft_entry__ as g
@@ -480,6 +483,21 @@ def main():
         with Engine(sc, sdpd_precision="f32") as eng:
             eng.sdpd_advance(30)
             print("profile sdpd", eng.last_timing())
+        return
+    if args.profile_coupled:
+        import __graft_entry__ as g
+        g.build()
+        from spatialpy_gb300 import scenario as S
+        from spatialpy_gb300.engine import Engine
+        W, K = 5, 20
+        sc = S.config_dam_break(num_steps=W + K)
+        sc = sc.copy(output_steps=np.array([0, W, W + K], np.int32))
+        with Engine(sc, sdpd_precision="f32") as eng:
+            eng.start(np.arange(SEED0, SEED0 + COUPLED_TRAJ, dtype=np.uint64))
+            eng.advance(2)
+            p = eng.profile()
+            print("profile coupled", p, "ms per step", p["total_ms"] / (W + K))
+            eng.finish()
         return
     if args.profile_case:
         import __graft_entry__ as g
