@@ -843,13 +843,19 @@ int sp_run_start(sp_handle* h, const sp_run_args* a, sp_outputs* out) {
             R.chem = true;
             std::vector<double> c0((size_t)I.N * I.S);
             std::vector<uint32_t> u(c0.size());
+            cudaError_t e = cudaSuccess;
             if (a->buffers_on_device)
-                cudaMemcpy(u.data(), u0ptr[i], sizeof(uint32_t) * u.size(), cudaMemcpyDeviceToHost);
+                e = cudaMemcpy(u.data(), u0ptr[i], sizeof(uint32_t) * u.size(), cudaMemcpyDeviceToHost);
             else
                 std::memcpy(u.data(), a->u0[i], sizeof(uint32_t) * u.size());
-            for (size_t e = 0; e < c0.size(); e++) c0[e] = (double)u[e];   // C = u0 (template :77-80)
-            cudaMemcpy(I.chem.C, c0.data(), sizeof(double) * c0.size(), cudaMemcpyHostToDevice);
-            cudaMemsetAsync(I.chem.Q, 0, sizeof(double) * c0.size(), st);
+            for (size_t q = 0; q < c0.size(); q++) c0[q] = (double)u[q];   // C = u0 (template :77-80)
+            if (e == cudaSuccess)
+                e = cudaMemcpy(I.chem.C, c0.data(), sizeof(double) * c0.size(), cudaMemcpyHostToDevice);
+            if (e == cudaSuccess) e = cudaMemsetAsync(I.chem.Q, 0, sizeof(double) * c0.size(), st);
+            if (e != cudaSuccess) {
+                run_release(h);
+                return spg_set_cuda_error(h, e, "chemistry reset", __FILE__, __LINE__);
+            }
         }
     }
     R.chem_step = 0;
