@@ -179,6 +179,8 @@ struct NsmInstance {
     const double* data;               // [num_data * N] data function values
     int32_t num_data;
     int32_t has_custom;
+    int32_t has_source;               // a zero-order or custom reaction: a voxel
+                                      // without molecules may still have propensity
 };
 
 // Per-trajectory mutable state (device resident for the whole run).

@@ -487,6 +487,9 @@ static int setup_instance(sp_handle* h, const sp_scenario& s, Instance& I) {
     d.data = I.data;
     d.num_data = I.num_data;
     d.has_custom = I.has_custom ? 1 : 0;
+    d.has_source = 0;
+    for (int r = 0; r < R; r++)
+        if (s.rxn_kind[r] == SP_RXN_ZERO || s.rxn_kind[r] == SP_RXN_CUSTOM) d.has_source = 1;
     if (s.enable_pde && S > 0) {
         ChemDev& D = I.chem;
         I.pde = true;

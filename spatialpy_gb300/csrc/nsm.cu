@@ -94,7 +94,7 @@ __global__ void nsm_init_leaves(NsmTraj* trajs, const NsmInstance* insts, int nt
     // the instance and trajectory fields the loop reads, held in registers
     // (the leaf stores below could otherwise alias them for the compiler)
     const int N = I.N, S = I.S, R = I.R, NT1 = I.level_off[1], stride = I.leaf_stride;
-    const bool tree1 = I.levels >= 1;
+    const bool tree1 = I.levels >= 1, source = I.has_source != 0;
     const int* __restrict__ X = T.x;
     long long* __restrict__ leaf = T.leaf;
     long long* __restrict__ nt = T.node_t;
@@ -108,7 +108,15 @@ __global__ void nsm_init_leaves(NsmTraj* trajs, const NsmInstance* insts, int nt
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < stride; v += gridDim.x * blockDim.x) {
         float a = 0.0f;
         long long tv = SP_INF_BITS;
-        if (v < N) {
+        bool idle = false;
+        if (v < N && !source) {
+            // no molecules and no reaction that fires without reactants:
+            // every propensity and diffusion rate is zero
+            int any = 0;
+            for (int s = 0; s < S; s++) any |= X[(size_t)v * S + s];
+            idle = any == 0;
+        }
+        if (v < N && !idle) {
             float srr = 0.0f, sdr = 0.0f;
             const int* x = X + (size_t)v * S;
             const int type = I.type[v];
