@@ -40,7 +40,7 @@
 extern "C" {
 #endif
 
-#define SP_ABI_VERSION 3
+#define SP_ABI_VERSION 4
 
 /* ---- return codes ------------------------------------------------------ */
 #define SP_OK              0
@@ -334,6 +334,87 @@ int sp_neighbors_noalloc(const double* x, int32_t n, int32_t dim, double h,
                          const double* hi, int32_t kmax, int32_t* count, int32_t* idx,
                          double* dist, double* dWdr, double* Dij, void* stream,
                          char* err, int32_t errlen);
+
+/* ---- learned surrogate: the FiLM-conditioned Fourier neural operator ----
+ *
+ * No counterpart in the reference.  A network that maps a lattice's input
+ * fields and a conditioning vector (log rate constants, time) to per-voxel
+ * output fields, run and trained by this library's own kernels
+ * (csrc/fno.cu): forward, backward and Adam, with bf16 weights and fp32
+ * arithmetic and accumulation.
+ *
+ *   h0      = lift(x)                               pointwise, in_ch -> width
+ *   g       = W2 GELU(W1 cond + b1) + b2            [layers][2][width]
+ *   u_k     = S_k(h_k) + L_k h_k + l_k              k = 0 .. layers-1
+ *   h_{k+1} = GELU(u_k * (1 + g[k][0]) + g[k][1])
+ *   out     = P2 GELU(P1 h_L + p1) + p2             width -> hidden -> out_ch
+ *
+ * S_k is the spectral convolution: the real 2-D DFT of each channel,
+ * truncated to the modes kx in [0, modes) U [n-modes, n), ky in [0, modes),
+ * mixed across channels by one complex width x width matrix per mode, and
+ * transformed back (the inverse real DFT of the truncated spectrum).  Fields
+ * are [batch][channel][n*n] fp32 (row-major x, y).
+ *
+ * Parameters are one flat fp32 array, in this order (row-major, [out][in]
+ * for the matrices):
+ *   lift_w [width][in_ch], lift_b [width]
+ *   per layer: spec_w [2*modes*modes][width_in][width_out][2] (mode index
+ *              kxi*modes + ky, kxi < modes: kx = kxi, else kx = n-2*modes+kxi;
+ *              [2] = real, imaginary), lin_w [width][width], lin_b [width]
+ *   film1_w [hidden][cond], film1_b [hidden],
+ *   film2_w [2*layers*width][hidden], film2_b [2*layers*width]
+ *   proj1_w [hidden][width], proj1_b [hidden], proj2_w [out_ch][hidden],
+ *   proj2_b [out_ch]
+ * The forward pass reads a bf16 copy (round to nearest even) of every
+ * parameter; gradients are taken with respect to those values and applied
+ * to the fp32 array by Adam, which refreshes the copy.
+ *
+ * Device pointers: x, cond, target, out.  x may be one input shared by the
+ * whole batch (x_shared = 1) or one per sample.  All calls are asynchronous
+ * on `stream` (NULL = the default stream) except the sp_fno_get_* and
+ * sp_fno_set_params copies and sp_fno_loss, which synchronise.
+ */
+typedef struct sp_fno_shape {
+    int32_t n;          /* lattice edge, 4 <= n <= 64 */
+    int32_t width;      /* channels, <= 64 */
+    int32_t modes;      /* 1 <= modes, 2*modes <= n */
+    int32_t layers;     /* 1 .. 8 */
+    int32_t in_ch;      /* 1 .. 16 */
+    int32_t out_ch;     /* 1 .. 16 */
+    int32_t cond;       /* 1 .. 16 */
+    int32_t hidden;     /* 1 .. 64: projection and conditioning MLP */
+    int32_t max_batch;  /* 1 .. 1024 samples per call */
+} sp_fno_shape;
+
+typedef struct sp_fno sp_fno;
+
+int         sp_fno_create(const sp_fno_shape* shape, sp_fno** out);
+int64_t     sp_fno_num_params(const sp_fno* f);
+/* fp32 parameters from the host; resets the Adam moments and step count */
+int         sp_fno_set_params(sp_fno* f, const float* params, int64_t count);
+int         sp_fno_get_params(sp_fno* f, float* params, int64_t count);
+/* gradients of the last sp_fno_backward (or training step) */
+int         sp_fno_get_grads(sp_fno* f, float* grads, int64_t count);
+/* out [batch][out_ch][n*n] */
+int         sp_fno_forward(sp_fno* f, const float* x, int32_t x_shared, const float* cond,
+                           int32_t batch, float* out, void* stream);
+/* after sp_fno_forward on the same batch: the mean squared error against
+   target [batch][out_ch][n*n] and the gradient of every parameter */
+int         sp_fno_backward(sp_fno* f, const float* target, int32_t batch, void* stream);
+/* one Adam step (PyTorch's Adam: beta1, beta2, eps, no weight decay) */
+int         sp_fno_adam(sp_fno* f, float lr, float beta1, float beta2, float eps, void* stream);
+/* gather rows idx[batch] (host array, each in 0 .. rows-1) of cond
+   [rows][cond], target [rows][out_ch][n*n] and, unless x_shared, x
+   [rows][in_ch][n*n]; then forward, backward and Adam, replayed as one CUDA
+   graph per (arrays, batch size) */
+int         sp_fno_train_step(sp_fno* f, const float* x, int32_t x_shared, const float* cond,
+                              const float* target, int32_t rows, const int32_t* idx,
+                              int32_t batch, float lr, float beta1, float beta2, float eps,
+                              void* stream);
+/* loss of the last backward pass (synchronises) */
+int         sp_fno_loss(sp_fno* f, float* loss);
+const char* sp_fno_last_error(sp_fno* f);
+void        sp_fno_destroy(sp_fno* f);
 
 #ifdef __cplusplus
 }

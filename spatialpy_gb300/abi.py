@@ -30,7 +30,7 @@ SP_BC_V, SP_BC_NU, SP_BC_RHO, SP_BC_C = 0, 1, 2, 3
 SP_SELECT_EXACT, SP_SELECT_REFERENCE = 0, 1
 SP_PREC_F32, SP_PREC_F64 = 0, 1
 
-ABI_VERSION = 3
+ABI_VERSION = 4
 
 _p = C.POINTER
 
@@ -150,7 +150,17 @@ EXPORTED_SYMBOLS = (
     "sp_run_finish", "sp_status", "sp_last_error", "sp_destroy", "sp_get_neighbors",
     "sp_get_ddiag", "sp_get_particles", "sp_sdpd_advance", "sp_last_timing",
     "sp_last_profile", "sp_neighbors_noalloc",
+    "sp_fno_create", "sp_fno_num_params", "sp_fno_set_params", "sp_fno_get_params",
+    "sp_fno_get_grads", "sp_fno_forward", "sp_fno_backward", "sp_fno_adam",
+    "sp_fno_train_step", "sp_fno_loss", "sp_fno_last_error", "sp_fno_destroy",
 )
+
+
+class SpFnoShape(C.Structure):
+    """``sp_fno_shape`` of include/spgpu.h."""
+    _fields_ = [(k, C.c_int32) for k in
+                ("n", "width", "modes", "layers", "in_ch", "out_ch", "cond", "hidden",
+                 "max_batch")]
 
 
 def ptr(arr, ctype):
@@ -280,6 +290,29 @@ def load_library(path: str | None = None):
     lib.sp_neighbors_noalloc.restype = C.c_int
     lib.sp_last_timing.argtypes = [C.c_void_p, _p(C.c_double), _p(C.c_int64)]
     lib.sp_last_timing.restype = C.c_int
+    vp, f32p, i32 = C.c_void_p, _p(C.c_float), C.c_int32
+    lib.sp_fno_create.argtypes = [_p(SpFnoShape), _p(C.c_void_p)]
+    lib.sp_fno_create.restype = C.c_int
+    lib.sp_fno_num_params.argtypes = [vp]
+    lib.sp_fno_num_params.restype = C.c_int64
+    for name in ("sp_fno_set_params", "sp_fno_get_params", "sp_fno_get_grads"):
+        getattr(lib, name).argtypes = [vp, f32p, C.c_int64]
+        getattr(lib, name).restype = C.c_int
+    lib.sp_fno_forward.argtypes = [vp, vp, i32, vp, i32, vp, vp]
+    lib.sp_fno_forward.restype = C.c_int
+    lib.sp_fno_backward.argtypes = [vp, vp, i32, vp]
+    lib.sp_fno_backward.restype = C.c_int
+    lib.sp_fno_adam.argtypes = [vp, C.c_float, C.c_float, C.c_float, C.c_float, vp]
+    lib.sp_fno_adam.restype = C.c_int
+    lib.sp_fno_train_step.argtypes = [vp, vp, i32, vp, vp, i32, _p(C.c_int32), i32, C.c_float,
+                                      C.c_float, C.c_float, C.c_float, vp]
+    lib.sp_fno_train_step.restype = C.c_int
+    lib.sp_fno_loss.argtypes = [vp, f32p]
+    lib.sp_fno_loss.restype = C.c_int
+    lib.sp_fno_last_error.argtypes = [vp]
+    lib.sp_fno_last_error.restype = C.c_char_p
+    lib.sp_fno_destroy.argtypes = [vp]
+    lib.sp_fno_destroy.restype = None
     if path is None:
         _lib = lib
     return lib

@@ -27,6 +27,7 @@ UNITS = {
     "neighbors.cu": ["-fmad=false"],
     "sdpd.cu": ["-fmad=false"],
     "chem.cu": ["-fmad=false"],
+    "fno.cu": [],
 }
 
 

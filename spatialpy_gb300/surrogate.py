@@ -9,17 +9,14 @@ n x n lattice; the parameters (k_f, k_r, k_birth, D_A = D_B, D_C) are drawn
 log-uniformly within one decade of the base values; the targets are the
 per-voxel mean and variance of A, B, C at the output times.
 
-The network (``FNO``): input channels are the voxel coordinates, the
-initial counts and the birth-region mask; a pointwise lift to ``width``
-channels; ``layers`` Fourier layers, each a spectral convolution on the
-lowest ``modes`` x ``modes`` frequencies plus a pointwise linear map, with
-FiLM scale and shift from an MLP on (log parameters, time) and GELU; a
-pointwise projection to 6 channels (means and log-variances).  Weights are
-kept in fp32 and the forward runs under bf16 autocast, so matrix products
-take bf16 operands with fp32 accumulation.
-
-The learned part runs on PyTorch operations (cuBLAS GEMMs and cuFFT under
-torch); the SSA it stands in for is this engine's own kernels.
+The network (``spatialpy_gb300.fno``, kernels in ``csrc/fno.cu``): input
+channels are the voxel coordinates, the initial counts and the birth-region
+mask; a pointwise lift to ``width`` channels; ``layers`` Fourier layers, each
+a spectral convolution on the lowest ``modes`` x ``modes`` frequencies plus a
+pointwise linear map, with FiLM scale and shift from an MLP on (log
+parameters, time) and GELU; a pointwise projection to 6 channels (means and
+log-variances).  Forward, backward and Adam are this library's own kernels,
+with bf16 weights and fp32 accumulation; PyTorch only holds device memory.
 
 Error and fallback: the SSA estimate of a point is noisy (a few molecules per
 voxel), so errors are measured on coarse-grained fields: the mean over
@@ -106,131 +103,91 @@ def rel_error(pred: np.ndarray, ref: np.ndarray, n: int, block: int = 8) -> np.n
 
 
 # ---------------------------------------------------------------------------
-# the network
+# the network: csrc/fno.cu through spatialpy_gb300.fno
 # ---------------------------------------------------------------------------
-def _torch():
-    import torch
-    return torch
-
-
-def build_fno(width: int = 32, modes: int = 12, layers: int = 4, in_ch: int = 6,
-              out_ch: int = 6, cond: int = 6):
-    torch = _torch()
-    nn = torch.nn
-
-    class Spectral(nn.Module):
-        def __init__(self):
-            super().__init__()
-            scale = 1.0 / (width * width)
-            self.w1 = nn.Parameter(scale * torch.randn(width, width, modes, modes, 2))
-            self.w2 = nn.Parameter(scale * torch.randn(width, width, modes, modes, 2))
-
-        def forward(self, x):
-            b, c, h, w = x.shape
-            # the FFT runs in fp32 (or fp64) whatever the autocast dtype
-            xr = x if x.dtype in (torch.float32, torch.float64) else x.float()
-            xf = torch.fft.rfft2(xr)
-            out = torch.zeros(b, width, h, w // 2 + 1, dtype=xf.dtype, device=x.device)
-            w1 = torch.view_as_complex(self.w1).to(xf.dtype)
-            w2 = torch.view_as_complex(self.w2).to(xf.dtype)
-            out[:, :, :modes, :modes] = torch.einsum("bixy,ioxy->boxy", xf[:, :, :modes, :modes], w1)
-            out[:, :, -modes:, :modes] = torch.einsum("bixy,ioxy->boxy", xf[:, :, -modes:, :modes], w2)
-            return torch.fft.irfft2(out, s=(h, w))
-
-    class FNO(nn.Module):
-        def __init__(self):
-            super().__init__()
-            self.lift = nn.Conv2d(in_ch, width, 1)
-            self.spec = nn.ModuleList([Spectral() for _ in range(layers)])
-            self.lin = nn.ModuleList([nn.Conv2d(width, width, 1) for _ in range(layers)])
-            self.film = nn.Sequential(nn.Linear(cond, 64), nn.GELU(), nn.Linear(64, 2 * width * layers))
-            self.proj = nn.Sequential(nn.Conv2d(width, 64, 1), nn.GELU(), nn.Conv2d(64, out_ch, 1))
-
-        def forward(self, x, c):
-            h = self.lift(x)
-            g = self.film(c).view(c.shape[0], len(self.spec), 2, -1, 1, 1)
-            for k, (sp, li) in enumerate(zip(self.spec, self.lin)):
-                h = sp(h) + li(h)
-                h = h * (1.0 + g[:, k, 0]) + g[:, k, 1]
-                h = torch.nn.functional.gelu(h)
-            return self.proj(h)
-
-    return FNO()
-
-
 class Surrogate:
     """FNO surrogate of the ensemble mean and variance of a parameter sweep."""
 
     def __init__(self, cfg: SweepConfig, device: str = "cuda", width: int = 32, modes: int = 12,
-                 layers: int = 4, seed: int = 0):
-        torch = _torch()
-        torch.manual_seed(seed)
+                 layers: int = 4, seed: int = 0, batch: int = 64, members: int = 1):
+        """``members`` networks with seeds seed, seed+1, ... are trained
+        independently; predictions are their average."""
+        import torch
+        from .fno import FnoNet, FnoShape
+        self.torch = torch
         self.cfg = cfg
         self.device = device
-        self.modes = min(modes, cfg.n // 2)
-        self.net = build_fno(width, self.modes, layers).to(device)
-        sc = point_scenario(np.array([BASE[k] for k in NAMES]), cfg)
+        self.batch = batch
         n = cfg.n
+        self.shape = FnoShape(n=n, width=width, modes=min(modes, n // 2), layers=layers,
+                              in_ch=6, out_ch=6, cond=len(NAMES) + 1, hidden=64, max_batch=batch)
+        self.nets = [FnoNet(self.shape, seed=seed + j) for j in range(members)]
+        self.seed = seed
+        sc = point_scenario(np.array([BASE[k] for k in NAMES]), cfg)
         xy = sc.x[:, :2].reshape(n, n, 2)
         u0 = sc.u0.astype(np.float64).reshape(n, n, 3)
         mask = (sc.type == 2).reshape(n, n, 1).astype(np.float64)
         grid = np.concatenate([xy, u0 / max(1.0, u0.max()), mask], axis=2)   # [n,n,6]
-        self.grid = torch.tensor(grid.transpose(2, 0, 1)[None], dtype=torch.float32, device=device)
+        self.grid = torch.tensor(np.ascontiguousarray(grid.transpose(2, 0, 1)),
+                                 dtype=torch.float32, device=device)          # shared input
         self.times = np.arange(1, cfg.num_times + 1) * (cfg.t_end / cfg.num_times)
         self.scale = None
 
     def _cond(self, params: np.ndarray):
-        torch = _torch()
         base = np.array([BASE[k] for k in NAMES])
         lp = np.log10(params / base)                           # [-1, 1]
-        P, T = len(params), len(self.times)
+        T = len(self.times)
         c = np.concatenate([np.repeat(lp, T, axis=0),
-                            np.tile(self.times / self.cfg.t_end, P)[:, None]], axis=1)
-        return torch.tensor(c, dtype=torch.float32, device=self.device)
+                            np.tile(self.times / self.cfg.t_end, len(params))[:, None]], axis=1)
+        return self.torch.tensor(c, dtype=self.torch.float32, device=self.device)
 
     def _targets(self, mean, var):
-        torch = _torch()
         P, T, N, S_ = mean.shape
         n = self.cfg.n
         y = np.concatenate([mean / self.scale, np.log1p(var) / np.log1p(self.scale)], axis=3)
         y = y.reshape(P * T, n, n, 2 * S_).transpose(0, 3, 1, 2)
-        return torch.tensor(np.ascontiguousarray(y), dtype=torch.float32, device=self.device)
+        return self.torch.tensor(np.ascontiguousarray(y), dtype=self.torch.float32,
+                                 device=self.device)
 
-    def fit(self, params, mean, var, epochs: int = 300, lr: float = 2e-3, batch: int = 64):
-        """Train on SSA ensemble moments; returns the final training loss."""
-        torch = _torch()
+    def fit(self, params, mean, var, epochs: int = 300, lr: float = 2e-3):
+        """Train every member on SSA ensemble moments (Adam, cosine
+        learning-rate schedule, minibatches of ``batch`` rows); returns the
+        members' mean final loss and sets ``train_seconds``."""
+        torch = self.torch
         self.scale = float(max(mean.max(), 1.0))
         c = self._cond(params)
         y = self._targets(mean, var)
-        opt = torch.optim.Adam(self.net.parameters(), lr=lr)
-        sched = torch.optim.lr_scheduler.CosineAnnealingLR(opt, epochs)
-        n = y.shape[0]
-        loss = torch.tensor(0.0)
-        for _ in range(epochs):
-            perm = torch.randperm(n, device=self.device)
-            for k in range(0, n, batch):
-                idx = perm[k:k + batch]
-                with torch.autocast("cuda", dtype=torch.bfloat16):
-                    out = self.net(self.grid.expand(len(idx), -1, -1, -1), c[idx])
-                loss = torch.mean((out.float() - y[idx]) ** 2)
-                opt.zero_grad(set_to_none=True)
-                loss.backward()
-                opt.step()
-            sched.step()
-        return float(loss.detach())
+        rows = y.shape[0]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        losses = []
+        for j, net in enumerate(self.nets):
+            rng = np.random.default_rng(self.seed + j)
+            for e in range(epochs):
+                lr_e = lr * 0.5 * (1.0 + math.cos(math.pi * e / epochs))
+                perm = rng.permutation(rows).astype(np.int32)
+                for k in range(0, rows, self.batch):
+                    net.train_step(self.grid, c, y, perm[k:k + self.batch], lr_e)
+            losses.append(net.loss())
+        self.train_seconds = time.perf_counter() - t0
+        return float(np.mean(losses))
 
     def predict(self, params):
         """(mean, var) [P, T, N, 3] and the device seconds of inference."""
-        torch = _torch()
+        torch = self.torch
         c = self._cond(params)
         n = self.cfg.n
+        outs = [torch.empty(c.shape[0], 6, n, n, dtype=torch.float32, device=self.device)
+                for _ in self.nets]
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        with torch.no_grad(), torch.autocast("cuda", dtype=torch.bfloat16):
-            out = self.net(self.grid.expand(c.shape[0], -1, -1, -1), c).float()
+        for net, out in zip(self.nets, outs):
+            for k in range(0, c.shape[0], self.batch):
+                net.forward(self.grid, c[k:k + self.batch], out=out[k:k + self.batch])
         torch.cuda.synchronize()
         sec = time.perf_counter() - t0
-        out = out.cpu().numpy().transpose(0, 2, 3, 1).reshape(len(params), len(self.times), n * n, 6)
+        out = np.mean([o.cpu().numpy() for o in outs], axis=0)
+        out = out.transpose(0, 2, 3, 1).reshape(len(params), len(self.times), n * n, 6)
         mean = np.maximum(out[..., :3] * self.scale, 0.0)
         var = np.maximum(np.expm1(out[..., 3:] * math.log1p(self.scale)), 0.0)
         return mean, var, sec

@@ -37,7 +37,8 @@ def test_every_declared_symbol_is_exported(spgpu_lib):
 
 STRUCTS = {"sp_scenario": abi.SpScenario, "sp_options": abi.SpOptions,
            "sp_run_args": abi.SpRunArgs, "sp_outputs": abi.SpOutputs,
-           "sp_traj_status": abi.SpTrajStatus, "sp_profile": abi.SpProfile}
+           "sp_traj_status": abi.SpTrajStatus, "sp_profile": abi.SpProfile,
+           "sp_fno_shape": abi.SpFnoShape}
 
 
 def test_struct_layout_matches_header(tmp_path):
@@ -93,3 +94,18 @@ def test_null_arguments(spgpu_lib):
     assert spgpu_lib.sp_run(None, None, None) == abi.SP_E_INVALID
     assert spgpu_lib.sp_status(None, 0, None) == abi.SP_E_INVALID
     spgpu_lib.sp_destroy(None)
+
+
+def test_fno_shape_checks_before_device_calls(spgpu_lib):
+    """sp_fno_create rejects shapes outside its limits without touching a GPU."""
+    good = dict(n=32, width=32, modes=12, layers=4, in_ch=6, out_ch=6, cond=6, hidden=64,
+                max_batch=64)
+    h = C.c_void_p()
+    assert spgpu_lib.sp_fno_create(None, C.byref(h)) == abi.SP_E_INVALID
+    for field, bad in [("n", 3), ("n", 65), ("modes", 17), ("modes", 0), ("width", 65),
+                       ("layers", 0), ("hidden", 65), ("max_batch", 0), ("in_ch", 17)]:
+        sh = abi.SpFnoShape(**{**good, field: bad})
+        assert spgpu_lib.sp_fno_create(C.byref(sh), C.byref(h)) == abi.SP_E_INVALID, field
+        assert not h.value
+    assert spgpu_lib.sp_fno_num_params(None) == -1
+    spgpu_lib.sp_fno_destroy(None)
