@@ -476,7 +476,36 @@ def main():
     ap.add_argument("--profile-coupled", action="store_true",
                     help="small case for ncu: 5 + 20 steps of the dam break with 64 species "
                          "trajectories")
+    ap.add_argument("--profile-fno", action="store_true",
+                    help="small case for ncu: 3 + 5 training steps and one forward batch of "
+                         "the surrogate network (32 x 32 lattice, batch 64)")
     args = ap.parse_args()
+    if args.profile_fno:
+        import __graft_entry__ as g
+        g.build()
+        import torch
+        from spatialpy_gb300.fno import FnoNet, FnoShape
+        shape = FnoShape(n=32, max_batch=64)
+        rng = np.random.default_rng(0)
+        rows = 256
+        grid = torch.tensor(rng.standard_normal((6, 32, 32)), dtype=torch.float32, device="cuda")
+        cond = torch.tensor(rng.uniform(-1, 1, (rows, 6)), dtype=torch.float32, device="cuda")
+        tgt = torch.tensor(rng.standard_normal((rows, 6, 32, 32)), dtype=torch.float32,
+                           device="cuda")
+        net = FnoNet(shape, seed=0)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        for k in range(8):
+            if k == 3:
+                ev[0].record()
+            net.train_step(grid, cond, tgt, rng.permutation(rows)[:64].astype(np.int32), 1e-3)
+        ev[1].record()
+        ev[2].record()
+        net.forward(grid, cond[:64])
+        ev[3].record()
+        torch.cuda.synchronize()
+        print(f"profile fno: {ev[0].elapsed_time(ev[1]) / 5:.3f} ms per training step, "
+              f"{ev[2].elapsed_time(ev[3]):.3f} ms per forward batch of 64, loss {net.loss():.4f}")
+        return
     if args.profile_sdpd:
         import __graft_entry__ as g
         g.build()

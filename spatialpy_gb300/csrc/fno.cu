@@ -104,12 +104,18 @@ __global__ void __launch_bounds__(128) fno_pointwise(PW a) {
 #pragma unroll
     for (int o = 0; o < CO; o++) acc[o] = o < a.cout ? ws[nw + o] : 0.0f;
     const float* src = a.in + (long long)b * a.in_bs + p;
-    for (int i = 0; i < a.cin; i++) {
-        const float v = src[(long long)i * a.P];
-        const float* wr = ws + i * a.cout;
+    for (int i0 = 0; i0 < a.cin; i0 += 8) {
+        float v[8];                        // eight independent loads in flight
 #pragma unroll
-        for (int o = 0; o < CO; o++)
-            if (o < a.cout) acc[o] += wr[o] * v;
+        for (int j = 0; j < 8; j++) v[j] = i0 + j < a.cin ? src[(long long)(i0 + j) * a.P] : 0.0f;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            if (i0 + j >= a.cin) break;
+            const float* wr = ws + (i0 + j) * a.cout;
+#pragma unroll
+            for (int o = 0; o < CO; o++)
+                if (o < a.cout) acc[o] += wr[o] * v[j];
+        }
     }
     const long long base = (long long)b * a.cout * a.P + p;
 #pragma unroll
@@ -151,10 +157,13 @@ __global__ void fno_analysis(const float* in, float2* out, const float2* tw_g, c
         const int x = e / m, ky = e % m;
         float re = 0.0f, im = 0.0f;
         const float* row = f + x * n;
+        int k = 0;                          // (ky * y) mod n
         for (int y = 0; y < n; y++) {
-            const float2 t = tw[(ky * y) % n];
+            const float2 t = tw[k];
             re += row[y] * t.x;
             im -= row[y] * t.y;
+            k += ky;
+            if (k >= n) k -= n;
         }
         A[x * m + ky] = make_float2(re, im);
     }
@@ -162,11 +171,14 @@ __global__ void fno_analysis(const float* in, float2* out, const float2* tw_g, c
     for (int q = threadIdx.x; q < M; q += blockDim.x) {
         const int kxi = q / m, ky = q % m, kx = mode_kx(kxi, n, m);
         float re = 0.0f, im = 0.0f;
+        int k = 0;                          // (kx * x) mod n
         for (int x = 0; x < n; x++) {
             const float2 a = A[x * m + ky];
-            const float2 t = tw[(kx * x) % n];
+            const float2 t = tw[k];
             re += a.x * t.x + a.y * t.y;
             im += a.y * t.x - a.x * t.y;
+            k += kx;
+            if (k >= n) k -= n;
         }
         const float sc = s_g[ky];
         out[plane * M + q] = make_float2(sc * re, sc * im);
@@ -192,11 +204,23 @@ __global__ void fno_synthesis(const float2* in, float* out, const float2* tw_g, 
     for (int e = threadIdx.x; e < n * m; e += blockDim.x) {
         const int x = e / m, ky = e % m;
         float re = 0.0f, im = 0.0f;
-        for (int kxi = 0; kxi < 2 * m; kxi++) {
+        int k = 0;                          // (kx * x) mod n, kx = 0, 1, .., m-1
+        for (int kxi = 0; kxi < m; kxi++) {
             const float2 v = F[kxi * m + ky];
-            const float2 t = tw[(mode_kx(kxi, n, m) * x) % n];
+            const float2 t = tw[k];
             re += v.x * t.x - v.y * t.y;
             im += v.x * t.y + v.y * t.x;
+            k += x;
+            if (k >= n) k -= n;
+        }
+        k = ((n - m) * x) % n;              // kx = n-m, .., n-1
+        for (int kxi = m; kxi < 2 * m; kxi++) {
+            const float2 v = F[kxi * m + ky];
+            const float2 t = tw[k];
+            re += v.x * t.x - v.y * t.y;
+            im += v.x * t.y + v.y * t.x;
+            k += x;
+            if (k >= n) k -= n;
         }
         Z[x * m + ky] = make_float2(re, im);
     }
@@ -205,10 +229,13 @@ __global__ void fno_synthesis(const float2* in, float* out, const float2* tw_g, 
     for (int e = threadIdx.x; e < P; e += blockDim.x) {
         const int x = e / n, y = e % n;
         float r = 0.0f;
+        int k = 0;                          // (ky * y) mod n
         for (int ky = 0; ky < m; ky++) {
             const float2 z = Z[x * m + ky];
-            const float2 t = tw[(ky * y) % n];
+            const float2 t = tw[k];
             r += z.x * t.x - z.y * t.y;
+            k += y;
+            if (k >= n) k -= n;
         }
         dst[e] = accumulate ? dst[e] + r : r;
     }
@@ -230,18 +257,25 @@ __global__ void fno_mix(const float2* X, const uint16_t* w, float2* Y, int B, in
         if (conj_t) wsm[o * C + i] = make_float2(re, -im);
         else        wsm[i * C + o] = make_float2(re, im);
     }
-    __syncthreads();
-    for (int e = threadIdx.x; e < B * C; e += blockDim.x) {
-        const int b = e / C, o = e % C;
-        float re = 0.0f, im = 0.0f;
-        const float2* xb = X + (long long)b * C * M + q;
-        for (int i = 0; i < C; i++) {
-            const float2 x = xb[(long long)i * M];
-            const float2 ww = wsm[i * C + o];
-            re += x.x * ww.x - x.y * ww.y;
-            im += x.x * ww.y + x.y * ww.x;
+    float2* xs = wsm + C * C;               // [16][C] inputs of this mode
+    for (int b0 = 0; b0 < B; b0 += 16) {
+        const int nb = min(16, B - b0);
+        __syncthreads();
+        for (int e = threadIdx.x; e < nb * C; e += blockDim.x)
+            xs[e] = X[((long long)b0 * C + e) * M + q];
+        __syncthreads();
+        for (int e = threadIdx.x; e < nb * C; e += blockDim.x) {
+            const int bb = e / C, o = e % C;
+            float re = 0.0f, im = 0.0f;
+            const float2* xr = xs + bb * C;
+            for (int i = 0; i < C; i++) {
+                const float2 x = xr[i];
+                const float2 ww = wsm[i * C + o];
+                re += x.x * ww.x - x.y * ww.y;
+                im += x.x * ww.y + x.y * ww.x;
+            }
+            Y[((long long)(b0 + bb) * C + o) * M + q] = make_float2(re, im);
         }
-        Y[((long long)b * C + o) * M + q] = make_float2(re, im);
     }
 }
 
@@ -329,14 +363,24 @@ __global__ void fno_wgrad_partial(const float* dy, const float* x, long long x_b
     }
 }
 
+// 256 threads: 32 consecutive entries (lanes) x 8 groups of partial rows,
+// combined in a fixed order
 __global__ void fno_wgrad_reduce(const float* part, int nblk, int O, int I, float* gw, float* gb) {
+    __shared__ float red[8][33];
     const int E = O * I + O;
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= E) return;
+    const int lane = threadIdx.x & 31, grp = threadIdx.x >> 5;
+    const int e = blockIdx.x * 32 + lane;
     float s = 0.0f;
-    for (int c = 0; c < nblk; c++) s += part[(long long)c * E + e];
-    if (e < O * I) gw[e] = s;
-    else gb[e - O * I] = s;
+    if (e < E)
+        for (int c = grp; c < nblk; c += 8) s += part[(long long)c * E + e];
+    red[grp][lane] = s;
+    __syncthreads();
+    if (grp == 0 && e < E) {
+        float t = red[0][lane];
+        for (int g = 1; g < 8; g++) t += red[g][lane];
+        if (e < O * I) gw[e] = t;
+        else gb[e - O * I] = t;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -624,7 +668,7 @@ void wgrad(sp_fno* f, const float* dy, const float* x, long long x_bs, int O, in
     const size_t smem = sizeof(float) * (O + I) * (kTile + 1);
     fno_wgrad_partial<<<nblk, 256, smem, f->st>>>(dy, x, x_bs, O, I, f->P, tiles, f->part);
     const int E = O * I + O;
-    fno_wgrad_reduce<<<(E + 255) / 256, 256, 0, f->st>>>(f->part, nblk, O, I, gw, gb);
+    fno_wgrad_reduce<<<(E + 31) / 32, 256, 0, f->st>>>(f->part, nblk, O, I, gw, gb);
 }
 
 // ---- forward / backward enqueue ------------------------------------------
@@ -649,7 +693,7 @@ void enqueue_forward(sp_fno* f, const float* x, long long x_bs, const float* con
         float* hk = f->h + k * stride_h;
         float2* Xk = f->X + k * stride_X;
         analysis(f, hk, Xk, B * C, f->s_one);
-        const size_t msm = sizeof(float2) * C * C;
+        const size_t msm = sizeof(float2) * (C * C + 16 * C);
         fno_mix<<<f->M, 256, msm, f->st>>>(Xk, f->pb + o.spec[k], f->Y, B, C, f->M, 0);
         synthesis(f, f->Y, f->sbuf, B * C, f->s_inv, 0);
         PW l = pw_base(f, B);
@@ -700,7 +744,7 @@ void enqueue_backward(sp_fno* f, const float* target, int B) {
     // layers, last to first
     float* dh = f->dhA;
     float* dh_next = f->dhB;
-    const size_t msm = sizeof(float2) * C * C;
+    const size_t msm = sizeof(float2) * (C * C + 16 * C);
     for (int k = L - 1; k >= 0; k--) {
         const float* hk = f->h + k * stride_h;
         const float2* Xk = f->X + k * stride_X;

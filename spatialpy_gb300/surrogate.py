@@ -186,17 +186,32 @@ class Surrogate:
                 net.forward(self.grid, c[k:k + self.batch], out=out[k:k + self.batch])
         torch.cuda.synchronize()
         sec = time.perf_counter() - t0
+        members = [self._fields(o.cpu().numpy(), len(params)) for o in outs]
+        self.last_members = members
         out = np.mean([o.cpu().numpy() for o in outs], axis=0)
-        out = out.transpose(0, 2, 3, 1).reshape(len(params), len(self.times), n * n, 6)
+        mean, var = self._fields(out, len(params))
+        return mean, var, sec
+
+    def _fields(self, out, P):
+        n = self.cfg.n
+        out = out.transpose(0, 2, 3, 1).reshape(P, len(self.times), n * n, 6)
         mean = np.maximum(out[..., :3] * self.scale, 0.0)
         var = np.maximum(np.expm1(out[..., 3:] * math.log1p(self.scale)), 0.0)
-        return mean, var, sec
+        return mean, var
 
 
 def sweep(surrogate: Surrogate, params, ssa_mean, ssa_var, ssa_seconds: float,
           threshold: float = 0.02, block: int = 8):
     """Surrogate answers with SSA fallback where the coarse error of the mean
-    or the variance exceeds ``threshold``; returns a summary dict."""
+    or the variance against the held-out SSA ensemble exceeds ``threshold``
+    (the SSA judges every point; only the fallback points' share of its time
+    is charged to the surrogate).  Returns a summary dict.
+
+    With several members it also reports a gate that needs no SSA: accept a
+    point when the members' spread around their average (the same coarse
+    metric) is at most ``threshold / 2`` for the mean and the variance; the
+    summary gives how many points it accepts, how many of those are within
+    ``threshold`` of the SSA, and the time with the SSA answering the rest."""
     cfg = surrogate.cfg
     pm, pv, inf_s = surrogate.predict(params)
     em = rel_error(pm, ssa_mean, cfg.n, block)
@@ -204,7 +219,17 @@ def sweep(surrogate: Surrogate, params, ssa_mean, ssa_var, ssa_seconds: float,
     ok = (em <= threshold) & (ev <= threshold)
     P = len(params)
     fallback_s = ssa_seconds * (P - ok.sum()) / P
-    return {"points": P, "accepted": int(ok.sum()), "err_mean_median": float(np.median(em)),
-            "err_var_median": float(np.median(ev)), "inference_s": inf_s,
-            "ssa_s": ssa_seconds, "surrogate_plus_fallback_s": inf_s + fallback_s,
-            "speedup": ssa_seconds / (inf_s + fallback_s), "threshold": threshold}
+    out = {"points": P, "accepted": int(ok.sum()), "err_mean_median": float(np.median(em)),
+           "err_var_median": float(np.median(ev)), "inference_s": inf_s,
+           "ssa_s": ssa_seconds, "surrogate_plus_fallback_s": inf_s + fallback_s,
+           "speedup": ssa_seconds / (inf_s + fallback_s), "threshold": threshold}
+    members = getattr(surrogate, "last_members", [])
+    if len(members) > 1:
+        sm = np.mean([rel_error(m, pm, cfg.n, block) for m, _ in members], axis=0)
+        sv = np.mean([rel_error(v, pv, cfg.n, block) for _, v in members], axis=0)
+        gate = (sm <= threshold / 2) & (sv <= threshold / 2)
+        gs = inf_s + ssa_seconds * (P - gate.sum()) / P
+        out.update({"gated_accepted": int(gate.sum()),
+                    "gated_within_threshold": int((gate & ok).sum()),
+                    "gated_seconds": gs, "gated_speedup": ssa_seconds / gs})
+    return out
