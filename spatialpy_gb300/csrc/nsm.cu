@@ -295,7 +295,7 @@ __global__ void __launch_bounds__(128) nsm_advance_generic(NsmTraj* trajs, const
                 evn++;
                 nev++;
                 if ((evn & 31) == 0) rb = rng_block(evn, lane, T.key0, T.key1);
-                // round 1: everything that depends on v only
+                // load phase 1: everything that depends on v only
                 int xv = lane < S ? X[(size_t)v * S + lane] : 0;
                 const float ddv = lane < S ? I.ddiag[(size_t)v * S + lane] : 0.0f;
                 const int typev = I.type[v];
@@ -389,7 +389,7 @@ __global__ void __launch_bounds__(128) nsm_advance_generic(NsmTraj* trajs, const
                     if (k < 0) { status = SP_TRAJ_SELECT_OVERFLOW; errv = v; break; }
                     const int w = prefetch ? __shfl_sync(SP_FULL, nb, k & 31)
                                            : I.nbr_idx[(size_t)v * K + k];
-                    // round 2: the destination
+                    // load phase 2: the destination
                     int xw = lane < S ? X[(size_t)w * S + lane] : 0;
                     const float ddw = lane < S ? I.ddiag[(size_t)w * S + lane] : 0.0f;
                     const int typew = I.type[w];
@@ -580,7 +580,7 @@ __global__ void __launch_bounds__(128) nsm_advance_small(NsmTraj* trajs, const N
                 evn++;
                 nev++;
                 if ((evn & 31) == 0) rbk = rng_block(evn, lane, T.key0, T.key1);
-                // round 1: uniform loads of the source voxel + its rows
+                // load phase 1: uniform loads of the source voxel + its rows
                 int xv[MS];
                 float ddv[MS];
 #pragma unroll
@@ -691,7 +691,7 @@ __global__ void __launch_bounds__(128) nsm_advance_small(NsmTraj* trajs, const N
                     if (k < 0) { status = SP_TRAJ_SELECT_OVERFLOW; errv = v; break; }
                     const int w = prefetch ? __shfl_sync(SP_FULL, nb, k & 31)
                                            : I.nbr_idx[(size_t)v * K + k];
-                    // round 2: the destination
+                    // load phase 2: the destination
                     int xw[MS];
                     float ddw[MS];
 #pragma unroll
