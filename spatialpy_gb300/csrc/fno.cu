@@ -828,6 +828,11 @@ int sp_fno_create(const sp_fno_shape* shape, sp_fno** out) {
         s.out_ch > 16 || s.cond < 1 || s.cond > 16 || s.hidden < 1 || s.hidden > 64 ||
         s.max_batch < 1 || s.max_batch > 1024)
         return SP_E_INVALID;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return SP_E_CUDA;    // no usable CUDA device
+    }
     sp_fno* f = new sp_fno();
     f->s = s;
     f->off = offsets(s);

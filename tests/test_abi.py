@@ -109,3 +109,19 @@ def test_fno_shape_checks_before_device_calls(spgpu_lib):
         assert not h.value
     assert spgpu_lib.sp_fno_num_params(None) == -1
     spgpu_lib.sp_fno_destroy(None)
+
+
+def test_fno_create_without_a_device_fails_cleanly(spgpu_lib):
+    """A valid shape on a machine without a CUDA device: an error code, no handle."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    sh = abi.SpFnoShape(n=16, width=8, modes=4, layers=2, in_ch=3, out_ch=2, cond=3, hidden=16,
+                        max_batch=4)
+    h = C.c_void_p()
+    assert spgpu_lib.sp_fno_create(C.byref(sh), C.byref(h)) == abi.SP_E_CUDA
+    assert not h.value
+    from spatialpy_gb300 import fno
+    with pytest.raises(fno.FnoError):
+        fno.FnoNet(fno.FnoShape(n=16, width=8, modes=4, layers=2, in_ch=3, out_ch=2, cond=3,
+                                hidden=16, max_batch=4))
