@@ -96,3 +96,17 @@ def test_bf16_rounding_is_nearest_even():
                         np.float32([0.0, -0.0, 1.0, 1.00390625, 1.01171875, 65504.0])])
     want = torch.tensor(a).to(torch.bfloat16).float().numpy()
     np.testing.assert_array_equal(F.bf16_round(a), want)
+
+
+def test_oracle_matches_autograd_at_the_sweep_shape():
+    """The shape the surrogate sweep trains (32 x 32, width 32, 12 modes,
+    4 layers), two samples, one input shared by the batch."""
+    s = F.FnoShape(n=32, max_batch=2)
+    flat, P, x, cond, target = _case(s, B=2, shared=True, seed=5)
+    out, cache = FO.forward(P, x, cond, s.n, s.modes, s.layers)
+    loss, dout = FO.mse(out, target)
+    G = FO.backward(P, cache, dout, s.n, s.modes, s.layers)
+    tl, tout, TG = TR.loss_and_grads(P, x, cond, target, s.n, s.modes, s.layers)
+    np.testing.assert_allclose(out, tout, rtol=1e-10, atol=1e-12)
+    for k, g in TG.items():
+        assert np.abs(G[k] - g).max() <= 1e-9 * (np.abs(g).max() + 1e-30), k
