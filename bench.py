@@ -48,6 +48,10 @@ B_RXN = 8 * 3 + 16 * 4 + 24 + 4 * 5              # 132
 # capture of the profile case (--profile-case: 7.046 GB over 8,894,255 events
 # in the captured launch; profiles/nsm_advance_batchw4_rdme40.txt)
 DRAM_BYTES_PER_EVENT = 792.0
+# DRAM bytes (read + write) per particle of one sdpd_pairs launch (the
+# step's dominant kernel) from one ncu capture of --profile-sdpd: 37.0 MB
+# for 84,696 particles (profiles/sdpd_pairs_dambreak.txt)
+SDPD_PAIRS_DRAM_BYTES_PER_PARTICLE = 437.0
 
 
 def workload(intervals: int | None = None):
@@ -239,8 +243,11 @@ def run_sdpd(args):
                                    "(84,696 particles), Lucy kernel h=1.5s, dt=1e-4, FP32",
                        "particles": int(sc.num_particles)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "peak_source": src,
-                         "bytes_per_particle_step": B_SDPD}}
+                         "frac": achieved / peak,
+                         "traffic": SDPD_PAIRS_DRAM_BYTES_PER_PARTICLE * sc.num_particles,
+                         "traffic_note": "ncu DRAM bytes of one sdpd_pairs launch (the step's "
+                                         "dominant kernel; state fits in L2)",
+                         "peak_source": src, "bytes_per_particle_step": B_SDPD}}
 
 
 COUPLED_TRAJ = 64
