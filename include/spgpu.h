@@ -190,7 +190,13 @@ typedef struct sp_options {
                                      3 = sequential register kernel;
                                      4 / 5 = speculative batches with 2 / 4 warps
                                      per trajectory */
-    int32_t reserved;
+    int32_t sdpd_self_pair;       /* how a moved particle meets its own start-of-step
+                                     point in the force pass (particle.cpp:240-294 on a
+                                     kd-tree of start-of-step points):
+                                     0 = FP64 from the rounded positions, as the
+                                     reference (no pair when the step rounds away);
+                                     FP32 at the distance |dt vt| of the step itself;
+                                     1 = at |dt vt| in both precisions */
     int64_t event_budget;         /* max events per trajectory per launch (0 = default) */
 } sp_options;
 

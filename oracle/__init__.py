@@ -67,7 +67,7 @@ def lib():
                                        _p(C.c_int64), _p(C.c_int32)]
         for fn in (L.spo_sdpd_f64, L.spo_sdpd_f32):
             fn.argtypes = [_p(SpScenario), C.c_int32, C.c_int32, C.c_int32, C.c_int32] + \
-                [_p(C.c_double)] * 7 + [_p(C.c_int32), C.c_void_p, C.c_void_p]
+                [_p(C.c_double)] * 7 + [_p(C.c_int32), C.c_void_p, C.c_void_p, C.c_void_p]
         L.spo_coupled_ensemble.argtypes = [_p(SpScenario), _p(C.c_uint32), _p(C.c_uint64),
                                            C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                            C.c_int32, C.c_int32, _p(C.c_int32),
@@ -160,9 +160,22 @@ def nsm_ensemble(sc, seeds, selection: int = 0, threads: int = 0, want_counts: b
     return out, ev, st, used
 
 
+class SpoF32State(C.Structure):
+    _fields_ = [("xh", _p(C.c_float)), ("xl", _p(C.c_float)), ("drho", _p(C.c_float)),
+                ("valid", C.c_int32)]
+
+
 class SdpdState:
+    """Flow state between oracle calls.  x and rho are the double views; the
+    FP32 flow keeps its stored state (positions as float hi + lo, densities
+    as float deviations from rho0) in xh, xl, drho."""
+
     def __init__(self, sc):
         n = sc.num_particles
+        self.xh = np.zeros((n, 3), np.float32)
+        self.xl = np.zeros((n, 3), np.float32)
+        self.drho = np.zeros(n, np.float32)
+        self.f32_valid = 0
         self.x = sc.x.copy()
         self.v = np.zeros((n, 3)) if sc.v is None else sc.v.copy()
         self.vt = np.zeros((n, 3))
@@ -181,13 +194,16 @@ def sdpd(sc, state: SdpdState, nsteps: int, precision: str = "f64", mode: int = 
     bit 2 = start-of-step neighbour points (both reference behaviours)."""
     s = scenario_struct(sc)
     fn = lib().spo_sdpd_f64 if precision == "f64" else lib().spo_sdpd_f32
+    fs = SpoF32State(_ptr(state.xh, C.c_float), _ptr(state.xl, C.c_float),
+                     _ptr(state.drho, C.c_float), state.f32_valid)
     rc = fn(C.byref(s), state.step, nsteps, mode, kmax, _ptr(state.x, C.c_double),
             _ptr(state.v, C.c_double), _ptr(state.vt, C.c_double), _ptr(state.rho, C.c_double),
             _ptr(state.F, C.c_double), _ptr(state.Fbp, C.c_double), _ptr(state.Frho, C.c_double),
             _ptr(state.nbr_count, C.c_int32), None,
-            C.byref(SpoChem(None, None, _ptr(state.nu, C.c_double))))
+            C.byref(SpoChem(None, None, _ptr(state.nu, C.c_double))), C.byref(fs))
     if rc != 0:
         raise RuntimeError(f"SDPD oracle failed (rc={rc})")
+    state.f32_valid = fs.valid
     state.step += nsteps
     return state
 

@@ -14,6 +14,7 @@
 #define FMAX fmax
 #define SPO_NB spo_nb_f64
 #define SPO_FN spo_sdpd_f64
+#define SPO_COMP 0
 #include "sdpd_oracle_impl.h"
 #undef REAL
 #undef SQRT
@@ -21,6 +22,7 @@
 #undef FMAX
 #undef SPO_NB
 #undef SPO_FN
+#undef SPO_COMP
 
 #define REAL float
 #define SQRT sqrtf
@@ -28,4 +30,5 @@
 #define FMAX fmaxf
 #define SPO_NB spo_nb_f32
 #define SPO_FN spo_sdpd_f32
+#define SPO_COMP 1
 #include "sdpd_oracle_impl.h"

@@ -721,6 +721,8 @@ int spo_coupled_ensemble(const sp_scenario *sc, const uint32_t *u0, const uint64
     memcpy(x, sc->x, sizeof(double) * 3 * N);
     if (sc->v) memcpy(v, sc->v, sizeof(double) * 3 * N);
     memcpy(rho, sc->rho, sizeof(double) * N);
+    spo_f32_state fs = {(float *)malloc(sizeof(float) * 3 * N), (float *)malloc(sizeof(float) * 3 * N),
+                        (float *)malloc(sizeof(float) * N), 0};
     spo_sdpd_lists L;
     L.count = (int32_t *)calloc(N, sizeof(int32_t));
     L.idx = (int32_t *)malloc(sizeof(int32_t) * (size_t)N * kmax);
@@ -762,8 +764,10 @@ int spo_coupled_ensemble(const sp_scenario *sc, const uint32_t *u0, const uint64
             oi++;
         }
         rc = precision == 64
-                 ? spo_sdpd_f64(sc, step, 1, mode, kmax, x, v, vt, rho, F, Fbp, Frho, NULL, &L, &ch)
-                 : spo_sdpd_f32(sc, step, 1, mode, kmax, x, v, vt, rho, F, Fbp, Frho, NULL, &L, &ch);
+                 ? spo_sdpd_f64(sc, step, 1, mode, kmax, x, v, vt, rho, F, Fbp, Frho, NULL, &L, &ch,
+                                NULL)
+                 : spo_sdpd_f32(sc, step, 1, mode, kmax, x, v, vt, rho, F, Fbp, Frho, NULL, &L, &ch,
+                                &fs);
         if (rc) break;
         /* nsm_core__initialize_rxn/diff_propensities (simulate_rdme.cpp:113-152)
            with this step's lists and the end-of-step densities */
@@ -791,6 +795,7 @@ int spo_coupled_ensemble(const sp_scenario *sc, const uint32_t *u0, const uint64
         oi++;
     }
     free(ch.C); free(ch.Q); free(ch.nu);
+    free(fs.xh); free(fs.xl); free(fs.drho);
     for (int j = 0; j < ntraj; j++) {
         ev[2 * j] = st[j].nrx;
         ev[2 * j + 1] = st[j].ndf;

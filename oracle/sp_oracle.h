@@ -84,12 +84,25 @@ typedef struct spo_chem {
     double *Q;
     double *nu;
 } spo_chem;
+/* The FP32 flow's stored state between calls (ignored by spo_sdpd_f64):
+ * positions as float pairs hi + lo [N*3] each, densities as float deviations
+ * from rho0 [N].  valid = 0 on the first call (state taken from x and rho);
+ * every call writes it back and sets valid = 1.  NULL: taken from x and rho
+ * on every call (exact only for a single call). */
+typedef struct spo_f32_state {
+    float *xh;
+    float *xl;
+    float *drho;
+    int32_t valid;
+} spo_f32_state;
 int spo_sdpd_f64(const sp_scenario *sc, int32_t step0, int32_t nsteps, int32_t mode, int32_t kmax,
                  double *x, double *v, double *vt, double *rho, double *F, double *Fbp,
-                 double *Frho, int32_t *nbr_count, spo_sdpd_lists *lists, spo_chem *chem);
+                 double *Frho, int32_t *nbr_count, spo_sdpd_lists *lists, spo_chem *chem,
+                 spo_f32_state *fs);
 int spo_sdpd_f32(const sp_scenario *sc, int32_t step0, int32_t nsteps, int32_t mode, int32_t kmax,
                  double *x, double *v, double *vt, double *rho, double *F, double *Fbp,
-                 double *Frho, int32_t *nbr_count, spo_sdpd_lists *lists, spo_chem *chem);
+                 double *Frho, int32_t *nbr_count, spo_sdpd_lists *lists, spo_chem *chem,
+                 spo_f32_state *fs);
 
 /* Deterministic chemistry (Model.enable_pde; model.cpp:151-189,
  * simulate.cpp:81-88, 166-171) with the layouts the matrices are written in

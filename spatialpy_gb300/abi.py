@@ -91,7 +91,7 @@ class SpOptions(C.Structure):
         ("device", C.c_int32),
         ("sdpd_precision", C.c_int32),
         ("nsm_variant", C.c_int32),
-        ("reserved", C.c_int32),
+        ("sdpd_self_pair", C.c_int32),
         ("event_budget", C.c_int64),
     ]
 

@@ -441,7 +441,7 @@ static int setup_instance(sp_handle* h, const sp_scenario& s, Instance& I) {
             SP_CUDA_TRY(cudaGetLastError());
         }
     } else {
-        I.sdpd = sdpd_create(s, h->opt.sdpd_precision, h->st, &h->err);
+        I.sdpd = sdpd_create(s, h->opt.sdpd_precision, h->opt.sdpd_self_pair, h->st, &h->err);
         if (!I.sdpd) return SP_E_CUDA;
         if (S > 0) {
             // species on a moving domain: the flow's force-pass lists carry

@@ -30,6 +30,15 @@
 // Densities read from neighbours in the corrector are their post-predictor
 // values (old_rho), the order a parallel engine reads them in.
 //
+// FP32 storage.  The FP32 instantiation computes in float but stores a
+// position as a float pair hi + lo (advanced by an error-free two-sum) and a
+// density as its deviation from rho0 (rho, old_rho), with the float density
+// rho0 + deviation in rfull for every reader other than the pressure
+// P = P0 (rho/rho0 - 1) = P0 deviation/rho0.  Plain float storage decides the
+// pressure term's sign switch (model.cpp:111-112) on rounding noise: after
+// 1,000 steps of the 1,368-particle dam break its velocities are 2.8e-4 from
+// FP64, these are 1.2e-6.  Box tests of boundary conditions read hi parts.
+//
 // Compiled with -fmad=false: the arithmetic rounds like the CPU oracle.
 #include <cuda_runtime.h>
 
@@ -47,12 +56,19 @@ template <typename R> struct Vec4;
 template <> struct Vec4<float> { using T = float4; };
 template <> struct Vec4<double> { using T = double4; };
 
+// float: compensated storage (hi + lo positions, density deviations)
+template <typename R> constexpr bool kComp = sizeof(R) == 4;
+
 template <typename R>
 struct SdpdDev {
     int N, dim, step, stat;
+    int self_step;   // self pair at |dt vt| (always in FP32)
     R h, dt, rho0, P0, alpha, g0, g1, g2;
+    double rho0d;
     typename Vec4<R>::T *pos, *vel, *vt, *F, *Fbp, *pold;
+    typename Vec4<R>::T *plo, *pold_lo, *cpos_lo;   // lo parts (float only)
     R *rho, *orho, *mass, *nu;
+    R* rfull;    // float: rho0 + deviation; double: the densities themselves
     const uint8_t* fixed;
     int *ccnt, *cidx;               // per cell: slot count, particle index [ncell][CAP]
     typename Vec4<R>::T* cpos;      // per cell slot: start-of-step position
@@ -78,6 +94,10 @@ struct SdpdDev {
 // corrector, simulate.cpp:88, 171).  Concentration targets are chem.cu's.
 template <typename R, typename V>
 __device__ __forceinline__ void flow_bcs(const SdpdDev<R>& D, int i, const V& p, V& v, R& rho) {
+    // the density as the condition sees it; a stored deviation changes only
+    // if the conditions leave a different density
+    const double rin = kComp<R> ? D.rho0d + (double)rho : (double)rho;
+    double rr = rin;
     for (int b = 0; b < D.nbc; b++) {
         const int tg = D.bc_target[b];
         if (tg >= SP_BC_C) continue;
@@ -94,9 +114,23 @@ __device__ __forceinline__ void flow_bcs(const SdpdDev<R>& D, int i, const V& p,
         } else if (tg == SP_BC_NU) {
             D.nu[i] = (R)val[0];
         } else {
-            rho = (R)val[0];
+            rr = val[0];
         }
     }
+    if (kComp<R>) {
+        if (rr != rin) rho = (R)(rr - D.rho0d);
+    } else {
+        rho = (R)rr;
+    }
+}
+
+// hi + lo += b, renormalised (two-sum, then fast two-sum)
+__device__ __forceinline__ void comp_add(float& hi, float& lo, float b) {
+    const float s = hi + b, bb = s - hi;
+    const float e = (hi - (s - bb)) + (b - bb);
+    const float l = lo + e, s2 = s + l;
+    lo = l - (s2 - s);
+    hi = s2;
 }
 
 constexpr int kCellCap = 16;
@@ -112,9 +146,12 @@ __device__ __forceinline__ int cellc(R p, const CellGrid& g, int d) {
 // take_step1 (simulate.cpp:56-109) + the cell key of the start-of-step point
 template <typename R>
 __global__ void sdpd_begin(SdpdDev<R> D) {
+    using V = typename Vec4<R>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= D.N) return;
     auto p = D.pos[i];
+    V pl{};
+    if (kComp<R>) pl = D.plo[i];
     auto v = D.vel[i];
     R rho = D.rho[i];
     if (isnan((double)p.x) || isinf((double)p.x) || isnan((double)p.y) || isinf((double)p.y) ||
@@ -128,10 +165,12 @@ __global__ void sdpd_begin(SdpdDev<R> D) {
     if (slot < kCellCap) {
         D.cidx[c * kCellCap + slot] = i;
         D.cpos[c * kCellCap + slot] = p;
+        if (kComp<R>) D.cpos_lo[c * kCellCap + slot] = pl;
     } else {
         atomicOr(D.flag, 4);
     }
     D.pold[i] = p;
+    if (kComp<R>) D.pold_lo[i] = pl;
     if (!D.stat && !D.fixed[i]) {
         const auto F = D.F[i];
         const auto Fb = D.Fbp[i];
@@ -143,9 +182,16 @@ __global__ void sdpd_begin(SdpdDev<R> D) {
         t.x = v.x + hdt * Fb.x;
         t.y = v.y + hdt * Fb.y;
         t.z = v.z + hdt * Fb.z;
-        p.x = p.x + D.dt * t.x;
-        p.y = p.y + D.dt * t.y;
-        p.z = p.z + D.dt * t.z;
+        if constexpr (kComp<R>) {
+            comp_add(p.x, pl.x, D.dt * t.x);
+            comp_add(p.y, pl.y, D.dt * t.y);
+            comp_add(p.z, pl.z, D.dt * t.z);
+            D.plo[i] = pl;
+        } else {
+            p.x = p.x + D.dt * t.x;
+            p.y = p.y + D.dt * t.y;
+            p.z = p.z + D.dt * t.z;
+        }
         rho = rho + hdt * F.w;
         D.vel[i] = v;
         D.vt[i] = t;
@@ -166,9 +212,17 @@ __global__ void sdpd_begin(SdpdDev<R> D) {
     D.orho[i] = rho;
     // the pressure term P/rho^2 and the volume m/rho of this particle, as the
     // force pass evaluates them for every pair it is in (model.cpp:105-120)
-    const R P = D.P0 * (rho / D.rho0 - (R)1.0);
-    D.pr[i] = P / (rho * rho);
-    D.wv[i] = D.mass[i] / rho;
+    if constexpr (kComp<R>) {
+        const R rf = D.rho0 + rho;
+        D.rfull[i] = rf;
+        const R P = D.P0 * (rho / D.rho0);
+        D.pr[i] = P / (rf * rf);
+        D.wv[i] = D.mass[i] / rf;
+    } else {
+        const R P = D.P0 * (rho / D.rho0 - (R)1.0);
+        D.pr[i] = P / (rho * rho);
+        D.wv[i] = D.mass[i] / rho;
+    }
 }
 
 // find_neighbors against the step's tree points + pairwiseForce (model.cpp:39-191)
@@ -185,13 +239,15 @@ __global__ void __launch_bounds__(TB) sdpd_pairs(SdpdDev<R> D, int first_step) {
     if (i >= D.N) return;
     // at the first step of a run the lists come from the unmoved points (take_step1)
     const auto q = first_step ? D.pold[i] : D.pos[i];
+    typename Vec4<R>::T ql{};
+    if (kComp<R>) ql = first_step ? D.pold_lo[i] : D.plo[i];
     const R h = D.h, sq = h * h;
     const int dim = D.dim;
     const int c0 = cellc<R>(q.x, D.g, 0), c1 = cellc<R>(q.y, D.g, 1), c2 = cellc<R>(q.z, D.g, 2);
     int m = 0;
     bool over = false;
     R self_d2 = 0;
-    if (sizeof(R) == 4 && !first_step) {
+    if (D.self_step && !first_step) {
         const auto t = D.vt[i];
         const R a = D.dt * t.x, b = D.dt * t.y, c = D.dt * t.z;
         self_d2 = a * a;
@@ -211,12 +267,18 @@ __global__ void __launch_bounds__(TB) sdpd_pairs(SdpdDev<R> D, int first_step) {
                 for (int t = 0; t < e; t++) {
                     const int j = D.cidx[cid * kCellCap + t];
                     const auto p = D.cpos[cid * kCellCap + t];
+                    R t0 = q.x - p.x, t1 = q.y - p.y, t2 = q.z - p.z;
+                    if constexpr (kComp<R>) {
+                        const auto pl = D.cpos_lo[cid * kCellCap + t];
+                        t0 = t0 + (ql.x - pl.x);
+                        t1 = t1 + (ql.y - pl.y);
+                        t2 = t2 + (ql.z - pl.z);
+                    }
                     R d2 = 0;
-                    const R t0 = q.x - p.x;
                     d2 = d2 + t0 * t0;
-                    if (dim > 1) { const R t1 = q.y - p.y; d2 = d2 + t1 * t1; }
-                    if (dim > 2) { const R t2 = q.z - p.z; d2 = d2 + t2 * t2; }
-                    if (sizeof(R) == 4 && j == i) d2 = self_d2;
+                    if (dim > 1) d2 = d2 + t1 * t1;
+                    if (dim > 2) d2 = d2 + t2 * t2;
+                    if (D.self_step && j == i) d2 = self_d2;
                     if (d2 > sq || d2 == (R)0) continue;     // kd_fix_rad_search.cpp:160-174
                     if (sqrt(d2) > h) continue;              // particle.cpp:160-162
                     if (m >= KCAP || m >= D.kcap) { over = true; continue; }
@@ -239,11 +301,13 @@ __global__ void __launch_bounds__(TB) sdpd_pairs(SdpdDev<R> D, int first_step) {
     D.ncnt[i] = m;
     const R alpha = D.alpha;
     const auto xi = D.pos[i];
+    typename Vec4<R>::T xli{};
+    if (kComp<R>) xli = D.plo[i];
     const auto vi = D.vel[i];
     const auto ti = D.vt[i];
-    const R rhoi = D.rho[i], mi = D.mass[i], nui = D.nu[i];
+    const R rhoi = D.rfull[i], mi = D.mass[i], nui = D.nu[i];
     const R P0 = D.P0, rho0 = D.rho0;
-    const R Pi = P0 * (rhoi / rho0 - (R)1.0);
+    const R Pi = kComp<R> ? P0 * (D.rho[i] / rho0) : P0 * (rhoi / rho0 - (R)1.0);
     const R pri = Pi / (rhoi * rhoi), npri = -Pi / (rhoi * rhoi), wi = D.wv[i];
     R Fx = D.g0, Fy = D.g1, Fz = D.g2, Bx = 0, By = 0, Bz = 0, Fr = 0;
     for (int k = 0; k < m; k++) {
@@ -263,7 +327,7 @@ __global__ void __launch_bounds__(TB) sdpd_pairs(SdpdDev<R> D, int first_step) {
             const R ihsq = ih * ih;
             const R dhr = h - r;
             const R wfd = (R)-25.066903536973515383 * dhr * dhr * ihsq * ihsq * ihsq * ih;
-            const R mj = D.mass[j], rj = D.rho[j];
+            const R mj = D.mass[j], rj = D.rfull[j];
             D.ndij[o] = (R)-2.0 * (mi * mj) / (mi + mj) * (rhoi + rj) / (rhoi * rj) * r2 * wfd /
                         (r2 + (R)0.01 * h * h);
         }
@@ -271,11 +335,18 @@ __global__ void __launch_bounds__(TB) sdpd_pairs(SdpdDev<R> D, int first_step) {
         const auto xj = D.pos[j];
         const auto vj4 = D.vel[j];
         const auto tj = D.vt[j];
+        R ex0 = xi.x - xj.x, ex1 = xi.y - xj.y, ex2 = xi.z - xj.z;
+        if constexpr (kComp<R>) {
+            const auto xlj = D.plo[j];
+            ex0 = ex0 + (xli.x - xlj.x);
+            ex1 = ex1 + (xli.y - xlj.y);
+            ex2 = ex2 + (xli.z - xlj.z);
+        }
         R dx0 = 0, dx1 = 0, dx2 = 0, dv0 = 0, dv1 = 0, dv2 = 0, dvdx = 0;
-        dx0 = xi.x - xj.x; dv0 = vi.x - vj4.x; dvdx = dvdx + dv0 * dx0;
-        if (dim > 1) { dx1 = xi.y - xj.y; dv1 = vi.y - vj4.y; dvdx = dvdx + dv1 * dx1; }
-        if (dim > 2) { dx2 = xi.z - xj.z; dv2 = vi.z - vj4.z; dvdx = dvdx + dv2 * dx2; }
-        const R rhoj = D.rho[j], mj = D.mass[j], nuj = D.nu[j];
+        dx0 = ex0; dv0 = vi.x - vj4.x; dvdx = dvdx + dv0 * dx0;
+        if (dim > 1) { dx1 = ex1; dv1 = vi.y - vj4.y; dvdx = dvdx + dv1 * dx1; }
+        if (dim > 2) { dx2 = ex2; dv2 = vi.z - vj4.z; dvdx = dvdx + dv2 * dx2; }
+        const R rhoj = D.rfull[j], mj = D.mass[j], nuj = D.nu[j];
         const R prj = D.pr[j];                 // Pj / (rhoj * rhoj)
         R pg = pri + prj;
         if (pg < 0) pg = npri + prj;
@@ -347,6 +418,8 @@ __global__ void sdpd_corrector(SdpdDev<R> D) {
     if (fluid) {
         rho = rho + hdt * F.w;
         const auto xi = D.pos[i];
+        typename Vec4<R>::T xli{};
+        if (kComp<R>) xli = D.plo[i];
         R nw0 = 0, nw1 = 0, nw2 = 0, vos = 0, vtot = 0;
         for (int k = 0; k < m; k++) {
             const R r = D.ndist[base + k];
@@ -357,10 +430,17 @@ __global__ void sdpd_corrector(SdpdDev<R> D) {
             const R W = alpha * (((R)1 + (R)3 * R_) * (omr * omr * omr));
             const R dWdr = D.ndw[base + k];
             const auto xj = D.pos[j];
-            R dx0 = xi.x - xj.x, dx1 = 0, dx2 = 0;
-            if (D.dim > 1) dx1 = xi.y - xj.y;
-            if (D.dim > 2) dx2 = xi.z - xj.z;
-            const R vj = D.mass[j] / D.orho[j];
+            R ex0 = xi.x - xj.x, ex1 = xi.y - xj.y, ex2 = xi.z - xj.z;
+            if constexpr (kComp<R>) {
+                const auto xlj = D.plo[j];
+                ex0 = ex0 + (xli.x - xlj.x);
+                ex1 = ex1 + (xli.y - xlj.y);
+                ex2 = ex2 + (xli.z - xlj.z);
+            }
+            R dx0 = ex0, dx1 = 0, dx2 = 0;
+            if (D.dim > 1) dx1 = ex1;
+            if (D.dim > 2) dx2 = ex2;
+            const R vj = D.mass[j] / (kComp<R> ? D.rho0 + D.orho[j] : D.orho[j]);
             const R vv = vj * vj;
             const bool solid = D.fixed[j];
             if (solid) vos = vos + vv * W;
@@ -394,6 +474,7 @@ __global__ void sdpd_corrector(SdpdDev<R> D) {
     if (D.nbc) flow_bcs(D, i, D.pos[i], v, rho);   // applyBoundaryConditions, simulate.cpp:171
     D.vel[i] = v;
     D.rho[i] = rho;
+    if (kComp<R>) D.rfull[i] = D.rho0 + rho;
 }
 
 // ---------------------------------------------------------------------------
@@ -401,7 +482,7 @@ __global__ void sdpd_corrector(SdpdDev<R> D) {
 // ---------------------------------------------------------------------------
 struct SdpdState {
     int prec = SP_PREC_F32;
-    int N = 0, dim = 0, step = 0, kcap = 48, stat = 0;
+    int N = 0, dim = 0, step = 0, kcap = 48, stat = 0, self_step = 1;
     double h = 0, dt = 0, rho0 = 0, P0 = 0, g[3] = {0, 0, 0};
     cudaStream_t st = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -409,11 +490,14 @@ struct SdpdState {
     void *pos = nullptr, *vel = nullptr, *vt = nullptr, *F = nullptr, *Fbp = nullptr,
          *pold = nullptr, *cpos = nullptr, *rho = nullptr, *orho = nullptr, *mass = nullptr,
          *nu = nullptr, *ndist = nullptr, *ndw = nullptr, *pr = nullptr, *wv = nullptr;
+    // FP32 only: lo parts of positions (current, start of step, cell slots)
+    // and the float densities rho0 + deviation
+    void *plo = nullptr, *pold_lo = nullptr, *cpos_lo = nullptr, *rfull = nullptr;
     uint8_t* fixed = nullptr;
     int *ccnt = nullptr, *cidx = nullptr, *ncnt = nullptr, *nidx = nullptr, *flag = nullptr;
     void* ndij = nullptr;
     // initial state (REAL-typed 4-vectors and densities) for sdpd_reset
-    std::vector<unsigned char> init_pos, init_vel, init_rho, init_nu;
+    std::vector<unsigned char> init_pos, init_vel, init_rho, init_nu, init_lo, init_rfull;
     int* type = nullptr;
     int nbc = 0;
     double *bc_box = nullptr, *bc_value = nullptr;
@@ -440,9 +524,11 @@ static SdpdDev<R> dev_view(SdpdState* s) {
     D.dim = s->dim;
     D.step = s->step;
     D.stat = s->stat;
+    D.self_step = s->self_step;
     D.h = (R)s->h;
     D.dt = (R)s->dt;
     D.rho0 = (R)s->rho0;
+    D.rho0d = s->rho0;
     D.P0 = (R)s->P0;
     const R h = (R)s->h;
     D.alpha = s->dim == 3 ? (R)105 / ((R)16 * (R)M_PI * h * h * h)
@@ -452,7 +538,9 @@ static SdpdDev<R> dev_view(SdpdState* s) {
     D.g2 = (R)s->g[2];
     D.pos = (V*)s->pos; D.vel = (V*)s->vel; D.vt = (V*)s->vt; D.F = (V*)s->F; D.Fbp = (V*)s->Fbp;
     D.pold = (V*)s->pold; D.cpos = (V*)s->cpos;
+    D.plo = (V*)s->plo; D.pold_lo = (V*)s->pold_lo; D.cpos_lo = (V*)s->cpos_lo;
     D.rho = (R*)s->rho; D.orho = (R*)s->orho; D.mass = (R*)s->mass; D.nu = (R*)s->nu;
+    D.rfull = kComp<R> ? (R*)s->rfull : (R*)s->rho;
     D.fixed = s->fixed;
     D.ccnt = s->ccnt; D.cidx = s->cidx;
     D.ncnt = s->ncnt; D.nidx = s->nidx; D.ndist = (R*)s->ndist; D.ndw = (R*)s->ndw;
@@ -483,15 +571,31 @@ static bool upload(SdpdState* s, const sp_scenario& sc, std::string* err) {
     void** ones[] = {&s->rho, &s->orho, &s->mass, &s->nu, &s->pr, &s->wv};
     for (void** p : ones)
         if (!sd_alloc(s, p, r1, err)) return false;
-    std::vector<V> pos(N), zero(N), vel(N);
-    std::vector<R> rho(N), mass(N), nu(N);
+    if (kComp<R>) {
+        void** lo[] = {&s->plo, &s->pold_lo};
+        for (void** p : lo)
+            if (!sd_alloc(s, p, v4, err)) return false;
+        if (!sd_alloc(s, &s->cpos_lo, sizeof(V) * (size_t)s->grid.ncell * kCellCap, err))
+            return false;
+        if (!sd_alloc(s, &s->rfull, r1, err)) return false;
+    }
+    std::vector<V> pos(N), zero(N), vel(N), lo(N);
+    std::vector<R> rho(N), mass(N), nu(N), rf(N);
     for (int i = 0; i < N; i++) {
         pos[i].x = (R)sc.x[3 * i]; pos[i].y = (R)sc.x[3 * i + 1]; pos[i].z = (R)sc.x[3 * i + 2];
         pos[i].w = 0;
         zero[i].x = zero[i].y = zero[i].z = zero[i].w = 0;
         vel[i] = zero[i];
+        lo[i] = zero[i];
         if (sc.v) { vel[i].x = (R)sc.v[3 * i]; vel[i].y = (R)sc.v[3 * i + 1]; vel[i].z = (R)sc.v[3 * i + 2]; }
         rho[i] = (R)sc.rho[i];
+        if (kComp<R>) {
+            lo[i].x = (R)(sc.x[3 * i] - (double)pos[i].x);
+            lo[i].y = (R)(sc.x[3 * i + 1] - (double)pos[i].y);
+            lo[i].z = (R)(sc.x[3 * i + 2] - (double)pos[i].z);
+            rho[i] = (R)(sc.rho[i] - sc.rho0);
+            rf[i] = (R)sc.rho0 + rho[i];
+        }
         mass[i] = (R)sc.mass[i];
         nu[i] = (R)sc.nu[i];
     }
@@ -499,6 +603,12 @@ static bool upload(SdpdState* s, const sp_scenario& sc, std::string* err) {
     s->init_vel.assign((unsigned char*)vel.data(), (unsigned char*)vel.data() + v4);
     s->init_rho.assign((unsigned char*)rho.data(), (unsigned char*)rho.data() + r1);
     s->init_nu.assign((unsigned char*)nu.data(), (unsigned char*)nu.data() + r1);
+    if (kComp<R>) {
+        s->init_lo.assign((unsigned char*)lo.data(), (unsigned char*)lo.data() + v4);
+        s->init_rfull.assign((unsigned char*)rf.data(), (unsigned char*)rf.data() + r1);
+        cudaMemcpyAsync(s->plo, lo.data(), v4, cudaMemcpyHostToDevice, s->st);
+        cudaMemcpyAsync(s->rfull, rf.data(), r1, cudaMemcpyHostToDevice, s->st);
+    }
     // F, Fbp, vt start at zero: the engine reads them before first writing
     // them (particle.cpp:70-83), the oracle zero-initialises them
     cudaMemcpyAsync(s->pos, pos.data(), v4, cudaMemcpyHostToDevice, s->st);
@@ -520,9 +630,11 @@ static bool upload(SdpdState* s, const sp_scenario& sc, std::string* err) {
     return true;
 }
 
-SdpdState* sdpd_create(const sp_scenario& sc, int precision, cudaStream_t st, std::string* err) {
+SdpdState* sdpd_create(const sp_scenario& sc, int precision, int self_step, cudaStream_t st,
+                       std::string* err) {
     SdpdState* s = new SdpdState();
     s->prec = precision == SP_PREC_F64 ? SP_PREC_F64 : SP_PREC_F32;
+    s->self_step = s->prec == SP_PREC_F32 || self_step ? 1 : 0;
     s->N = sc.num_particles;
     s->dim = sc.dimension;
     s->h = sc.h;
@@ -667,17 +779,24 @@ template <typename R>
 static int get_state_t(SdpdState* s, double* x, double* v, double* rho, std::string* err) {
     using V = typename Vec4<R>::T;
     const int N = s->N;
-    std::vector<V> p(N), u(N);
+    std::vector<V> p(N), u(N), pl(N);
     std::vector<R> r(N);
     cudaMemcpy(p.data(), s->pos, sizeof(V) * N, cudaMemcpyDeviceToHost);
+    if (kComp<R>) cudaMemcpy(pl.data(), s->plo, sizeof(V) * N, cudaMemcpyDeviceToHost);
     cudaMemcpy(u.data(), s->vel, sizeof(V) * N, cudaMemcpyDeviceToHost);
-    cudaError_t e = cudaMemcpy(r.data(), s->rho, sizeof(R) * N, cudaMemcpyDeviceToHost);
+    cudaError_t e = cudaMemcpy(r.data(), kComp<R> ? s->rfull : s->rho, sizeof(R) * N,
+                               cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) {
         *err = std::string("SDPD state copy: ") + cudaGetErrorString(e);
         return SP_E_CUDA;
     }
     for (int i = 0; i < N; i++) {
         if (x) { x[3 * i] = p[i].x; x[3 * i + 1] = p[i].y; x[3 * i + 2] = p[i].z; }
+        if (x && kComp<R>) {
+            x[3 * i] += (double)pl[i].x;
+            x[3 * i + 1] += (double)pl[i].y;
+            x[3 * i + 2] += (double)pl[i].z;
+        }
         if (v) { v[3 * i] = u[i].x; v[3 * i + 1] = u[i].y; v[3 * i + 2] = u[i].z; }
         if (rho) rho[i] = r[i];
     }
@@ -745,6 +864,9 @@ int sdpd_reset(SdpdState* s, std::string* err) {
     cudaMemcpyAsync(s->rho, s->init_rho.data(), r1, cudaMemcpyHostToDevice, s->st);
     cudaMemcpyAsync(s->orho, s->init_rho.data(), r1, cudaMemcpyHostToDevice, s->st);
     cudaMemcpyAsync(s->nu, s->init_nu.data(), r1, cudaMemcpyHostToDevice, s->st);
+    if (s->plo) cudaMemcpyAsync(s->plo, s->init_lo.data(), v4, cudaMemcpyHostToDevice, s->st);
+    if (s->rfull)
+        cudaMemcpyAsync(s->rfull, s->init_rfull.data(), r1, cudaMemcpyHostToDevice, s->st);
     cudaMemsetAsync(s->ncnt, 0, sizeof(int) * s->N, s->st);
     cudaMemsetAsync(s->flag, 0, sizeof(int), s->st);
     cudaError_t e = cudaStreamSynchronize(s->st);   // host staging buffers stay valid
@@ -789,7 +911,7 @@ SdpdLists sdpd_lists(SdpdState* s) {
     L.count = s->ncnt;
     L.idx = s->nidx;
     L.dij = s->ndij;
-    L.rho = s->rho;
+    L.rho = s->prec == SP_PREC_F64 ? s->rho : s->rfull;   // full densities
     L.dist = s->ndist;
     L.dwdr = s->ndw;
     L.mass = s->mass;
@@ -814,7 +936,7 @@ void sdpd_launch_volumes(SdpdState* s, const double* mass, float* vol, float* iv
     if (s->prec == SP_PREC_F64)
         sdpd_volumes<double><<<(n + tb - 1) / tb, tb, 0, s->st>>>(n, mass, (const double*)s->rho, vol, ivol);
     else
-        sdpd_volumes<float><<<(n + tb - 1) / tb, tb, 0, s->st>>>(n, mass, (const float*)s->rho, vol, ivol);
+        sdpd_volumes<float><<<(n + tb - 1) / tb, tb, 0, s->st>>>(n, mass, (const float*)s->rfull, vol, ivol);
 }
 
 template <typename R>
@@ -824,8 +946,14 @@ __global__ void sdpd_state_out(SdpdDev<R> D, double* x, double* v, double* rho) 
     const auto p = D.pos[i];
     const auto u = D.vel[i];
     if (x) { x[3 * i] = p.x; x[3 * i + 1] = p.y; x[3 * i + 2] = p.z; }
+    if (x && kComp<R>) {
+        const auto pl = D.plo[i];
+        x[3 * i] = (double)p.x + (double)pl.x;
+        x[3 * i + 1] = (double)p.y + (double)pl.y;
+        x[3 * i + 2] = (double)p.z + (double)pl.z;
+    }
     if (v) { v[3 * i] = u.x; v[3 * i + 1] = u.y; v[3 * i + 2] = u.z; }
-    if (rho) rho[i] = D.rho[i];
+    if (rho) rho[i] = D.rfull[i];
 }
 
 void sdpd_launch_state_out(SdpdState* s, double* x, double* v, double* rho) {

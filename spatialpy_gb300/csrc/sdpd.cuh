@@ -12,7 +12,10 @@ struct SdpdState;
 
 // Uploads the particle state of a moving-domain instance.  Returns nullptr
 // (with *err set) on failure.
-SdpdState* sdpd_create(const sp_scenario& s, int precision, cudaStream_t st, std::string* err);
+// self_step: a moved particle meets its own start-of-step point at |dt vt|
+// (always so in FP32; in FP64 only when set, else from the rounded positions)
+SdpdState* sdpd_create(const sp_scenario& s, int precision, int self_step, cudaStream_t st,
+                       std::string* err);
 void sdpd_destroy(SdpdState* s);
 // nsteps engine steps (take_step substeps 0,1,2; simulate.cpp:33-48)
 int sdpd_advance(SdpdState* s, int nsteps, double* ms, long long* launches, std::string* err);

@@ -34,13 +34,21 @@ class Engine:
     scenarios : Scenario or list of Scenario
         Model instances (a list runs heterogeneous batches in one launch).
     sdpd_precision : "f32" or "f64"
+    sdpd_self_pair : "position" (default) or "step".  How a moved particle
+        meets its own start-of-step point in the force pass: from the rounded
+        positions, as the reference's FP64 engine (no pair when the step
+        rounds away), or at the distance |dt vt| of the step.  FP32 always
+        uses the step.
     nsm_variant : 0 chosen per run, 1 generic sequential warp, 2 speculative batch
         warp, 3 sequential register-resident warp, 4 / 5 speculative batches
         with 2 / 4 warps per trajectory
     """
 
     def __init__(self, scenarios, device: int = 0, sdpd_precision: str = "f32",
-                 nsm_variant: int = 0, event_budget: int = 0, lib_path: str | None = None):
+                 nsm_variant: int = 0, event_budget: int = 0, lib_path: str | None = None,
+                 sdpd_self_pair: str = "position"):
+        if sdpd_self_pair not in ("position", "step"):
+            raise ValueError("sdpd_self_pair must be 'position' or 'step'")
         self.lib = abi.load_library(lib_path)
         if not isinstance(scenarios, (list, tuple)):
             scenarios = [scenarios]
@@ -52,6 +60,7 @@ class Engine:
         opt.device = device
         opt.sdpd_precision = abi.SP_PREC_F64 if sdpd_precision == "f64" else abi.SP_PREC_F32
         opt.nsm_variant = nsm_variant
+        opt.sdpd_self_pair = 1 if sdpd_self_pair == "step" else 0
         opt.event_budget = event_budget
         self._h = C.c_void_p()
         rc = self.lib.sp_create(self._structs, len(scenarios), C.byref(opt), C.byref(self._h))
