@@ -312,28 +312,33 @@ int sp_last_profile(sp_handle* h, sp_profile* p);
 /*
  * sp_neighbors_noalloc — the neighbour lists of sp_get_neighbors (same
  * predicate, order and values), computed without allocating device memory.
- * It has no counterpart in the reference: it exists for callers that cannot
- * call cudaMalloc while they run, such as code recording a CUDA stream
- * capture (allocation is not permitted there) or hosts that hand out all
- * device memory from their own fixed arena.
+ * It has no counterpart in the reference.  It is for callers that cannot
+ * call cudaMalloc while they run: hosts that hand out all device memory from
+ * their own fixed arena (once the arena holds the device a side allocation
+ * fails, or escapes the host's accounting), and loops that cannot take the
+ * device-wide synchronisation that cudaMalloc and cudaFree imply while other
+ * streams are busy.
  *
  * Every array is a device pointer the caller owns: x[n*3], mass[n], rho[n];
  * outputs count[n] and idx/dist/dWdr/Dij[n*kmax] (dist, dWdr, Dij may be
  * NULL).  lo[3]/hi[3] are host arrays bounding the points (points outside
  * fall into edge cells and are still found).  Work is queued on `stream`
- * (NULL = default stream) and the call returns after it completes.
+ * (NULL = default stream); the call synchronises `stream` to read back its
+ * overflow flag and returns after its work completes.
  *
  * Limits: n <= 262,144 particles, at most 524,288 cells of edge h inside
- * [lo, hi], kmax <= 256; larger sizes return SP_E_INVALID with a message in
- * err (errlen bytes, may be NULL).  SP_E_UNSUPPORTED: some particle has more
- * than kmax neighbours.
+ * [lo, hi], kmax <= 256; larger sizes, a non-finite or inverted box and a
+ * non-finite h return SP_E_INVALID with a message in err (errlen bytes, may
+ * be NULL) before any device work.  SP_E_UNSUPPORTED: some particle has
+ * more than kmax neighbours.
  *
  * The cell-list scratch is one file-scope device array of 8.4 MB that every
  * GPU loading the library holds until the process exits.  The first call on a
- * device looks up that array's device address (cudaGetSymbolAddress); make
- * that first call before any stream capture.  All calls share the array:
- * calls that overlap on the GPU (different streams or host threads) race, so
- * serialise them.
+ * device looks up that array's device address (cudaGetSymbolAddress) with the
+ * device current; make that first call before any stream capture.  All calls
+ * share the array, which keeps the last call's contents (each call clears
+ * what must start at zero): calls that overlap on the GPU (different streams
+ * or host threads) race, so serialise them.
  */
 int sp_neighbors_noalloc(const double* x, int32_t n, int32_t dim, double h,
                          const double* mass, const double* rho, const double* lo,

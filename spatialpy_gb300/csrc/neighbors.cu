@@ -12,6 +12,7 @@
 // dimension order), the sum is non-zero (no self match) and sqrt(.) <= h, and
 // stores the list sorted by (r^2, j).  Compiled with -fmad=false, so dist,
 // dWdr and D_ij equal the reference engine's values bit for bit.
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <mutex>
@@ -188,6 +189,7 @@ CellGrid make_grid(const double* x_host, int n, int dim, double h) {
     CellGrid g{};
     g.dim = dim;
     g.cs = h * 1.0000001;
+    double ext[3] = {0.0, 0.0, 0.0};
     for (int d = 0; d < 3; d++) {
         double lo = 0.0, hi = 0.0;
         if (d < dim && n > 0) {
@@ -198,14 +200,19 @@ CellGrid make_grid(const double* x_host, int n, int dim, double h) {
                 hi = p > hi ? p : hi;
             }
         }
-        g.lo[d] = lo;
-        g.nc[d] = d < dim ? (int)((hi - lo) / g.cs) + 1 : 1;
+        g.lo[d] = std::isfinite(lo) ? lo : 0.0;
+        ext[d] = d < dim && std::isfinite(hi - lo) ? hi - lo : 0.0;
     }
-    // keep the grid modest: coarser cells only widen the candidate set
-    while ((long long)g.nc[0] * g.nc[1] * g.nc[2] > (1ll << 26)) {
-        g.cs *= 2.0;
-        for (int d = 0; d < dim; d++) g.nc[d] = g.nc[d] / 2 + 1;
-    }
+    // keep the grid modest: coarser cells only widen the candidate set.  The
+    // counts are formed in double and bounded before the cast to int.
+    auto cells = [&](double cs) {
+        double c = 1.0;
+        for (int d = 0; d < dim; d++) c *= std::floor(ext[d] / cs) + 1.0;
+        return c;
+    };
+    if (!(g.cs > 0.0) || !std::isfinite(g.cs)) g.cs = 1.0;   // callers check h > 0
+    while (!(cells(g.cs) <= (double)(1ll << 26))) g.cs *= 2.0;
+    for (int d = 0; d < 3; d++) g.nc[d] = d < dim ? (int)(std::floor(ext[d] / g.cs) + 1.0) : 1;
     g.ncell = g.nc[0] * g.nc[1] * g.nc[2];
     return g;
 }
@@ -299,7 +306,7 @@ extern "C" int sp_neighbors_noalloc(const double* x, int32_t n, int32_t dim, dou
                                     char* err, int32_t errlen) {
     using namespace spg;
     if (!x || !mass || !rho || !lo || !hi || !count || !idx || n < 1 || dim < 1 || dim > 3 ||
-        !(h > 0.0) || kmax < 1) {
+        !(h > 0.0) || !std::isfinite(h) || kmax < 1) {
         noalloc_msg(err, errlen, "sp_neighbors_noalloc: missing buffer or bad size");
         return SP_E_INVALID;
     }
@@ -314,18 +321,28 @@ extern "C" int sp_neighbors_noalloc(const double* x, int32_t n, int32_t dim, dou
     CellGrid g{};
     g.dim = dim;
     g.cs = h * 1.0000001;
+    // cell counts are formed in double and bounded before any cast to int
+    double cells = 1.0;
     for (int d = 0; d < 3; d++) {
         g.lo[d] = d < dim ? lo[d] : 0.0;
-        g.nc[d] = d < dim ? (int)((hi[d] - lo[d]) / g.cs) + 1 : 1;
-        if (d < dim && !(hi[d] >= lo[d])) {
+        g.nc[d] = 1;
+        if (d >= dim) continue;
+        if (!std::isfinite(lo[d]) || !std::isfinite(hi[d])) {
+            noalloc_msg(err, errlen, "sp_neighbors_noalloc: bounding box not finite");
+            return SP_E_INVALID;
+        }
+        if (!(hi[d] >= lo[d])) {
             noalloc_msg(err, errlen, "sp_neighbors_noalloc: bounding box hi < lo");
             return SP_E_INVALID;
         }
-    }
-    if ((long long)g.nc[0] * g.nc[1] * g.nc[2] > kNoAllocMaxCells) {
-        noalloc_msg(err, errlen,
-                    "sp_neighbors_noalloc: more than 524,288 cells of edge h in the bounding box");
-        return SP_E_INVALID;
+        const double ext = std::floor((hi[d] - lo[d]) / g.cs) + 1.0;
+        cells *= ext;
+        if (!(ext <= (double)kNoAllocMaxCells) || !(cells <= (double)kNoAllocMaxCells)) {
+            noalloc_msg(err, errlen,
+                        "sp_neighbors_noalloc: more than 524,288 cells of edge h in the bounding box");
+            return SP_E_INVALID;
+        }
+        g.nc[d] = (int)ext;
     }
     g.ncell = g.nc[0] * g.nc[1] * g.nc[2];
     int dev = 0;
@@ -354,10 +371,16 @@ extern "C" int sp_neighbors_noalloc(const double* x, int32_t n, int32_t dim, dou
     int* start = fill + kNoAllocMaxCells;
     int* flag = start + kNoAllocMaxCells + 1;
     cudaStream_t st = (cudaStream_t)stream;
+    // an error left on this thread by earlier, unrelated work is not this call's
+    (void)cudaGetLastError();
     // the array keeps the previous call's contents: clear what starts at zero
-    cudaMemsetAsync(hist, 0, sizeof(int) * g.ncell, st);
-    cudaMemsetAsync(fill, 0, sizeof(int) * g.ncell, st);
-    cudaMemsetAsync(flag, 0, sizeof(int), st);
+    cudaError_t e = cudaMemsetAsync(hist, 0, sizeof(int) * g.ncell, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(fill, 0, sizeof(int) * g.ncell, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(flag, 0, sizeof(int), st);
+    if (e != cudaSuccess) {
+        noalloc_msg(err, errlen, cudaGetErrorString(e));
+        return SP_E_CUDA;
+    }
     const int tb = 256, nb = (n + tb - 1) / tb;
     cell_hist<<<nb, tb, 0, st>>>(x, n, g, cell, hist);
     scan_single_block<<<1, 1024, 0, st>>>(hist, start, g.ncell);
@@ -373,9 +396,9 @@ extern "C" int sp_neighbors_noalloc(const double* x, int32_t n, int32_t dim, dou
         neighbor_search_f64<256><<<sb, 128, 0, st>>>(x, x, n, g, h, mass, rho, start, order, kmax,
                                                      count, idx, dist, dWdr, Dij, flag);
     int over = 0;
-    cudaError_t e = cudaMemcpyAsync(&over, flag, sizeof(int), cudaMemcpyDeviceToHost, st);
+    e = cudaGetLastError();                                   // launch errors
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&over, flag, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) {
         noalloc_msg(err, errlen, cudaGetErrorString(e));
         return SP_E_CUDA;

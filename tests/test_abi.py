@@ -125,3 +125,35 @@ def test_fno_create_without_a_device_fails_cleanly(spgpu_lib):
     with pytest.raises(fno.FnoError):
         fno.FnoNet(fno.FnoShape(n=16, width=8, modes=4, layers=2, in_ch=3, out_ch=2, cond=3,
                                 hidden=16, max_batch=4))
+
+
+def test_noalloc_rejects_bad_sizes_before_device_work(spgpu_lib):
+    """sp_neighbors_noalloc checks every size before it touches the device
+    (these calls run without a GPU): too many particles, a box of more cells
+    than its static scratch holds (including one whose cell count overflows
+    an int), an inverted or non-finite box, a non-finite h, kmax above 256."""
+    err = C.create_string_buffer(256)
+    dummy = C.c_void_p(16)
+
+    def box(*v):
+        return (C.c_double * 3)(*v)
+
+    def call(n, h, lo, hi, kmax=32):
+        return spgpu_lib.sp_neighbors_noalloc(dummy, n, 3, h, dummy, dummy, lo, hi, kmax, dummy,
+                                              dummy, None, None, None, None, err, len(err))
+
+    assert call(262145, 0.1, box(0, 0, 0), box(1, 1, 1)) == abi.SP_E_INVALID
+    assert b"262,144" in err.value
+    assert call(1000, 1e-3, box(0, 0, 0), box(1, 1, 1)) == abi.SP_E_INVALID
+    assert b"524,288" in err.value
+    assert call(1000, 1.0, box(0, 0, 0), box(1e12, 1, 1)) == abi.SP_E_INVALID
+    assert b"524,288" in err.value
+    assert call(1000, 1.0, box(0, 0, 0), box(3e9, 3e9, 3e9)) == abi.SP_E_INVALID
+    assert call(1000, 1.0, box(0, 0, 0), box(float("inf"), 1, 1)) == abi.SP_E_INVALID
+    assert b"finite" in err.value
+    assert call(1000, 1.0, box(0, 0, 0), box(float("nan"), 1, 1)) == abi.SP_E_INVALID
+    assert call(1000, 1.0, box(0, 2, 0), box(1, 1, 1)) == abi.SP_E_INVALID
+    assert b"hi < lo" in err.value
+    assert call(1000, float("inf"), box(0, 0, 0), box(1, 1, 1)) == abi.SP_E_INVALID
+    assert call(1000, 0.1, box(0, 0, 0), box(1, 1, 1), kmax=257) == abi.SP_E_INVALID
+    assert b"256" in err.value

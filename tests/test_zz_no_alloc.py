@@ -1,9 +1,12 @@
 """The allocation-free neighbour entry point (sp_neighbors_noalloc).
 
-Callers that cannot allocate device memory while they run (code recording a
-CUDA stream capture, hosts with their own fixed device-memory arena) pass
-their own device buffers; the call keeps its cell-list scratch in a static
-device array.  This file is collected last so that a failure here stops a
+Some callers cannot call cudaMalloc while they run: hosts that hand out all
+device memory from their own fixed arena, and loops that cannot take the
+device-wide synchronisation of cudaMalloc/cudaFree.  They pass their own
+device buffers; the call keeps its cell-list scratch in a static device
+array shared by every call.  These tests compare it with sp_get_neighbors
+(itself pinned to the oracle and to the reference's neighbour lists) on two
+calls in a row.  This file is collected last so that a failure here stops a
 run only after every other test has run; it also passes on its own in a
 fresh process.
 """
@@ -35,22 +38,10 @@ def _call(lib, sc, kmax, dev, lo, hi, err):
         C.c_void_p(dev["dij"].data_ptr()), None, err, len(err))
 
 
-@pytest.mark.parametrize("case", ["rdme3d", "dam"])
-def test_noalloc_neighbors_equal_existing_entry_point(lib, case):
-    torch = pytest.importorskip("torch")
-    from spatialpy_gb300.engine import Engine
-    if case == "rdme3d":
-        sc = S.config_rdme_3d(n=14, nA=10, nB=10)
-        kmax = 64
-    else:
-        sc = S.config_dam_break(spacing_div=16, num_steps=10).copy(static_domain=True)
-        kmax = 64
-    # the existing path: sp_create + sp_get_neighbors
-    with Engine(sc) as eng:
-        want = eng.neighbors(0, kmax)
+def _device_buffers(torch, sc, kmax):
     n = sc.num_particles
     cuda = torch.device("cuda", 0)
-    dev = {
+    return {
         "x": torch.tensor(sc.x, dtype=torch.float64, device=cuda),
         "mass": torch.tensor(sc.mass, dtype=torch.float64, device=cuda),
         "rho": torch.tensor(sc.rho, dtype=torch.float64, device=cuda),
@@ -60,8 +51,34 @@ def test_noalloc_neighbors_equal_existing_entry_point(lib, case):
         "dw": torch.zeros((n, kmax), dtype=torch.float64, device=cuda),
         "dij": torch.zeros((n, kmax), dtype=torch.float64, device=cuda),
     }
+
+
+def _case(case):
+    if case == "rdme3d":     # 3-D lattice, h = 2.2 s: interior particles have 32 neighbours
+        return S.config_rdme_3d(n=14, nA=10, nB=10)
+    return S.config_dam_break(spacing_div=16, num_steps=10).copy(static_domain=True)
+
+
+@pytest.mark.parametrize("case,kmax,box", [("rdme3d", 32, "tight"), ("rdme3d", 128, "tight"),
+                                           ("dam", 64, "tight"), ("dam", 32, "inside")])
+def test_noalloc_neighbors_equal_existing_entry_point(lib, case, kmax, box):
+    """Two calls in a row equal sp_get_neighbors exactly (kmax 32 and 64
+    run one kernel width each, 128 the widest); with the box shrunk inside
+    the point cloud the outside particles fall into edge cells and every
+    list is still complete."""
+    torch = pytest.importorskip("torch")
+    from spatialpy_gb300.engine import Engine
+    sc = _case(case)
+    # the existing path: sp_create + sp_get_neighbors
+    with Engine(sc) as eng:
+        want = eng.neighbors(0, kmax)
+    n = sc.num_particles
+    dev = _device_buffers(torch, sc, kmax)
     lo = sc.x.min(axis=0)
     hi = sc.x.max(axis=0)
+    if box == "inside":
+        span = hi - lo
+        lo, hi = lo + 0.3 * span, hi - 0.3 * span
     err = C.create_string_buffer(256)
     for call in range(2):                       # two calls in a row share the scratch
         for k in ("count", "dist", "dw", "dij"):
@@ -80,14 +97,22 @@ def test_noalloc_neighbors_equal_existing_entry_point(lib, case):
                 np.testing.assert_array_equal(a[i, :c], b[i, :c], err_msg=f"call {call} p {i}")
 
 
-def test_noalloc_rejects_sizes_beyond_its_limit(lib):
+def test_noalloc_reports_lists_longer_than_kmax_then_recovers(lib):
+    """kmax below the largest neighbour count gives SP_E_UNSUPPORTED; the
+    next call with a sufficient kmax starts from a cleared flag and is
+    exact."""
+    torch = pytest.importorskip("torch")
+    from spatialpy_gb300.engine import Engine
+    sc = _case("rdme3d")
     err = C.create_string_buffer(256)
-    one = (C.c_double * 3)(0, 0, 0)
-    big = (C.c_double * 3)(1, 1, 1)
-    dummy = C.c_void_p(16)
-    rc = lib.sp_neighbors_noalloc(dummy, 262145, 3, 0.1, dummy, dummy, one, big, 32, dummy,
-                                  dummy, None, None, None, None, err, len(err))
-    assert rc == abi.SP_E_INVALID and b"262,144" in err.value
-    rc = lib.sp_neighbors_noalloc(dummy, 1000, 3, 1e-3, dummy, dummy, one, big, 32, dummy,
-                                  dummy, None, None, None, None, err, len(err))
-    assert rc == abi.SP_E_INVALID and b"524,288" in err.value
+    lo, hi = sc.x.min(axis=0), sc.x.max(axis=0)
+    dev = _device_buffers(torch, sc, 8)
+    rc = _call(lib, sc, 8, dev, lo, hi, err)
+    assert rc == abi.SP_E_UNSUPPORTED and b"kmax" in err.value
+    with Engine(sc) as eng:
+        want = eng.neighbors(0, 64)
+    dev = _device_buffers(torch, sc, 64)
+    rc = _call(lib, sc, 64, dev, lo, hi, err)
+    assert rc == abi.SP_OK, err.value.decode()
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(dev["count"].cpu().numpy(), want[0])
