@@ -12,8 +12,10 @@ output interval (t -> t+1) of all 256 trajectories.  The trajectory state
          resident in HBM
   e2e    the same metric through the C ABI with host buffers: sp_run of K
          intervals from host u0 to host moment sums (H2D + D2H inside)
-  --impl reference  the CPU restatement of the reference algorithm (oracle)
-         on all host cores, same workload and metric
+  --impl reference  the reference's own C++ engine (compiled from the
+         installed reference package into oracle/_ref, -O2 and -O0 as shipped)
+         on all host cores, same workload, window and metric; the CPU
+         restatement (oracle) only where the engine could not be built
 
 Prints one JSON line on rank 0.
 """
@@ -174,49 +176,92 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def cpu_baseline(threads: int | None = None, ntraj: int = 128, intervals: int = 16):
-    """The oracle (CPU restatement of the reference algorithm) on the host
-    cores, a bounded sample of the same workload."""
+def _reference_engine() -> bool:
+    """Build the reference engine (oracle/_ref) from the installed reference
+    package where it is present; True when its libraries exist."""
     import oracle
     oracle.build()
-    sc = workload(intervals)
-    threads = threads or os.cpu_count() or 1
+    oracle.build_reference()
+    return oracle.reference_available("_exact") and oracle.reference_available("_O0")
+
+
+def _time_reference(ntraj: int, warm: int, timed: int, variant: str, processes: int):
+    """The compiled reference engine (exact-selection twin, or the stock -O0
+    build) on `processes` host cores: ntraj trajectories of the workload,
+    each timed over output intervals [warm, warm + timed)."""
+    import oracle
+    sc = workload(warm + timed)
     seeds = np.arange(SEED0, SEED0 + ntraj, dtype=np.uint64)
     t0 = time.perf_counter()
-    _, ev, st, used = oracle.nsm_ensemble(sc, seeds, 0, threads, want_counts=False)
+    rate, events, used = oracle.ref_nsm_bench(sc, seeds, warm, variant, processes)
+    return rate, events, used, time.perf_counter() - t0
+
+
+def cpu_baseline(warm: int = 3, timed: int = 5):
+    """The reference's compiled engine (-O2, exact-selection twin) on every
+    host core, a bounded sample of the workload: 4 trajectories per core,
+    timed over output intervals [warm, warm + timed).  The CPU restatement
+    (oracle, kind "port") only where the engine could not be built."""
+    cores = os.cpu_count() or 1
+    ntraj = 4 * cores
+    if _reference_engine():
+        rate, events, used, wall = _time_reference(ntraj, warm, timed, "_exact", cores)
+        return {"value": rate, "unit": UNIT, "cores": int(used), "kind": "reference",
+                "sample": f"reference engine -O2, {ntraj} trajectories, output intervals "
+                          f"[{warm}, {warm + timed}) timed ({events} events; {wall:.1f} s wall "
+                          f"with set-up)"}
+    import oracle
+    seeds = np.arange(SEED0, SEED0 + ntraj, dtype=np.uint64)
+    t0 = time.perf_counter()
+    _, ev, _, used = oracle.nsm_ensemble(workload(timed), seeds, 0, cores, want_counts=False)
     dt = time.perf_counter() - t0
     return {"value": float(ev.sum() / dt), "unit": UNIT, "cores": int(used), "kind": "port",
-            "sample": f"{ntraj} trajectories x {intervals} output intervals "
+            "sample": f"port, {ntraj} trajectories x {timed} output intervals "
                       f"({int(ev.sum())} events, {dt:.1f} s)"}
 
 
 def run_reference(args, rank, pg):
-    """--impl reference: the CPU restatement of the reference on all cores."""
+    """--impl reference: the reference's own C++ engine on every host core,
+    the bench's workload over its window (W untimed output intervals, then K
+    timed), 256 trajectories.  Both builds are timed: -O2 (exact-selection
+    twin, the same code with the two selection lines rescaled) gives the
+    line's value; the stock -O0 build, as the reference's SCons build
+    compiles it, is reported beside it on 32 trajectories."""
     if rank != 0:
         return None
-    import oracle
-    oracle.build()
-    threads = os.cpu_count() or 1
-    seeds = np.arange(SEED0, SEED0 + NTRAJ, dtype=np.uint64)
-    # warm-up: W intervals of a few trajectories
-    oracle.nsm_ensemble(workload(max(1, args.warmup)), seeds[:threads], 0, threads,
-                        want_counts=False)
-    sc = workload(args.steps)
-    t0 = time.perf_counter()
-    _, ev, st, used = oracle.nsm_ensemble(sc, seeds, 0, threads, want_counts=False)
-    dt = time.perf_counter() - t0
-    value = float(ev.sum() / dt)
-    sample = f"{NTRAJ} trajectories x {args.steps} output intervals ({int(ev.sum())} events)"
-    return {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+    cores = os.cpu_count() or 1
+    W, K = max(1, args.warmup), args.steps
+    sc = workload(W + K)
+    if _reference_engine():
+        rate, events, used, wall = _time_reference(NTRAJ, W, K, "_exact", cores)
+        r0, e0, _, w0 = _time_reference(32, W, K, "_O0", cores)
+        kind = "reference"
+        sample = (f"reference engine -O2 (exact-selection twin), {NTRAJ} trajectories, "
+                  f"output intervals [{W}, {W + K}) timed, {events} events, {wall:.1f} s wall "
+                  f"with set-up; one trajectory per process at a time")
+        extra = {"reference_O0": {"value": r0, "sample": f"stock -O0 build, 32 trajectories, "
+                                                         f"{e0} events, {w0:.1f} s wall"}}
+    else:
+        import oracle
+        seeds = np.arange(SEED0, SEED0 + NTRAJ, dtype=np.uint64)
+        t0 = time.perf_counter()
+        _, ev, _, used = oracle.nsm_ensemble(workload(K), seeds, 0, cores, want_counts=False)
+        wall = time.perf_counter() - t0
+        rate, events, kind, extra = float(ev.sum() / wall), int(ev.sum()), "port", {}
+        sample = (f"CPU restatement (the reference engine could not be built), {NTRAJ} "
+                  f"trajectories x {K} output intervals from t = 0")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": K, "warmup": W, "ms_per_step": events / rate * 1e3 / K if rate else None,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "int32 counts, f32 propensities, f64 clock", "data": "synthetic",
-        "config": config_dict(sc),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": int(used), "kind": "port",
+        "dtype": "int32 counts, f64 propensities and clock (reference engine)",
+        "data": "synthetic", "config": config_dict(sc),
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": int(used), "kind": kind,
                          "sample": sample},
-        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    line.update(extra)
+    return line
 
 
 B_SDPD = 200   # algorithmic bytes per particle-step (state r/w, cell key, D_ij row)

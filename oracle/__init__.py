@@ -35,10 +35,25 @@ def build(quiet: bool = True) -> str:
     return LIB
 
 
+def reference_root() -> str | None:
+    """Where the reference SpatialPy package lies: $SPATIALPY_REFERENCE, else
+    its pip install in baseline/_ref (which carries the engine's C++ sources);
+    None when neither holds a spatialpy/ directory."""
+    for r in (os.environ.get("SPATIALPY_REFERENCE"),
+              os.path.join(os.path.dirname(HERE), "baseline", "_ref")):
+        if r and os.path.isdir(os.path.join(r, "spatialpy")):
+            return r
+    return None
+
+
 def build_reference() -> bool:
     """Build oracle/_ref from the reference sources; False when they are absent."""
+    root = reference_root()
+    if root is None:
+        return False
     script = os.path.join(HERE, "build_ref.sh")
-    out = subprocess.run(["bash", script], capture_output=True, text=True)
+    out = subprocess.run(["bash", script], capture_output=True, text=True,
+                         env=dict(os.environ, SPATIALPY_REFERENCE=root))
     return out.returncode == 0
 
 
@@ -272,6 +287,8 @@ def ref_lib(variant: str = ""):
                                 _p(C.c_int64)]
         L.spref_sdpd.argtypes = [_p(SpScenario), C.c_int32, _p(C.c_double), _p(C.c_double),
                                  _p(C.c_double)]
+        L.spref_nsm_bench.argtypes = [_p(SpScenario), _p(C.c_uint32), C.c_uint64, C.c_int32,
+                                      _p(C.c_int64), _p(C.c_double)]
         _ref[variant] = L
     return _ref[variant]
 
@@ -302,6 +319,42 @@ def ref_nsm(sc, seed: int, variant: str = "", u0=None):
     if rc != 0:
         raise RuntimeError(f"reference NSM failed ({rc})")
     return out, ev
+
+
+def _ref_bench_worker(args):
+    sc, seeds, timed_from, variant = args
+    L = ref_lib(variant)
+    s = scenario_struct(sc)
+    u0 = np.ascontiguousarray(sc.u0, np.uint32)
+    events, seconds = 0, 0.0
+    for seed in seeds:
+        ev = np.zeros(2, np.int64)
+        sec = C.c_double(0.0)
+        rc = L.spref_nsm_bench(C.byref(s), _ptr(u0, C.c_uint32), int(seed), timed_from,
+                               _ptr(ev, C.c_int64), C.byref(sec))
+        if rc != 0:
+            raise RuntimeError(f"reference NSM failed ({rc})")
+        events += int(ev.sum())
+        seconds += sec.value
+    return events, seconds
+
+
+def ref_nsm_bench(sc, seeds, timed_from: int, variant: str = "_exact", processes: int = 0):
+    """All-core throughput of the compiled reference engine on a static
+    domain.  The engine keeps global state (its mt19937_64 and the driver's
+    tables), so trajectories run one at a time per process, spread over
+    `processes` spawn-started processes (0 = every host core).  Each process
+    times the event loop of steps [timed_from, nt) of its trajectories; the
+    processes run side by side, so the all-core rate is the sum of their
+    rates.  Returns (events/s, events timed, processes)."""
+    import multiprocessing as mp
+    seeds = np.asarray(seeds, np.uint64)
+    processes = min(processes or os.cpu_count() or 1, len(seeds))
+    chunks = [c for c in np.array_split(seeds, processes) if len(c)]
+    with mp.get_context("spawn").Pool(len(chunks)) as pool:
+        res = pool.map(_ref_bench_worker, [(sc, c, timed_from, variant) for c in chunks])
+    rate = sum(ev / sec for ev, sec in res if sec > 0)
+    return rate, sum(ev for ev, _ in res), len(chunks)
 
 
 def ref_sdpd(sc, nsteps: int):

@@ -1,6 +1,6 @@
 #!/usr/bin/env bash
 # TEST INFRASTRUCTURE (oracle).  Builds the UNMODIFIED SpatialPy C++ engine
-# from its sources where they lie under the reference checkout, together with
+# from its sources where they lie under the reference package, together with
 # oracle/ref_driver.cpp, into oracle/_ref/ (git-ignored):
 #   libspref.so        stock engine (-O2)
 #   libspref_exact.so  same, with the two selection lines of
@@ -12,7 +12,8 @@
 # fields deterministic (particle.cpp:70-83).  Needs g++ only (no SCons).
 set -euo pipefail
 here="$(cd "$(dirname "$0")" && pwd)"
-ref="${SPATIALPY_REFERENCE:-/root/reference}"
+# the reference checkout, or its pip install in baseline/_ref (same layout)
+ref="${SPATIALPY_REFERENCE:-$here/../baseline/_ref}"
 eng="$ref/spatialpy/solvers/c_base/ssa_sdpd-c-simulation-engine"
 out="$here/_ref"
 if [ ! -d "$eng/src" ]; then
@@ -20,6 +21,17 @@ if [ ! -d "$eng/src" ]; then
   exit 2
 fi
 mkdir -p "$out"
+# nothing to do when every library is newer than the driver, this recipe and the ABI header
+stale=0
+for v in "" _exact _O0; do
+  lib="$out/libspref$v.so"
+  if [ ! -f "$lib" ] || [ "$here/ref_driver.cpp" -nt "$lib" ] || [ "$0" -nt "$lib" ] ||
+     [ "$here/../include/spgpu.h" -nt "$lib" ]; then stale=1; fi
+done
+if [ "$stale" = 0 ] && [ "${1:-}" != "--force" ]; then
+  echo "up to date: $(ls "$out"/*.so | xargs -n1 basename | tr '\n' ' ')"
+  exit 0
+fi
 core="count_cores model NRMConstant_v5 output particle pthread_barrier simulate simulate_threads"
 ann="ANN brute kd_tree kd_util kd_split kd_dump kd_search kd_pr_search kd_fix_rad_search bd_tree bd_search bd_pr_search bd_fix_rad_search perf"
 inc="-I$eng/include -I$eng/external/ANN/include -I$here/../include"

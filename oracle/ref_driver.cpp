@@ -15,6 +15,7 @@
  * thread: per step buildKDTree, take_step substeps 0,1,2 over all particles
  * in vector order, then simulate_rdme.
  */
+#include <chrono>
 #include <cstdint>
 #include <cstring>
 #include <cstdio>
@@ -249,6 +250,47 @@ int spref_nsm(const sp_scenario *sc, const uint32_t *u0, uint64_t seed, int32_t 
     }
     counters[0] = sys->total_reactions;
     counters[1] = sys->total_diffusion;
+    return SP_OK;
+}
+
+/*
+ * CPU baseline: one static-domain NSM trajectory of the unmodified engine,
+ * timing only the event loop (simulate_rdme of simulate_rdme.cpp:53-68,
+ * i.e. nsm_core__take_step) over steps [timed_from, nt).  The set-up
+ * (particles, kd-tree, neighbour lists, initialize_rdme, the first queue
+ * build) and the untimed steps before timed_from are excluded, as the GPU
+ * figure excludes them.  counters: (reactions, diffusions) in the timed
+ * steps; *seconds: their wall time (steady clock).
+ */
+int spref_nsm_bench(const sp_scenario *sc, const uint32_t *u0, uint64_t seed, int32_t timed_from,
+                    int64_t *counters, double *seconds) {
+    Built b;
+    int rc = build(sc, b, 1);
+    if (rc) return rc;
+    ParticleSystem *sys = b.sys;
+    if (!sys->static_domain) return SP_E_UNSUPPORTED;
+    if (timed_from < 1 || timed_from >= (int)sc->num_steps) return SP_E_INVALID;
+    const int S = sc->num_species, N = sc->num_particles;
+    b.u0.assign(u0, u0 + (size_t)N * S);
+    rng = std::mt19937_64(seed);
+    initialize_rdme(sys, b.irN.data(), b.jcN.data(), b.prN.data(), b.irG.data(), b.jcG.data(),
+                    b.u0.data());
+    buildKDTree(sys);
+    for (auto &p : sys->particles) p.find_neighbors(sys);
+    long long r0 = 0, d0 = 0;
+    auto t0 = std::chrono::steady_clock::now();
+    for (sys->current_step = 0; sys->current_step < sys->nt; sys->current_step++) {
+        if ((int)sys->current_step == timed_from) {
+            r0 = sys->total_reactions;
+            d0 = sys->total_diffusion;
+            t0 = std::chrono::steady_clock::now();
+        }
+        simulate_rdme(sys, sys->current_step);
+    }
+    const auto t1 = std::chrono::steady_clock::now();
+    counters[0] = sys->total_reactions - r0;
+    counters[1] = sys->total_diffusion - d0;
+    *seconds = std::chrono::duration<double>(t1 - t0).count();
     return SP_OK;
 }
 
