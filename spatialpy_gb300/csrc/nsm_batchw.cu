@@ -8,14 +8,20 @@
 //
 //  1. candidates: warp 0 walks the shared-memory tree down to level 2; the
 //     level-2 frontier (up to 32*W nodes) is expanded by all warps, one node
-//     per lane; the level-1 nodes below the horizon are gathered, one per
-//     thread, and sorted by (time, voxel) with a CTA-wide bitonic network
-//     (shuffles within a warp, shared memory across warps).
+//     per lane, into the leaf groups whose minimum lies below the horizon;
+//     each such group's 32 leaf times are scanned by one thread, and EVERY
+//     leaf below the horizon is a candidate (a group's runner-up included).
+//     The candidates are sorted by (time, voxel) with a CTA-wide bitonic
+//     network (shuffles within a warp, shared memory across warps).
 //  2. thread g executes candidate g as event number n+g.
-//  3. the accepted prefix: time bounds by prefix minima (warp shuffles, then
-//     the minima of earlier warps); voxel conflicts through a hashed table of
-//     the smallest candidate index touching each voxel (a collision only
-//     rejects more, which is safe: a rejected event is redone later).
+//  3. the accepted prefix: time bounds by prefix minima of the redrawn times
+//     (warp shuffles, then the minima of earlier warps); voxel conflicts
+//     through a hashed table of the smallest candidate index touching each
+//     voxel.  No leaf outside the candidates lies below the horizon, so no
+//     group bound cuts the prefix: with group minima as candidates a group's
+//     runner-up had to stay above every later candidate, which cut batches
+//     near the birthday bound of the 2,000 groups (about 48 events of 128);
+//     with leaves only the 64,000 voxels' conflicts and redrawn times do.
 //  4. accepted events are written, their voxel groups rescanned, and the
 //     tree repaired level by level, one thread per changed node.
 //
@@ -61,9 +67,10 @@ static size_t batchw_smem_bytes(const NsmInstance& d, int W) {
     b += 2 * (size_t)(64 * W) * 4;             // frontiers
     b += (NN - N1) * 4;                        // repair flags, levels >= 2
     b += (size_t)kHash * 8;                    // conflict table: keys, values
-    b += (size_t)(32 * W) * 4;                 // candidate list
+    b += (size_t)(32 * W) * 4;                 // candidate groups
     b = (b + 15) / 16 * 16;
     b += 2 * (size_t)(32 * W) * 12;            // sort exchange, double-buffered
+    b += (size_t)(32 * W) * 12;                // candidate leaves: times, voxels
     return (b + 15) / 16 * 16;
 }
 
@@ -121,6 +128,8 @@ __global__ void __launch_bounds__(32 * W, 1)
         unsigned char* xb = (unsigned char*)(((uintptr_t)(clist + NC) + 15) & ~(uintptr_t)15);
         long long* xt = (long long*)xb;            // [2][NC]
         int* xi = (int*)(xt + 2 * NC);             // [2][NC]
+        long long* lt = (long long*)(xi + 2 * NC); // [NC] candidate leaf times
+        int* lv = (int*)(lt + NC);                 // [NC] candidate voxels
         const int flg_base = I.level_off[2];
         for (int e = tid; e < NN - N1; e += NC) flg[e] = 0;
         for (int e = tid; e < kHash; e += NC) { hkey[e] = -1; hval[e] = INT_MAX; }
@@ -249,17 +258,59 @@ __global__ void __launch_bounds__(32 * W, 1)
                         for (unsigned m = mask; m; m &= m - 1) clist[pos++] = base + __ffs(m) - 1;
                     }
                     __syncthreads();
-                    if (got > NC) {
+                    // level 1 -> leaves: group clist[tid] per thread, its 32
+                    // leaf times (16-byte loads; padded leaves hold infinity)
+                    int lgot = NC + 1;
+                    if (got <= NC) {
+                        unsigned lm = 0u;
+                        int gb = 0;
+                        if (tid < got) {
+                            gb = clist[tid] * 32;
+                            const longlong2* lp = (const longlong2*)(LF + gb);
+#pragma unroll
+                            for (int q = 0; q < 16; q++) {
+                                const longlong2 u = lp[q];
+                                lm |= (unsigned)(u.x < thb) << (2 * q);
+                                lm |= (unsigned)(u.y < thb) << (2 * q + 1);
+                            }
+                        }
+                        const int nl = __popc(lm);
+                        int li = nl;
+#pragma unroll
+                        for (int o = 1; o < 32; o <<= 1) {
+                            const int u = __shfl_up_sync(SP_FULL, li, o);
+                            if (lane >= o) li += u;
+                        }
+                        if (lane == 31) s_wcnt[wid] = li;
+                        __syncthreads();
+                        int lbase = 0;
+                        lgot = 0;
+#pragma unroll
+                        for (int u = 0; u < W; u++) {
+                            if (u < wid) lbase += s_wcnt[u];
+                            lgot += s_wcnt[u];
+                        }
+                        if (lgot <= NC) {
+                            int pos = lbase + li - nl;
+                            for (unsigned m = lm; m; m &= m - 1) {
+                                const int e = gb + __ffs(m) - 1;
+                                lt[pos] = LF[e];
+                                lv[pos] = e;
+                                pos++;
+                            }
+                        }
+                        __syncthreads();
+                    }
+                    if (lgot > NC) {
                         if (bsc > 1.0f) { bsc *= 0.5f; continue; }
                         count = 1;        // degenerate: the minimum alone
                         ct = tid == 0 ? rt : SP_INF_BITS;
                         ci = tid == 0 ? ri : INT_MAX;
                     } else {
-                        count = got;
-                        if (tid < got) {
-                            const int node = clist[tid];
-                            ct = NT[off1 + node];
-                            ci = NI[off1 + node];
+                        count = lgot;
+                        if (tid < count) {
+                            ct = lt[tid];
+                            ci = lv[tid];
                         }
                         // bitonic sort of NC keys (t, i), ascending
 #pragma unroll
@@ -290,7 +341,8 @@ __global__ void __launch_bounds__(32 * W, 1)
                             }
                         }
                     }
-                    ct2 = tid < count ? T2[ci >> 5] : SP_INF_BITS;
+                    // every leaf below the horizon is a candidate: no group bound
+                    ct2 = SP_INF_BITS;
                     if (count >= 28 * W) bsc = bsc * 0.8f;
                     else if (count < 16 * W && bsc < 64.0f * W) bsc = bsc * 1.25f;
                 }
