@@ -8,11 +8,13 @@
 //
 //  1. candidates: warp 0 walks the shared-memory tree down to level 2; the
 //     level-2 frontier (up to 32*W nodes) is expanded by all warps, one node
-//     per lane, into the leaf groups whose minimum lies below the horizon;
-//     each such group's 32 leaf times are scanned by one thread, and EVERY
-//     leaf below the horizon is a candidate (a group's runner-up included).
-//     The candidates are sorted by (time, voxel) with a CTA-wide bitonic
-//     network (shuffles within a warp, shared memory across warps).
+//     per lane, into the leaf groups whose minimum lies below the horizon,
+//     and EVERY leaf below the horizon is a candidate (a group's runner-up
+//     included).  Each group's minimum, runner-up (time and voxel) and third
+//     smallest time are kept in shared memory, so a group's 32 leaf times
+//     are read from global memory only when three or more of them lie below
+//     the horizon.  The candidates are ordered by rank: thread g counts the
+//     candidates whose (time, voxel) key is smaller than its own.
 //  2. thread g executes candidate g as event number n+g.
 //  3. the accepted prefix: time bounds by prefix minima of the redrawn times
 //     (warp shuffles, then the minima of earlier warps); voxel conflicts
@@ -22,8 +24,9 @@
 //     runner-up had to stay above every later candidate, which cut batches
 //     near the birthday bound of the 2,000 groups (about 48 events of 128);
 //     with leaves only the 64,000 voxels' conflicts and redrawn times do.
-//  4. accepted events are written, their voxel groups rescanned, and the
-//     tree repaired level by level, one thread per changed node.
+//  4. accepted events are written and, after a CTA barrier (a group may
+//     hold several accepted events), their voxel groups rescanned; then the
+//     tree is repaired level by level, one thread per changed node.
 //
 // Scalars that steer the loop (clock, counters, running propensity total)
 // are kept in every thread and updated from the same shared values in the
@@ -61,9 +64,95 @@ __device__ __forceinline__ int ctab_find(const int* key, int v) {
     return -1;
 }
 
+// The three smallest leaf times of a group and the voxels of the first two,
+// ordered by (time, voxel).
+struct Top3 {
+    long long t0, t1, t2;
+    int i0, i1;
+};
+
+__device__ __forceinline__ Top3 merge3(const Top3& a, const Top3& b) {
+    const bool fa = kless(a.t0, a.i0, b.t0, b.i0);
+    Top3 r;
+    r.t0 = fa ? a.t0 : b.t0;
+    r.i0 = fa ? a.i0 : b.i0;
+    const long long ha = fa ? a.t1 : a.t0, hb = fa ? b.t0 : b.t1;   // the lists' next heads
+    const int hai = fa ? a.i1 : a.i0, hbi = fa ? b.i0 : b.i1;
+    const long long na = fa ? a.t2 : a.t1, nb = fa ? b.t1 : b.t2;   // and the items after them
+    const bool fs = kless(ha, hai, hb, hbi);
+    r.t1 = fs ? ha : hb;
+    r.i1 = fs ? hai : hbi;
+    const long long c1 = fs ? na : ha, c2 = fs ? hb : nb;
+    r.t2 = c1 < c2 ? c1 : c2;
+    return r;
+}
+
+// 16 leaves (8 aligned pairs) starting at leaf `base`
+__device__ __forceinline__ Top3 top3_half(const longlong2* p, int base) {
+    Top3 v[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        const longlong2 u = p[q];
+        const bool a = u.x <= u.y;               // ties: the lower index first
+        v[q].t0 = a ? u.x : u.y;
+        v[q].t1 = a ? u.y : u.x;
+        v[q].t2 = SP_INF_BITS;
+        v[q].i0 = a ? base + 2 * q : base + 2 * q + 1;
+        v[q].i1 = a ? base + 2 * q + 1 : base + 2 * q;
+    }
+#pragma unroll
+    for (int w = 4; w >= 1; w >>= 1)
+#pragma unroll
+        for (int q = 0; q < w; q++) v[q] = merge3(v[q], v[q + w]);
+    return v[0];
+}
+
+// Level-1 node g (the group's minimum), its runner-up time T2 (as the other
+// kernels keep it) and voxel I2, and its third-smallest time T3, from the
+// group's 32 leaf times.
+__device__ __forceinline__ void rescan3(const NsmInstance& I, const long long* LF, long long* NT,
+                                        int* NI, long long* T2, int* I2, long long* T3, int g) {
+    const longlong2* p = (const longlong2*)(LF + (size_t)g * 32);
+    const Top3 a = top3_half(p, g * 32);
+    const Top3 b = top3_half(p + 8, g * 32 + 16);
+    const Top3 r = merge3(a, b);
+    NT[I.level_off[1] + g] = r.t0;
+    NI[I.level_off[1] + g] = r.i0;
+    T2[g] = r.t1;
+    I2[g] = r.i1;
+    T3[g] = r.t2;
+}
+
+// rescan3 of groups ga and gb (gb < 0: none) with both groups' leaf loads in
+// flight together
+__device__ __forceinline__ void rescan3_pair(const NsmInstance& I, const long long* LF,
+                                             long long* NT, int* NI, long long* T2, int* I2,
+                                             long long* T3, int ga, int gb) {
+    const int gq = gb >= 0 ? gb : ga;
+    const longlong2* pa = (const longlong2*)(LF + (size_t)ga * 32);
+    const longlong2* pb = (const longlong2*)(LF + (size_t)gq * 32);
+    const Top3 a0 = top3_half(pa, ga * 32), b0 = top3_half(pb, gq * 32);
+    const Top3 a1 = top3_half(pa + 8, ga * 32 + 16), b1 = top3_half(pb + 8, gq * 32 + 16);
+    const Top3 ra = merge3(a0, a1), rb = merge3(b0, b1);
+    const int off1 = I.level_off[1];
+    NT[off1 + ga] = ra.t0;
+    NI[off1 + ga] = ra.i0;
+    T2[ga] = ra.t1;
+    I2[ga] = ra.i1;
+    T3[ga] = ra.t2;
+    if (gb >= 0) {
+        NT[off1 + gb] = rb.t0;
+        NI[off1 + gb] = rb.i0;
+        T2[gb] = rb.t1;
+        I2[gb] = rb.i1;
+        T3[gb] = rb.t2;
+    }
+}
+
 static size_t batchw_smem_bytes(const NsmInstance& d, int W) {
     const size_t NN = d.num_nodes, N1 = d.level_size[1];
     size_t b = NN * 8 + N1 * 8 + NN * 4;      // tree times, second minima, indices
+    b += N1 * 12;                              // third minima, runner-up voxels
     b += 2 * (size_t)(64 * W) * 4;             // frontiers
     b += (NN - N1) * 4;                        // repair flags, levels >= 2
     b += (size_t)kHash * 8;                    // conflict table: keys, values
@@ -118,8 +207,10 @@ __global__ void __launch_bounds__(32 * W, 1)
         // shared-memory layout (batchw_smem_bytes)
         long long* NT = (long long*)smem;
         long long* T2 = NT + NN;
-        int* NI = (int*)(T2 + N1);
-        int* fa = NI + NN;
+        long long* T3 = T2 + N1;                   // third-smallest leaf time per group
+        int* NI = (int*)(T3 + N1);
+        int* I2 = NI + NN;                         // runner-up voxel per group
+        int* fa = I2 + N1;
         int* fb = fa + 64 * W;
         int* flg = fb + 64 * W;
         int* hkey = flg + (NN - N1);
@@ -134,7 +225,10 @@ __global__ void __launch_bounds__(32 * W, 1)
         for (int e = tid; e < NN - N1; e += NC) flg[e] = 0;
         for (int e = tid; e < kHash; e += NC) { hkey[e] = -1; hval[e] = INT_MAX; }
         for (int e = tid; e < NN; e += NC) { NT[e] = T.node_t[e]; NI[e] = T.node_i[e]; }
-        for (int e = tid; e < N1; e += NC) T2[e] = T.node_t2[e];
+        __syncthreads();
+        // level 1 with runner-ups and third minima from the leaves (the
+        // other event kernels keep only the runner-up times)
+        for (int g = tid; g < N1; g += NC) rescan3(I, T.leaf, NT, NI, T2, I2, T3, g);
         __syncthreads();
         long long* LF = T.leaf;
         int32_t* X = T.x;
@@ -152,7 +246,6 @@ __global__ void __launch_bounds__(32 * W, 1)
         asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_start));
         long long rt = NT[I.level_off[L]];
         int ri = NI[I.level_off[L]];
-        int xbuf = 0;
         while (step < step_end && status == SP_TRAJ_OK) {
             const double t_end = dt * (double)step + dt;   // simulate_rdme.cpp:67, 215
             const long long t_end_bits = __double_as_longlong(t_end);
@@ -258,23 +351,32 @@ __global__ void __launch_bounds__(32 * W, 1)
                         for (unsigned m = mask; m; m &= m - 1) clist[pos++] = base + __ffs(m) - 1;
                     }
                     __syncthreads();
-                    // level 1 -> leaves: group clist[tid] per thread, its 32
-                    // leaf times (16-byte loads; padded leaves hold infinity)
+                    // level 1 -> leaves: group clist[tid] per thread.  Its
+                    // minimum is below the horizon; its runner-up too when
+                    // T2 < horizon; only when T3 < horizon are its 32 leaf
+                    // times read (16-byte loads; padded leaves hold infinity)
                     int lgot = NC + 1;
                     if (got <= NC) {
                         unsigned lm = 0u;
-                        int gb = 0;
+                        int gb = 0, g = -1, nl = 0;
+                        bool scan = false;
                         if (tid < got) {
-                            gb = clist[tid] * 32;
-                            const longlong2* lp = (const longlong2*)(LF + gb);
+                            g = clist[tid];
+                            gb = g * 32;
+                            if (T3[g] < thb) {
+                                scan = true;
+                                const longlong2* lp = (const longlong2*)(LF + gb);
 #pragma unroll
-                            for (int q = 0; q < 16; q++) {
-                                const longlong2 u = lp[q];
-                                lm |= (unsigned)(u.x < thb) << (2 * q);
-                                lm |= (unsigned)(u.y < thb) << (2 * q + 1);
+                                for (int q = 0; q < 16; q++) {
+                                    const longlong2 u = lp[q];
+                                    lm |= (unsigned)(u.x < thb) << (2 * q);
+                                    lm |= (unsigned)(u.y < thb) << (2 * q + 1);
+                                }
+                                nl = __popc(lm);
+                            } else {
+                                nl = T2[g] < thb ? 2 : 1;
                             }
                         }
-                        const int nl = __popc(lm);
                         int li = nl;
 #pragma unroll
                         for (int o = 1; o < 32; o <<= 1) {
@@ -290,13 +392,22 @@ __global__ void __launch_bounds__(32 * W, 1)
                             if (u < wid) lbase += s_wcnt[u];
                             lgot += s_wcnt[u];
                         }
-                        if (lgot <= NC) {
+                        if (lgot <= NC && tid < got) {
                             int pos = lbase + li - nl;
-                            for (unsigned m = lm; m; m &= m - 1) {
-                                const int e = gb + __ffs(m) - 1;
-                                lt[pos] = LF[e];
-                                lv[pos] = e;
-                                pos++;
+                            if (scan) {
+                                for (unsigned m = lm; m; m &= m - 1) {
+                                    const int e = gb + __ffs(m) - 1;
+                                    lt[pos] = LF[e];
+                                    lv[pos] = e;
+                                    pos++;
+                                }
+                            } else {
+                                lt[pos] = NT[off1 + g];
+                                lv[pos] = NI[off1 + g];
+                                if (nl == 2) {
+                                    lt[pos + 1] = T2[g];
+                                    lv[pos + 1] = I2[g];
+                                }
                             }
                         }
                         __syncthreads();
@@ -312,44 +423,36 @@ __global__ void __launch_bounds__(32 * W, 1)
                             ct = lt[tid];
                             ci = lv[tid];
                         }
-                        // bitonic sort of NC keys (t, i), ascending
-#pragma unroll
-                        for (int k = 2; k <= NC; k <<= 1) {
-#pragma unroll
-                            for (int jj = k >> 1; jj > 0; jj >>= 1) {
-                                long long pt;
-                                int pi;
-                                if (jj >= 32) {
-                                    xt[xbuf * NC + tid] = ct;
-                                    xi[xbuf * NC + tid] = ci;
-                                    __syncthreads();
-                                    pt = xt[xbuf * NC + (tid ^ jj)];
-                                    pi = xi[xbuf * NC + (tid ^ jj)];
-                                    xbuf ^= 1;
-                                } else {
-                                    pt = __shfl_xor_sync(SP_FULL, ct, jj);
-                                    pi = __shfl_xor_sync(SP_FULL, ci, jj);
-                                }
-                                const bool up = (tid & k) == 0;
-                                const bool lower = (tid & jj) == 0;
-                                const bool take = (lower == up) ? kless(pt, pi, ct, ci)
-                                                                : kless(ct, ci, pt, pi);
-                                if (take) {
-                                    ct = pt;
-                                    ci = pi;
-                                }
-                            }
+                        // order by rank: keys are distinct (one per voxel)
+                        int rank = 0;
+                        if (tid < count)
+                            for (int j = 0; j < count; j++) rank += kless(lt[j], lv[j], ct, ci);
+                        if (tid < count) {
+                            xt[rank] = ct;
+                            xi[rank] = ci;
+                        }
+                        __syncthreads();
+                        if (tid < count) {
+                            ct = xt[tid];
+                            ci = xi[tid];
                         }
                     }
                     // every leaf below the horizon is a candidate: no group bound
                     ct2 = SP_INF_BITS;
-                    if (count >= 28 * W) bsc = bsc * 0.8f;
-                    else if (count < 16 * W && bsc < 64.0f * W) bsc = bsc * 1.25f;
+                    if (count >= 30 * W) bsc = bsc * 0.8f;
+                    else if (count < 24 * W && bsc < 64.0f * W) bsc = bsc * 1.25f;
                 }
                 stat_b++;
                 stat_c += count;
                 // ---- 2. speculative execution, one candidate per thread -------
                 const bool act = tid < count;
+                if (act) {
+                    // the source's leaf group, read again by the rescan after the
+                    // commit: start bringing its two lines into L1 now
+                    const long long* gp = LF + (size_t)(ci >> 5) * 32;
+                    asm volatile("prefetch.global.L1 [%0];" ::"l"(gp));
+                    asm volatile("prefetch.global.L1 [%0];" ::"l"(gp + 16));
+                }
                 Cand<MS> Cd;
                 batch_execute<REF, MS, MR, EX>(I, Q, X, act, ci, ct, evn + (uint64_t)tid, T.key0,
                                                T.key1, Cd);
@@ -433,9 +536,12 @@ __global__ void __launch_bounds__(32 * W, 1)
                 }
                 if (m > 0 && tid == m - 1) s_tl = ct;
                 // ---- 5. rescan and tree repair ------------------------------------
+                // a group may hold several accepted events: every commit is
+                // stored before any rescan reads the group
+                __syncthreads();
                 const int gv = v >> 5;
                 const int gw = (w >= 0 && (w >> 5) != gv) ? w >> 5 : -1;
-                if (acc) lane_rescan2(I, LF, NT, NI, T2, gv, gw);
+                if (acc) rescan3_pair(I, LF, NT, NI, T2, I2, T3, gv, gw);
                 __syncthreads();
 #pragma unroll
                 for (int u = 0; u < W; u++) {
