@@ -289,6 +289,12 @@ def ref_lib(variant: str = ""):
                                  _p(C.c_double)]
         L.spref_nsm_bench.argtypes = [_p(SpScenario), _p(C.c_uint32), C.c_uint64, C.c_int32,
                                       _p(C.c_int64), _p(C.c_double)]
+        L.spref_chem.argtypes = [_p(SpScenario), _p(C.c_uint32), _p(C.c_double)]
+        L.spref_coupled.argtypes = [_p(SpScenario), _p(C.c_uint32), C.c_uint64, _p(C.c_int32),
+                                    _p(C.c_int64)]
+        L.spref_vtk_run.argtypes = [_p(SpScenario), _p(C.c_uint32), C.c_uint64,
+                                    _p(C.c_char_p), C.c_char_p] + [_p(C.c_double)] * 5 + \
+            [_p(C.c_int32), _p(C.c_double)]
         _ref[variant] = L
     return _ref[variant]
 
@@ -355,6 +361,53 @@ def ref_nsm_bench(sc, seeds, timed_from: int, variant: str = "_exact", processes
         res = pool.map(_ref_bench_worker, [(sc, c, timed_from, variant) for c in chunks])
     rate = sum(ev / sec for ev, sec in res if sec > 0)
     return rate, sum(ev for ev, _ in res), len(chunks)
+
+
+def ref_chem(sc, u0=None):
+    """The reference's deterministic chemistry: concentrations [T, N, S] at
+    the output steps."""
+    u0 = np.ascontiguousarray(sc.u0 if u0 is None else u0, np.uint32)
+    s = scenario_struct(sc)
+    out = np.zeros((len(sc.output_steps), sc.num_particles, sc.num_species))
+    rc = ref_lib().spref_chem(C.byref(s), _ptr(u0, C.c_uint32), _ptr(out, C.c_double))
+    if rc != 0:
+        raise RuntimeError(f"reference chemistry failed ({rc})")
+    return out
+
+
+def ref_coupled(sc, seed: int, variant: str = "", u0=None):
+    """One moving-domain trajectory of the reference engine (flow + species):
+    counts [T, N, S] at the output steps and (reactions, diffusions)."""
+    u0 = np.ascontiguousarray(sc.u0 if u0 is None else u0, np.uint32)
+    s = scenario_struct(sc)
+    out = np.zeros((len(sc.output_steps), sc.num_particles, sc.num_species), np.int32)
+    ev = np.zeros(2, np.int64)
+    rc = ref_lib(variant).spref_coupled(C.byref(s), _ptr(u0, C.c_uint32), seed,
+                                        _ptr(out, C.c_int32), _ptr(ev, C.c_int64))
+    if rc != 0:
+        raise RuntimeError(f"reference coupled run failed ({rc})")
+    return out, ev
+
+
+def ref_vtk_run(sc, seed: int, names, directory, variant: str = ""):
+    """Runs the engine loop with the engine's own VTK writer into `directory`
+    (outputN.vtk, N counting this process's files) and returns the state at
+    each output: dict of x, v [T,N,3], rho, bvf_phi, nu [T,N], counts and
+    chem [T,N,S]."""
+    u0 = np.ascontiguousarray(sc.u0, np.uint32)
+    s = scenario_struct(sc)
+    T, n, S = len(sc.output_steps), sc.num_particles, sc.num_species
+    r = {"x": np.zeros((T, n, 3)), "v": np.zeros((T, n, 3)), "rho": np.zeros((T, n)),
+         "bvf_phi": np.zeros((T, n)), "nu": np.zeros((T, n)),
+         "counts": np.zeros((T, n, S), np.int32), "chem": np.zeros((T, n, S))}
+    cnames = (C.c_char_p * max(S, 1))(*[nm.encode() for nm in names])
+    rc = ref_lib(variant).spref_vtk_run(
+        C.byref(s), _ptr(u0, C.c_uint32), seed, cnames, os.fsencode(directory),
+        *[_ptr(r[k], C.c_double) for k in ("x", "v", "rho", "bvf_phi", "nu")],
+        _ptr(r["counts"], C.c_int32), _ptr(r["chem"], C.c_double))
+    if rc != 0:
+        raise RuntimeError(f"reference VTK run failed ({rc})")
+    return r
 
 
 def ref_sdpd(sc, nsteps: int):

@@ -3,9 +3,15 @@
 # from its sources where they lie under the reference package, together with
 # oracle/ref_driver.cpp, into oracle/_ref/ (git-ignored):
 #   libspref.so        stock engine (-O2)
-#   libspref_exact.so  same, with the two selection lines of
-#                      src/simulate_rdme.cpp:260,317 rescaled (a patched copy
-#                      written into oracle/_ref/, never into the repository)
+#   libspref_exact.so  the exact SSA that SP_SELECT_EXACT runs: the same
+#                      engine with the two selection lines of
+#                      src/simulate_rdme.cpp:260,317 rescaled, no event past
+#                      the step end (the loop of :233-238 returns when the
+#                      selected time lies beyond it; selectReaction only
+#                      peeks), and a diffusion destination's reactions
+#                      evaluated with its own volume (:431-433) (a patched
+#                      copy written into oracle/_ref/, never into the
+#                      repository)
 #   libspref_O0.so     stock engine at -O0, as the shipped SCons build compiles it
 # File lists follow src/SConscript:2-12 and external/ANN/src/SConscript:2-17.
 # -ftrivial-auto-var-init=zero makes the engine's uninitialised step-0 particle
@@ -58,9 +64,13 @@ build_variant() {  # $1 = suffix, $2 = optimisation flag, $3 = simulate_rdme sou
 # exact-selection twin: rescale the reused uniform (rand1) to the chosen class
 sed -e 's/double rand_rval = rand1 \* subvol->srrate;/double rand_rval = rand1 * totrate;/' \
     -e 's/double diff_rand = rand1 \* subvol->sdrate;/double diff_rand = rand1 * totrate - subvol->srrate;/' \
+    -e 's|(dest_subvol->xx,tt,vol,dest_subvol->data_fn,dest_subvol->type)|(dest_subvol->xx,tt,dest_subvol->mass / dest_subvol->rho,dest_subvol->data_fn,dest_subvol->type)|' \
+    -e 's|subvol_index = timeRxnPair.second;|subvol_index = timeRxnPair.second; if (tt > end_time) return;|' \
     "$eng/src/simulate_rdme.cpp" > "$out/simulate_rdme_exact.cpp"
 grep -q 'rand_rval = rand1 \* totrate' "$out/simulate_rdme_exact.cpp"
 grep -q 'diff_rand = rand1 \* totrate - subvol->srrate' "$out/simulate_rdme_exact.cpp"
+grep -q '(dest_subvol->xx,tt,dest_subvol->mass / dest_subvol->rho,' "$out/simulate_rdme_exact.cpp"
+grep -q 'subvol_index = timeRxnPair.second; if (tt > end_time) return;' "$out/simulate_rdme_exact.cpp"
 
 build_variant "" "-O2" "$eng/src/simulate_rdme.cpp"
 build_variant "_exact" "-O2" "$out/simulate_rdme_exact.cpp"

@@ -8,14 +8,19 @@
  * It replaces the code that Solver.compile() would generate from
  * propensity_file_template.cpp (main at :101-142): the particle set-up of
  * init_all_particles (:73-90), the mass-action propensity functions
- * (solver.py:344-373 from reaction.py:260-313), get_next_output
- * (solver.py:290-299), an empty applyBoundaryConditions (no BCs), and
- * `rng`/`debug_flag`.  The step loop replays run_simulation
+ * (solver.py:344-373 from reaction.py:260-313), the mass-action ODE rates of
+ * the deterministic chemistry (solver.py:160-190, reaction.py:297-303),
+ * get_next_output (solver.py:290-299), applyBoundaryConditions as
+ * boundarycondition.py:121-167 generates it (one if-block per condition, in
+ * order), and `rng`/`debug_flag`.  The step loop replays run_simulation
  * (src/simulate_threads.cpp:232-281) with one worker thread and no output
  * thread: per step buildKDTree, take_step substeps 0,1,2 over all particles
  * in vector order, then simulate_rdme.
  */
+#include <algorithm>
 #include <chrono>
+#include <climits>
+#include <unistd.h>
 #include <cstdint>
 #include <cstring>
 #include <cstdio>
@@ -26,6 +31,7 @@
 #include "simulate.hpp"
 #include "simulate_rdme.hpp"
 #include "model.hpp"
+#include "output.hpp"
 #include "propensities.hpp"
 #include "spgpu.h"
 
@@ -45,6 +51,10 @@ int g_a[kMaxRxn], g_b[kMaxRxn];
 std::vector<uint8_t> g_allowed;   /* [R*(T+1)] */
 std::vector<unsigned int> g_outsteps;
 size_t g_outidx = 0;
+/* boundary conditions: box [6], type (0 = any), target SP_BC_*, value [3] */
+int g_nbc = 0;
+std::vector<double> g_bc_box, g_bc_val;
+std::vector<int> g_bc_type, g_bc_target;
 
 /* Mass-action propensity with the operator order of the generated C++
  * (e.g. "k_birth*vol", "k*A*B/vol"); x is the engine's unsigned int* xx read
@@ -62,9 +72,28 @@ double massaction(const unsigned int *xu, double, double vol, double *, int sd) 
     }
 }
 
+/* The ODE rate of a mass-action reaction on concentrations, as the
+ * generated det<name> function returns it: "k", "k * A", "k * A * B",
+ * "k * A * A" (reaction.py:297-303), 0 outside restrict_to types. */
+template <int R>
+double chem_massaction(double *x, double, double, double *, int sd) {
+    if (!g_allowed.empty() && !g_allowed[(size_t)R * (g_T + 1) + sd]) return 0.0;
+    const double k = g_k[R];
+    switch (g_kind[R]) {
+        case SP_RXN_ZERO:   return k;
+        case SP_RXN_FIRST:  return k * x[g_a[R]];
+        case SP_RXN_SECOND: return k * x[g_a[R]] * x[g_b[R]];
+        default:            return k * x[g_a[R]] * x[g_a[R]];
+    }
+}
+
 template <int... Is> struct Table {
     static PropensityFun *make() {
         static PropensityFun t[] = {(PropensityFun)&massaction<Is>...};
+        return t;
+    }
+    static ChemRxnFun *make_chem() {
+        static ChemRxnFun t[] = {(ChemRxnFun)&chem_massaction<Is>...};
         return t;
     }
 };
@@ -76,7 +105,26 @@ unsigned int get_next_output(ParticleSystem *) {
     if (g_outidx < g_outsteps.size()) return g_outsteps[g_outidx++];
     return 0xffffffffu;
 }
-void applyBoundaryConditions(Particle *, ParticleSystem *) {}
+void applyBoundaryConditions(Particle *me, ParticleSystem *) {
+    for (int b = 0; b < g_nbc; b++) {
+        const double *bx = &g_bc_box[6 * (size_t)b];
+        if (!(me->x[0] >= bx[0] && me->x[0] <= bx[1] && me->x[1] >= bx[2] && me->x[1] <= bx[3] &&
+              me->x[2] >= bx[4] && me->x[2] <= bx[5]))
+            continue;
+        if (g_bc_type[b] != 0 && me->type != g_bc_type[b]) continue;
+        const double *val = &g_bc_val[3 * (size_t)b];
+        const int tg = g_bc_target[b];
+        if (tg == SP_BC_V) {
+            for (int i = 0; i < 3; i++) me->v[i] = val[i];
+        } else if (tg == SP_BC_NU) {
+            me->nu = val[0];
+        } else if (tg == SP_BC_RHO) {
+            me->rho = val[0];
+        } else {
+            me->C[tg - SP_BC_C] = val[0];
+        }
+    }
+}
 }  // namespace Spatialpy
 
 using namespace Spatialpy;
@@ -106,6 +154,11 @@ int load_network(const sp_scenario *sc) {
     if (sc->rxn_allowed) g_allowed.assign(sc->rxn_allowed, sc->rxn_allowed + (size_t)g_R * (g_T + 1));
     g_outsteps.assign(sc->output_steps, sc->output_steps + sc->num_outputs);
     g_outidx = 0;
+    g_nbc = sc->num_bcs;
+    g_bc_box.assign(sc->bc_box, sc->bc_box + 6 * (size_t)g_nbc);
+    g_bc_val.assign(sc->bc_value, sc->bc_value + 3 * (size_t)g_nbc);
+    g_bc_type.assign(sc->bc_type, sc->bc_type + g_nbc);
+    g_bc_target.assign(sc->bc_target, sc->bc_target + g_nbc);
     return SP_OK;
 }
 
@@ -138,13 +191,18 @@ void dep_graph(const sp_scenario *sc, Built &b) {
     }
 }
 
-int build(const sp_scenario *sc, Built &b, int with_rdme) {
+/* with_chem: the deterministic chemistry on (Model.enable_pde), its
+ * concentrations starting at u0 (propensity_file_template.cpp:77-80). */
+int build(const sp_scenario *sc, Built &b, int with_rdme, const uint32_t *chem_u0 = nullptr) {
     int rc = load_network(sc);
     if (rc) return rc;
     const int S = sc->num_species, R = sc->num_reactions, N = sc->num_particles;
-    b.sys = new ParticleSystem(sc->num_types, 0, 0, with_rdme ? S : 0, with_rdme ? R : 0, 0);
+    const int with_chem = chem_u0 != nullptr;
+    b.sys = new ParticleSystem(sc->num_types, with_chem ? S : 0, with_chem ? R : 0,
+                               with_rdme ? S : 0, with_rdme ? R : 0, 0);
     ParticleSystem *sys = b.sys;
     sys->static_domain = sc->static_domain != 0;
+    sys->initialized = 0;   /* not set by the constructor (particle.cpp:49-58) */
     sys->dt = sc->dt;
     sys->nt = sc->num_steps;
     sys->h = sc->h;
@@ -155,8 +213,16 @@ int build(const sp_scenario *sc, Built &b, int with_rdme) {
     for (int d = 0; d < 3; d++) sys->gravity[d] = sc->gravity[d];
     sys->subdomain_diffusion_matrix = sc->diffusion;
     sys->stoch_rxn_propensity_functions = Gen<kMaxRxn>::type::make();
-    sys->chem_rxn_rhs_functions = nullptr;
+    sys->chem_rxn_rhs_functions = with_chem ? Gen<kMaxRxn>::type::make_chem() : nullptr;
     sys->stoichiometric_matrix = nullptr;
+    if (with_chem) {
+        /* dense [species][reaction], as solver.py:225-231 writes it */
+        b.Ndense.assign((size_t)S * (R > 0 ? R : 1), 0);
+        for (int r = 0; r < R; r++)
+            for (int64_t q = sc->jcN[r]; q < sc->jcN[r + 1]; q++)
+                b.Ndense[(size_t)sc->irN[q] * R + r] += sc->prN[q];
+        sys->stoichiometric_matrix = b.Ndense.data();
+    }
     sys->species_names = nullptr;
     sys->particles.reserve(N);
     for (int i = 0; i < N; i++) {
@@ -174,6 +240,8 @@ int build(const sp_scenario *sc, Built &b, int with_rdme) {
         p.bvf_phi = 0.0;
         p.old_rho = p.rho;
         p.particle_index = (size_t)i;
+        if (with_chem)
+            for (int s2 = 0; s2 < S; s2++) p.C[s2] = (double)chem_u0[(size_t)i * S + s2];
         sys->particles.emplace_back(p);
     }
     if (with_rdme && S > 0) {
@@ -291,6 +359,149 @@ int spref_nsm_bench(const sp_scenario *sc, const uint32_t *u0, uint64_t seed, in
     counters[0] = sys->total_reactions - r0;
     counters[1] = sys->total_diffusion - d0;
     *seconds = std::chrono::duration<double>(t1 - t0).count();
+    return SP_OK;
+}
+
+/*
+ * Deterministic chemistry (Model.enable_pde) on any domain: the engine's
+ * substeps over [0, nt) with the stochastic part off.  out: [num_outputs][N][S]
+ * concentrations C at the output steps.
+ */
+int spref_chem(const sp_scenario *sc, const uint32_t *u0, double *out) {
+    Built b;
+    int rc = build(sc, b, 0, u0);
+    if (rc) return rc;
+    ParticleSystem *sys = b.sys;
+    const int S = sc->num_species, N = sc->num_particles;
+    unsigned int next_output = get_next_output(sys);
+    int oi = 0;
+    auto snap = [&]() {
+        for (int i = 0; i < N; i++)
+            for (int s2 = 0; s2 < S; s2++)
+                out[((size_t)oi * N + i) * S + s2] = sys->particles[i].C[s2];
+        oi++;
+    };
+    for (sys->current_step = 0; sys->current_step < sys->nt; sys->current_step++) {
+        buildKDTree(sys);
+        if (sys->current_step >= next_output && oi < sc->num_outputs) {
+            snap();
+            next_output = get_next_output(sys);
+        }
+        for (unsigned sub = 0; sub < 3; sub++)
+            for (auto &p : sys->particles) take_step(&p, sys, sys->current_step, sub);
+    }
+    while (oi < sc->num_outputs) snap();
+    return SP_OK;
+}
+
+/*
+ * A moving domain with stochastic species: per step the kd-tree, the SDPD
+ * substeps and simulate_rdme, which on a non-static domain rebuilds the
+ * propensities and the queue (simulate_rdme.cpp:53-68).  out:
+ * [num_outputs][N][S] counts at the output steps; counters: (reactions,
+ * diffusions).
+ */
+int spref_coupled(const sp_scenario *sc, const uint32_t *u0, uint64_t seed, int32_t *out,
+                  int64_t *counters) {
+    Built b;
+    int rc = build(sc, b, 1);
+    if (rc) return rc;
+    ParticleSystem *sys = b.sys;
+    if (sys->static_domain) return SP_E_UNSUPPORTED;
+    const int S = sc->num_species, N = sc->num_particles;
+    b.u0.assign(u0, u0 + (size_t)N * S);
+    rng = std::mt19937_64(seed);
+    initialize_rdme(sys, b.irN.data(), b.jcN.data(), b.prN.data(), b.irG.data(), b.jcG.data(),
+                    b.u0.data());
+    unsigned int next_output = get_next_output(sys);
+    int oi = 0;
+    for (sys->current_step = 0; sys->current_step < sys->nt; sys->current_step++) {
+        buildKDTree(sys);
+        if (sys->current_step >= next_output && oi < sc->num_outputs) {
+            std::memcpy(out + (size_t)oi * N * S, b.u0.data(), sizeof(uint32_t) * N * S);
+            oi++;
+            next_output = get_next_output(sys);
+        }
+        for (unsigned sub = 0; sub < 3; sub++)
+            for (auto &p : sys->particles) take_step(&p, sys, sys->current_step, sub);
+        simulate_rdme(sys, sys->current_step);
+    }
+    while (oi < sc->num_outputs) {
+        std::memcpy(out + (size_t)oi * N * S, b.u0.data(), sizeof(uint32_t) * N * S);
+        oi++;
+    }
+    counters[0] = sys->total_reactions;
+    counters[1] = sys->total_diffusion;
+    return SP_OK;
+}
+
+/*
+ * The engine loop of run_simulation (kd-tree, output, substeps 0-2,
+ * simulate_rdme) with the engine's own VTK writer (output.cpp:59-229)
+ * writing outputN.vtk into `dir` at the output steps (N counts the files
+ * this process has written).  The full-precision state at each output goes
+ * to the arrays (any may be NULL): x, v [T][N][3]; rho, bvf_phi, nu [T][N];
+ * counts [T][N][S] (stochastic species) and chem [T][N][S] (with enable_pde).
+ */
+int spref_vtk_run(const sp_scenario *sc, const uint32_t *u0, uint64_t seed,
+                  const char *const *names, const char *dir, double *x, double *v, double *rho,
+                  double *bvf, double *nu, int32_t *counts, double *chem) {
+    Built b;
+    const int S = sc->num_species, N = sc->num_particles;
+    const int rdme = S > 0;
+    int rc = build(sc, b, rdme, sc->enable_pde && S > 0 ? u0 : nullptr);
+    if (rc) return rc;
+    ParticleSystem *sys = b.sys;
+    sys->species_names = names;
+    sys->xlo = sys->ylo = sys->zlo = 1e300;
+    sys->xhi = sys->yhi = sys->zhi = -1e300;
+    for (const auto &p : sys->particles) {
+        sys->xlo = std::min(sys->xlo, p.x[0]); sys->xhi = std::max(sys->xhi, p.x[0]);
+        sys->ylo = std::min(sys->ylo, p.x[1]); sys->yhi = std::max(sys->yhi, p.x[1]);
+        sys->zlo = std::min(sys->zlo, p.x[2]); sys->zhi = std::max(sys->zhi, p.x[2]);
+    }
+    if (rdme) {
+        b.u0.assign(u0, u0 + (size_t)N * S);
+        rng = std::mt19937_64(seed);
+        initialize_rdme(sys, b.irN.data(), b.jcN.data(), b.prN.data(), b.irG.data(),
+                        b.jcG.data(), b.u0.data());
+    }
+    char cwd[PATH_MAX];
+    if (!getcwd(cwd, sizeof(cwd)) || chdir(dir) != 0) return SP_E_INVALID;
+    unsigned int next_output = get_next_output(sys);
+    int oi = 0;
+    auto snap = [&]() {
+        output_vtk__sync_step(sys, sys->current_step);
+        output_vtk__async_step(sys);
+        for (int i = 0; i < N; i++) {
+            const Particle &p = sys->particles[i];
+            const size_t o = (size_t)oi * N + i;
+            for (int d = 0; d < 3; d++) {
+                if (x) x[3 * o + d] = p.x[d];
+                if (v) v[3 * o + d] = p.v[d];
+            }
+            if (rho) rho[o] = p.rho;
+            if (bvf) bvf[o] = p.bvf_phi;
+            if (nu) nu[o] = p.nu;
+            for (int s2 = 0; s2 < S; s2++) {
+                if (counts && rdme) counts[o * S + s2] = (int32_t)b.u0[(size_t)i * S + s2];
+                if (chem && sc->enable_pde) chem[o * S + s2] = p.C[s2];
+            }
+        }
+        oi++;
+    };
+    for (sys->current_step = 0; sys->current_step < sys->nt; sys->current_step++) {
+        buildKDTree(sys);
+        if (sys->current_step >= next_output && oi < sc->num_outputs) {
+            snap();
+            next_output = get_next_output(sys);
+        }
+        for (unsigned sub = 0; sub < 3; sub++)
+            for (auto &p : sys->particles) take_step(&p, sys, sys->current_step, sub);
+        if (rdme) simulate_rdme(sys, sys->current_step);
+    }
+    while (oi < sc->num_outputs) snap();
+    if (chdir(cwd) != 0) return SP_E_INVALID;
     return SP_OK;
 }
 

@@ -46,3 +46,28 @@ def flow_bcs(spacing_div=16, num_steps=30):
                            [-INF, INF, -INF, INF, -INF, 0.1]],
                    bc_type=[1, 0, 2], bc_target=[0, 2, 1],
                    bc_value=[[0.2, 0.0, 0.0], [1.05, 0, 0], [5e-3, 0, 0]])
+
+
+def pinned_chem(n=10):
+    """Deterministic chemistry that the reference engine can be compared on.
+    The engine reads the diffusion matrix type-major and the dense
+    stoichiometry reaction-major (model.cpp:165, 186) from arrays written the
+    other way round (solver.py:225-231, 269-286); with one particle type and a
+    symmetric stoichiometry both reads agree with the layouts.  2-D n x n
+    lattice, species A, B (D = 0.1 / 0.05), A -> B (k 0.3), B -> A (k 0.1),
+    and a boundary condition holding C[B] = 4 for y > 0.8."""
+    base = S.config_birth_death_2d(n=n, count=0, t_end=3.0, num_points=4, dt=0.05)
+    N = base.num_particles
+    programs = {}
+    rate, kind, reac, allowed, jcN, irN, prN = S.mass_action(
+        ["A", "B"], [(0.3, {"A": 1}, {"B": 1}, None), (0.1, {"B": 1}, {"A": 1}, None)], 1, {},
+        [], programs)
+    u0 = np.zeros((N, 2), np.uint32)
+    rng = np.random.default_rng(5)
+    u0[:, 0] = rng.integers(0, 20, N)
+    u0[:, 1] = rng.integers(0, 10, N)
+    return base.copy(species=["A", "B"], rxn_rate=rate, rxn_kind=kind, rxn_reactants=reac,
+                     rxn_allowed=allowed, jcN=jcN, irN=irN, prN=prN,
+                     diffusion=np.array([[0.1], [0.05]]), u0=u0, enable_pde=True,
+                     bc_box=[[-INF, INF, 0.8, INF, -INF, INF]], bc_type=[0], bc_target=[3 + 1],
+                     bc_value=[[4.0, 0.0, 0.0]], name="pinned_chem", **programs)

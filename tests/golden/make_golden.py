@@ -4,7 +4,7 @@ Run where the SpatialPy reference is present ($SPATIALPY_REFERENCE or its
 pip install in baseline/_ref; its engine is compiled by oracle/build_ref.sh
 into oracle/_ref/), optionally naming the fixtures to write:
 
-    python tests/golden/make_golden.py [neighbors] [bd] [rdme] [rdme40] [sdpd]
+    python tests/golden/make_golden.py [neighbors] [bd] [rdme] [rdme40] [sdpd] [pins] [coupled] [vtk]
 
 Fixtures (all inputs are rebuilt by spatialpy_gb300.scenario builders with the
 parameters stored alongside):
@@ -25,6 +25,23 @@ parameters stored alongside):
                      the species totals, and per voxel and species the sums
                      of x, x^2, x^3, x^4 over the trajectories at t = 1 and 5
 * sdpd_small.npz     reference SDPD dam-break states after 1, 5, 21, 41 steps
+* pins.npz           the deterministic chemistry on a static lattice
+                     (tests/chem_cases.py pinned_chem) and on the moving dam
+                     break (tests/coupled_cases.py dam_break_chem): the
+                     concentrations at every output; the dam break with flow
+                     boundary conditions (chem_cases.flow_bcs): x, v, rho
+                     after 1, 5, 21, 41 steps
+* nsm_coupled.npz    2,000-trajectory ensembles of the moving dam break with
+                     species (coupled_cases.dam_break_species, 1,368
+                     particles, network "full", 60 steps), stock and rescaled
+                     selection: per particle and output the mean, variance
+                     and fourth central moment of the counts, the totals'
+                     mean and variance, and the mean event counts
+* vtk_ref.npz        outputN.vtk files written by the engine's own VTK writer
+                     (output.cpp) for three runs (the birth-death lattice; the
+                     pinned chemistry case with C[] and D[] fields; the moving
+                     dam break with species), with the full-precision state
+                     each file was written from
 """
 from __future__ import annotations
 
@@ -128,6 +145,43 @@ def central_moments(m, n):
     return mu, var, m4
 
 
+def _coupled_worker(args):
+    variant, seeds, kw = args
+    sys.path.insert(0, os.path.dirname(HERE))
+    from coupled_cases import dam_break_species
+    sc = dam_break_species(**kw)
+    m, tots, ev = None, [], []
+    for s in seeds:
+        out, e = oracle.ref_coupled(sc, int(s), variant)
+        x = out.astype(np.float64)
+        p = [x, x * x, x * x * x, x * x * x * x]
+        m = p if m is None else [a + b for a, b in zip(m, p)]
+        tots.append(out.sum(axis=1))
+        ev.append(e)
+    return m, np.array(tots), np.array(ev)
+
+
+def vtk_cases():
+    sys.path.insert(0, os.path.dirname(HERE))
+    from chem_cases import pinned_chem
+    from coupled_cases import dam_break_species
+    return {"bd": (S.config_birth_death_2d(t_end=2.0, num_points=3), ["A"]),
+            "chem": (pinned_chem(), ["A", "B"]),
+            "dam": (dam_break_species(spacing_div=8, num_steps=10, num_outputs=2,
+                                      network="decay"), ["S"])}
+
+
+def _vtk_worker(key):
+    import tempfile
+    sc, names = vtk_cases()[key]
+    with tempfile.TemporaryDirectory() as d:
+        st = oracle.ref_vtk_run(sc, 11, names, d)
+        files = [open(os.path.join(d, f"output{k}.vtk"), "rb").read()
+                 for k in range(len(sc.output_steps))]
+        bbox = open(os.path.join(d, "output0_boundingBox.vtk"), "rb").read()
+    return st, files, bbox
+
+
 def ensemble(name, variant, ntraj, seed0, kw, procs=8):
     seeds = np.arange(seed0, seed0 + ntraj, dtype=np.uint64)
     chunks = np.array_split(seeds, procs)
@@ -212,6 +266,63 @@ def main():
                "events_mean": ev.mean(0)}
         np.savez_compressed(os.path.join(HERE, "nsm_rdme40.npz"), **out)
         print("rdme40", tots[:, -1].mean(0), ev.mean(0))
+
+    if "pins" in want:
+        sys.path.insert(0, os.path.dirname(HERE))
+        from chem_cases import flow_bcs, pinned_chem
+        from coupled_cases import dam_break_chem
+        out = {"static/C": oracle.ref_chem(pinned_chem()),
+               "moving/C": oracle.ref_chem(dam_break_chem())}
+        sc = flow_bcs(spacing_div=8, num_steps=41)
+        for nsteps in (1, 5, 21, 41):
+            x, v, rho = oracle.ref_sdpd(sc, nsteps)
+            out[f"bcs/{nsteps}/x"] = x
+            out[f"bcs/{nsteps}/v"] = v
+            out[f"bcs/{nsteps}/rho"] = rho
+        np.savez_compressed(os.path.join(HERE, "pins.npz"), **out)
+        print("pins.npz written")
+
+    if "coupled" in want:
+        kw = dict(spacing_div=8, num_steps=60, num_outputs=4, network="full")
+        out = {}
+        procs = os.cpu_count() or 1
+        for variant in ("", "_exact"):
+            seeds = np.arange(3030, 3030 + 2000, dtype=np.uint64)
+            chunks = [c for c in np.array_split(seeds, procs) if len(c)]
+            with mp.get_context("spawn").Pool(len(chunks)) as pool:
+                parts = pool.map(_coupled_worker, [(variant, c, kw) for c in chunks])
+            m = [sum(p[0][k] for p in parts) for k in range(4)]
+            tots = np.concatenate([p[1] for p in parts])
+            ev = np.concatenate([p[2] for p in parts])
+            n = len(tots)
+            mu, var, m4 = central_moments(m, n)
+            tag = variant.strip("_") or "stock"
+            out[f"{tag}/mean"] = mu[..., 0]                   # [T, N]
+            out[f"{tag}/var"] = var[..., 0]
+            out[f"{tag}/m4"] = m4[..., 0]
+            out[f"{tag}/total_mean"] = tots[..., 0].mean(0)
+            out[f"{tag}/total_var"] = tots[..., 0].var(0, ddof=1)
+            out[f"{tag}/events_mean"] = ev.mean(0)
+            out[f"{tag}/ntraj"] = np.int32(n)
+            print("coupled", tag, tots[:, -1, 0].mean(), ev.mean(0))
+        np.savez_compressed(os.path.join(HERE, "nsm_coupled.npz"), **out)
+
+    if "vtk" in want:
+        out = {}
+        for key, (sc, names) in vtk_cases().items():
+            with mp.get_context("spawn").Pool(1) as pool:      # a fresh file counter
+                st, files, bbox = pool.map(_vtk_worker, [key])[0]
+            for k, f in enumerate(files):
+                out[f"{key}/file{k}"] = np.frombuffer(f, np.uint8)
+            out[f"{key}/bbox"] = np.frombuffer(bbox, np.uint8)
+            for name, a in st.items():
+                out[f"{key}/{name}"] = a
+            out[f"{key}/type"] = sc.type
+            out[f"{key}/mass"] = sc.mass
+            out[f"{key}/names"] = np.array(names)
+            out[f"{key}/chem_on"] = np.int32(bool(sc.enable_pde))
+        np.savez_compressed(os.path.join(HERE, "vtk_ref.npz"), **out)
+        print("vtk_ref.npz written")
 
     if "sdpd" in want:
         sc = S.config_dam_break(spacing_div=8, num_steps=41)

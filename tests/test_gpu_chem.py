@@ -8,8 +8,9 @@ import pytest
 from spatialpy_gb300 import abi
 from spatialpy_gb300 import scenario as S
 
-from .chem_cases import flow_bcs, static_chem
-from .coupled_cases import dam_break_species
+from .chem_cases import flow_bcs, pinned_chem, static_chem
+from .conftest import golden
+from .coupled_cases import dam_break_chem, dam_break_species
 
 pytestmark = pytest.mark.gpu
 
@@ -68,3 +69,44 @@ def test_moving_domain_chemistry_bitexact(oracle_lib, prec, mode):
     np.testing.assert_array_equal(res["events"], ev)
     for j in range(len(seeds)):
         np.testing.assert_array_equal(res["counts"][j], out[j])
+
+
+def test_chemistry_vs_compiled_reference():
+    """GPU concentrations against the compiled engine (tests/golden/pins.npz):
+    the static lattice with a concentration boundary condition and the
+    moving dam break with an FP64 flow within 1e-12 of the largest value at
+    every output; with the FP32 flow within 1e-7 (the oracle's FP32 run is
+    3.8e-9 from the engine)."""
+    from spatialpy_gb300.engine import Engine
+    g = golden("pins.npz")
+    seeds = np.arange(1, dtype=np.uint64) + 3
+    with Engine(pinned_chem()) as eng:
+        res = eng.run(seeds, want_chem=True)
+    assert res["rc"] == abi.SP_OK, res.get("error")
+    want = g["static/C"]
+    assert np.abs(res["chem"][0] - want).max() <= 1e-12 * np.abs(want).max()
+    want = g["moving/C"]
+    for prec, tol in (("f64", 1e-12), ("f32", 1e-7)):
+        with Engine(dam_break_chem(), sdpd_precision=prec) as eng:
+            res = eng.run(seeds, want_chem=True)
+        assert res["rc"] == abi.SP_OK, res.get("error")
+        assert np.abs(res["chem"][0] - want).max() <= tol * np.abs(want).max(), prec
+
+
+def test_flow_boundary_conditions_vs_compiled_reference():
+    """The FP64 flow with boundary conditions on v, nu and rho against the
+    compiled engine after 1, 5, 21 and 41 steps: positions and densities
+    within 1e-12, velocities within 1e-9 norm-wise."""
+    from spatialpy_gb300.engine import Engine
+    g = golden("pins.npz")
+    sc = flow_bcs(spacing_div=8, num_steps=41)
+    with Engine(sc, sdpd_precision="f64") as eng:
+        done = 0
+        for n in (1, 5, 21, 41):
+            eng.sdpd_advance(n - done)
+            done = n
+            x, v, rho = eng.particles(0)
+            rv = g[f"bcs/{n}/v"]
+            assert np.abs(x - g[f"bcs/{n}/x"]).max() <= 1e-12
+            assert np.linalg.norm(v - rv) <= 1e-9 * np.linalg.norm(rv)
+            assert np.abs(rho - g[f"bcs/{n}/rho"]).max() <= 1e-12

@@ -9,6 +9,7 @@ import pytest
 
 from spatialpy_gb300 import abi
 
+from .conftest import golden
 from .coupled_cases import dam_break_species
 
 pytestmark = pytest.mark.gpu
@@ -83,3 +84,32 @@ def test_coupled_multiwarp_batches(oracle_lib, variant):
     np.testing.assert_array_equal(res["events"], ev)
     for j in range(len(SEEDS)):
         np.testing.assert_array_equal(res["counts"][j], out[j])
+
+
+@pytest.mark.parametrize("tag,selection", [("stock", abi.SP_SELECT_REFERENCE),
+                                           ("exact", abi.SP_SELECT_EXACT)])
+def test_coupled_vs_reference_ensembles(tag, selection):
+    """4,000 GPU trajectories of the moving dam break with species (FP32
+    flow) against 2,000 of the compiled engine, which runs the same flow in
+    FP64 with its own random streams: totals inside 99.9% bands at every
+    output, mean event counts within 5%, per particle and output mean and
+    variance inside 99% bands (at least 97% / 96% of the cells holding 10 or
+    more expected molecules: about 290, the particles the molecules reach).
+    The exact-selection reference is the twin that also evaluates a
+    diffusion destination's reactions with the destination's own volume, as
+    exact selection does."""
+    from .stats import band_fractions, moments_from_samples
+    g = golden("nsm_coupled.npz")
+    gn = int(g[f"{tag}/ntraj"])
+    sc = dam_break_species(spacing_div=8, num_steps=60, num_outputs=4, network="full")
+    n = 4000
+    res, _ = _run(sc, "f32", selection, seeds=np.arange(n, dtype=np.uint64) + 4242)
+    cnt = np.array(res["counts"])[..., 0]                      # [n, T, N]
+    tot = cnt.sum(-1)
+    se = np.sqrt(tot.var(0, ddof=1) / n + g[f"{tag}/total_var"] / gn)
+    assert np.all(np.abs(tot.mean(0) - g[f"{tag}/total_mean"])[1:] <= 3.29 * se[1:])
+    np.testing.assert_allclose(res["events"].mean(0), g[f"{tag}/events_mean"], rtol=0.05)
+    ref = (g[f"{tag}/mean"], g[f"{tag}/var"], g[f"{tag}/m4"], gn)
+    fm, fv, cells = band_fractions(moments_from_samples(cnt), ref, min_count=10)
+    assert cells >= 250          # the molecules start on the top ~10% of the fluid
+    assert fm >= 0.97 and fv >= 0.96, (fm, fv)

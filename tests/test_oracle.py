@@ -218,6 +218,80 @@ def test_coupled_oracle_flow_and_species(oracle_lib):
     np.testing.assert_array_equal(ev, ev2)
 
 
+def test_chemistry_oracle_vs_compiled_reference(oracle_lib):
+    """The deterministic chemistry against the compiled engine
+    (tests/golden/pins.npz): a static lattice with a concentration boundary
+    condition, and the moving dam break (FP64 flow, both neighbour modes):
+    concentrations within 1e-12 of the largest at every output (measured
+    2.8e-16 and 9e-21).  The cases are ones on which the engine's transposed
+    reads of the diffusion matrix and stoichiometry (model.cpp:165, 186)
+    agree with the layouts written (tests/chem_cases.py pinned_chem)."""
+    from .chem_cases import pinned_chem
+    from .coupled_cases import dam_break_chem
+    g = golden("pins.npz")
+    want = g["static/C"]
+    got = oracle_lib.chem_static(pinned_chem())
+    assert np.abs(got - want).max() <= 1e-12 * np.abs(want).max()
+    assert np.abs(want[-1] - want[0]).max() > 0.5
+    want = g["moving/C"]
+    for mode in (2, 3):
+        ch = oracle_lib.coupled_ensemble(dam_break_chem(), np.arange(1, dtype=np.uint64),
+                                         precision="f64", mode=mode, want_chem=True)[5]
+        assert np.abs(ch - want).max() <= 1e-12 * np.abs(want).max()
+
+
+def test_flow_boundary_conditions_vs_compiled_reference(oracle_lib):
+    """The dam break with boundary conditions on v, nu and rho against the
+    compiled engine running the same conditions (applyBoundaryConditions as
+    boundarycondition.py:121-167 generates it): FP64 oracle states after 1,
+    5, 21 and 41 steps within 1e-12 (positions, densities) and 1e-9
+    norm-wise (velocities), in the reference's neighbour mode and the GPU's."""
+    from .chem_cases import flow_bcs
+    g = golden("pins.npz")
+    sc = flow_bcs(spacing_div=8, num_steps=41)
+    for mode in (3, 2):
+        st = oracle_lib.SdpdState(sc)
+        done = 0
+        for n in (1, 5, 21, 41):
+            oracle_lib.sdpd(sc, st, n - done, "f64", mode)
+            done = n
+            rv = g[f"bcs/{n}/v"]
+            assert np.abs(st.x - g[f"bcs/{n}/x"]).max() <= 1e-12
+            assert np.linalg.norm(st.v - rv) <= 1e-9 * np.linalg.norm(rv)
+            assert np.abs(st.rho - g[f"bcs/{n}/rho"]).max() <= 1e-12
+
+
+@pytest.mark.parametrize("tag,selection", [("stock", abi.SP_SELECT_REFERENCE),
+                                           ("exact", abi.SP_SELECT_EXACT)])
+def test_coupled_oracle_vs_reference_ensembles(oracle_lib, tag, selection):
+    """Moving dam break with species (1,368 particles, network "full", 60
+    steps; FP32 flow as on the GPU) against 2,000 trajectories of the
+    compiled engine (stock / rescaled selection): totals inside 99.9% bands
+    at every output, mean event counts within 5%, and per particle and
+    output mean and variance inside 99% bands (at least 97% / 96% of the
+    cells holding 10 or more expected molecules: about 290 cells, the
+    particles the molecules reach).  The exact-selection reference is the
+    twin that also evaluates a diffusion destination's reactions with the
+    destination's own volume, as exact selection does."""
+    from .coupled_cases import dam_break_species
+    from .stats import band_fractions, moments_from_samples
+    g = golden("nsm_coupled.npz")
+    gn = int(g[f"{tag}/ntraj"])
+    sc = dam_break_species(spacing_div=8, num_steps=60, num_outputs=4, network="full")
+    n = 1000
+    out, ev, st, _, _ = oracle_lib.coupled_ensemble(sc, np.arange(n, dtype=np.uint64) + 77,
+                                                    selection=selection, want_particles=False)
+    assert (st == 0).all()
+    tot = out[..., 0].sum(-1)
+    se = np.sqrt(tot.var(0, ddof=1) / n + g[f"{tag}/total_var"] / gn)
+    assert np.all(np.abs(tot.mean(0) - g[f"{tag}/total_mean"])[1:] <= 3.29 * se[1:])
+    np.testing.assert_allclose(ev.mean(0), g[f"{tag}/events_mean"], rtol=0.05)
+    ref = (g[f"{tag}/mean"], g[f"{tag}/var"], g[f"{tag}/m4"], gn)
+    fm, fv, cells = band_fractions(moments_from_samples(out[..., 0]), ref, min_count=10)
+    assert cells >= 250          # the molecules start on the top ~10% of the fluid
+    assert fm >= 0.97 and fv >= 0.96, (fm, fv)
+
+
 def test_chem_oracle_conserves_and_integrates(oracle_lib):
     """Deterministic chemistry (model.cpp:151-189): SPH diffusion alone keeps
     the total of C; a zero-order ODE rate k adds k*dt per step to every
