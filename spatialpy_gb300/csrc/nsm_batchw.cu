@@ -25,8 +25,10 @@
 //     near the birthday bound of the 2,000 groups (about 48 events of 128);
 //     with leaves only the 64,000 voxels' conflicts and redrawn times do.
 //  4. accepted events are written and, after a CTA barrier (a group may
-//     hold several accepted events), their voxel groups rescanned; then the
-//     tree is repaired level by level, one thread per changed node.
+//     hold several accepted events), their voxel groups are listed and
+//     rescanned, 4 lanes per group (8 leaves per lane, merged by shuffles)
+//     and two rounds of groups per pass with all their loads in flight;
+//     then the tree is repaired level by level, one thread per changed node.
 //
 // Scalars that steer the loop (clock, counters, running propensity total)
 // are kept in every thread and updated from the same shared values in the
@@ -123,30 +125,26 @@ __device__ __forceinline__ void rescan3(const NsmInstance& I, const long long* L
     T3[g] = r.t2;
 }
 
-// rescan3 of groups ga and gb (gb < 0: none) with both groups' leaf loads in
-// flight together
-__device__ __forceinline__ void rescan3_pair(const NsmInstance& I, const long long* LF,
-                                             long long* NT, int* NI, long long* T2, int* I2,
-                                             long long* T3, int ga, int gb) {
-    const int gq = gb >= 0 ? gb : ga;
-    const longlong2* pa = (const longlong2*)(LF + (size_t)ga * 32);
-    const longlong2* pb = (const longlong2*)(LF + (size_t)gq * 32);
-    const Top3 a0 = top3_half(pa, ga * 32), b0 = top3_half(pb, gq * 32);
-    const Top3 a1 = top3_half(pa + 8, ga * 32 + 16), b1 = top3_half(pb + 8, gq * 32 + 16);
-    const Top3 ra = merge3(a0, a1), rb = merge3(b0, b1);
-    const int off1 = I.level_off[1];
-    NT[off1 + ga] = ra.t0;
-    NI[off1 + ga] = ra.i0;
-    T2[ga] = ra.t1;
-    I2[ga] = ra.i1;
-    T3[ga] = ra.t2;
-    if (gb >= 0) {
-        NT[off1 + gb] = rb.t0;
-        NI[off1 + gb] = rb.i0;
-        T2[gb] = rb.t1;
-        I2[gb] = rb.i1;
-        T3[gb] = rb.t2;
-    }
+// Top3 of two adjacent leaves `base`, `base` + 1
+__device__ __forceinline__ Top3 pair3(const longlong2 u, int base) {
+    const bool a = u.x <= u.y;                   // ties: the lower index first
+    Top3 r;
+    r.t0 = a ? u.x : u.y;
+    r.t1 = a ? u.y : u.x;
+    r.t2 = SP_INF_BITS;
+    r.i0 = a ? base : base + 1;
+    r.i1 = a ? base + 1 : base;
+    return r;
+}
+
+__device__ __forceinline__ Top3 shfl_xor3(const Top3& t, int o) {
+    Top3 q;
+    q.t0 = __shfl_xor_sync(SP_FULL, t.t0, o);
+    q.t1 = __shfl_xor_sync(SP_FULL, t.t1, o);
+    q.t2 = __shfl_xor_sync(SP_FULL, t.t2, o);
+    q.i0 = __shfl_xor_sync(SP_FULL, t.i0, o);
+    q.i1 = __shfl_xor_sync(SP_FULL, t.i1, o);
+    return q;
 }
 
 static size_t batchw_smem_bytes(const NsmInstance& d, int W) {
@@ -536,12 +534,76 @@ __global__ void __launch_bounds__(32 * W, 1)
                 }
                 if (m > 0 && tid == m - 1) s_tl = ct;
                 // ---- 5. rescan and tree repair ------------------------------------
+                const int off1r = I.level_off[1];
                 // a group may hold several accepted events: every commit is
                 // stored before any rescan reads the group
                 __syncthreads();
                 const int gv = v >> 5;
                 const int gw = (w >= 0 && (w >> 5) != gv) ? w >> 5 : -1;
-                if (acc) rescan3_pair(I, LF, NT, NI, T2, I2, T3, gv, gw);
+                {
+                    // the groups to rescan, listed in fa (free after the walk)
+                    const int nr = acc ? (gw >= 0 ? 2 : 1) : 0;
+                    int rinc = nr;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int u = __shfl_up_sync(SP_FULL, rinc, o);
+                        if (lane >= o) rinc += u;
+                    }
+                    if (lane == 31) s_wcnt[wid] = rinc;
+                    __syncthreads();
+                    int rbase = 0, rtot = 0;
+#pragma unroll
+                    for (int u = 0; u < W; u++) {
+                        if (u < wid) rbase += s_wcnt[u];
+                        rtot += s_wcnt[u];
+                    }
+                    if (nr) {
+                        fa[rbase + rinc - nr] = gv;
+                        if (nr == 2) fa[rbase + rinc - 1] = gw;
+                    }
+                    __syncthreads();
+                    // 4 lanes per group (lane l4 reads leaves 8*l4 .. 8*l4+7),
+                    // two rounds of NC/4 groups with all their loads in flight
+                    const int sg = tid >> 2, l4 = tid & 3;
+                    for (int r0 = 0; r0 < rtot; r0 += NC / 2) {
+                        const int ra = r0 + sg, rb = ra + NC / 4;
+                        const int ga = ra < rtot ? fa[ra] : -1;
+                        const int gb2 = rb < rtot ? fa[rb] : -1;
+                        longlong2 ua[4], ub[4];
+                        const int basea = (ga >= 0 ? ga : 0) * 32 + l4 * 8;
+                        const int baseb = (gb2 >= 0 ? gb2 : 0) * 32 + l4 * 8;
+#pragma unroll
+                        for (int q = 0; q < 4; q++) {
+                            ua[q] = ga >= 0 ? ((const longlong2*)(LF + basea))[q]
+                                            : make_longlong2(SP_INF_BITS, SP_INF_BITS);
+                            ub[q] = gb2 >= 0 ? ((const longlong2*)(LF + baseb))[q]
+                                             : make_longlong2(SP_INF_BITS, SP_INF_BITS);
+                        }
+                        Top3 ta = merge3(merge3(pair3(ua[0], basea), pair3(ua[1], basea + 2)),
+                                         merge3(pair3(ua[2], basea + 4), pair3(ua[3], basea + 6)));
+                        Top3 tb = merge3(merge3(pair3(ub[0], baseb), pair3(ub[1], baseb + 2)),
+                                         merge3(pair3(ub[2], baseb + 4), pair3(ub[3], baseb + 6)));
+#pragma unroll
+                        for (int o = 1; o < 4; o <<= 1) {
+                            ta = merge3(ta, shfl_xor3(ta, o));
+                            tb = merge3(tb, shfl_xor3(tb, o));
+                        }
+                        if (l4 == 0 && ga >= 0) {
+                            NT[off1r + ga] = ta.t0;
+                            NI[off1r + ga] = ta.i0;
+                            T2[ga] = ta.t1;
+                            I2[ga] = ta.i1;
+                            T3[ga] = ta.t2;
+                        }
+                        if (l4 == 0 && gb2 >= 0) {
+                            NT[off1r + gb2] = tb.t0;
+                            NI[off1r + gb2] = tb.i0;
+                            T2[gb2] = tb.t1;
+                            I2[gb2] = tb.i1;
+                            T3[gb2] = tb.t2;
+                        }
+                    }
+                }
                 __syncthreads();
 #pragma unroll
                 for (int u = 0; u < W; u++) {
