@@ -281,7 +281,23 @@ def run_sdpd(args):
     ps = sc.num_particles * args.sdpd_steps / (ms / 1e3)
     peak, src = measured_peak()
     achieved = B_SDPD * ps / 1e9
+    cpu = None
+    if not args.skip_cpu and _reference_engine():
+        # the reference engine's flow, one independent replica per host core
+        # (one flow does not gain from its threads: SURVEY F5), steps [2, 4)
+        import oracle
+        cores = os.cpu_count() or 1
+        scb = S.config_dam_break(num_steps=4)
+        runs, used = oracle.ref_moving_bench(scb, np.arange(cores, dtype=np.uint64), False, 2,
+                                             "_exact", cores)
+        per_run = [scb.num_particles * 2 / sec for _, sec in runs]
+        cpu = {"value": float(sum(per_run)), "unit": "particle-steps/s", "cores": int(used),
+               "kind": "reference",
+               "single_flow": float(np.mean(per_run)),
+               "sample": f"reference engine -O2, {used} independent flows (one per core), "
+                         f"steps 2-3 timed after set-up; single_flow = one flow on one core"}
     return {"metric": "SDPD particle-steps/s", "value": ps, "unit": "particle-steps/s",
+            **({"cpu_baseline": cpu} if cpu else {}),
             "steps": args.sdpd_steps, "warmup": 20, "ms_per_step": ms / args.sdpd_steps,
             "dtype": "f32", "gpu_launches": int(launches),
             "config": {"workload": "SDPD dam break 1x0.5x0.5, 48x32x32 fluid + 3 wall layers "
@@ -327,21 +343,24 @@ def run_coupled(args, with_cpu: bool):
            "config": {"workload": "dam break 84,696 particles + species S over 64 "
                                   "trajectories (decay 0.01, D=1e-3 fluid only)",
                       "particles": int(sc.num_particles), "trajectories": COUPLED_TRAJ}}
-    if with_cpu:
+    if with_cpu and _reference_engine():
+        # the reference engine: every trajectory carries its own flow, so the
+        # 64 trajectories cost 64 flows; one trajectory per core, steps [2, 4)
+        # timed after set-up
         import oracle
-        oracle.build()
-        n = 3
-        sc3 = S.config_dam_break(num_steps=n, num_outputs=2)
-        t0 = time.perf_counter()
-        _, ev, _, _, _ = oracle.coupled_ensemble(sc3, seeds, want_particles=False,
-                                                 want_counts=False)
-        dt = time.perf_counter() - t0
+        cores = os.cpu_count() or 1
+        scb = S.config_dam_break(num_steps=4)
+        runs, used = oracle.ref_moving_bench(scb, np.arange(cores, dtype=np.uint64) + SEED0, True,
+                                             2, "_exact", cores)
+        mean_s = float(np.mean([sec for _, sec in runs]))
         out["cpu_baseline"] = {
-            "value": sc3.num_particles * n / dt, "unit": "particle-steps/s",
-            "events_per_s": float(ev.sum() / dt), "cores": os.cpu_count() or 1,
-            "kind": "port",
-            "sample": f"first {n} steps, 64 trajectories: SDPD on one thread, trajectories "
-                      f"on all cores ({dt:.1f} s)"}
+            "value": scb.num_particles * 2 / (COUPLED_TRAJ * mean_s / used),
+            "unit": "particle-steps/s",
+            "events_per_s": float(sum(ev / sec for ev, sec in runs)),
+            "cores": int(used), "kind": "reference",
+            "sample": f"reference engine -O2, {used} trajectories (one per core, each with its "
+                      f"own flow), steps 2-3 timed after set-up ({mean_s:.2f} s per trajectory); "
+                      f"value scales to the {COUPLED_TRAJ} trajectories over {used} cores"}
     return out
 
 

@@ -292,6 +292,8 @@ def ref_lib(variant: str = ""):
         L.spref_chem.argtypes = [_p(SpScenario), _p(C.c_uint32), _p(C.c_double)]
         L.spref_coupled.argtypes = [_p(SpScenario), _p(C.c_uint32), C.c_uint64, _p(C.c_int32),
                                     _p(C.c_int64)]
+        L.spref_moving_bench.argtypes = [_p(SpScenario), _p(C.c_uint32), C.c_uint64, C.c_int32,
+                                         C.c_int32, _p(C.c_int64), _p(C.c_double)]
         L.spref_vtk_run.argtypes = [_p(SpScenario), _p(C.c_uint32), C.c_uint64,
                                     _p(C.c_char_p), C.c_char_p] + [_p(C.c_double)] * 5 + \
             [_p(C.c_int32), _p(C.c_double)]
@@ -387,6 +389,39 @@ def ref_coupled(sc, seed: int, variant: str = "", u0=None):
     if rc != 0:
         raise RuntimeError(f"reference coupled run failed ({rc})")
     return out, ev
+
+
+def _ref_moving_worker(args):
+    sc, seeds, with_rdme, timed_from, variant = args
+    L = ref_lib(variant)
+    s = scenario_struct(sc)
+    u0 = np.ascontiguousarray(sc.u0, np.uint32)
+    out = []
+    for seed in seeds:
+        ev = np.zeros(2, np.int64)
+        sec = C.c_double(0.0)
+        rc = L.spref_moving_bench(C.byref(s), _ptr(u0, C.c_uint32), int(seed), int(with_rdme),
+                                  timed_from, _ptr(ev, C.c_int64), C.byref(sec))
+        if rc != 0:
+            raise RuntimeError(f"reference moving-domain run failed ({rc})")
+        out.append((int(ev.sum()), sec.value))
+    return out
+
+
+def ref_moving_bench(sc, seeds, with_rdme: bool, timed_from: int, variant: str = "_exact",
+                     processes: int = 0):
+    """The compiled engine on a moving domain, one run per seed, spread over
+    `processes` spawn-started processes (0 = every host core); each run
+    times its steps [timed_from, nt).  Returns [(events, seconds)] per run
+    and the number of processes."""
+    import multiprocessing as mp
+    seeds = np.asarray(seeds, np.uint64)
+    processes = min(processes or os.cpu_count() or 1, len(seeds))
+    chunks = [c for c in np.array_split(seeds, processes) if len(c)]
+    with mp.get_context("spawn").Pool(len(chunks)) as pool:
+        res = pool.map(_ref_moving_worker,
+                       [(sc, c, with_rdme, timed_from, variant) for c in chunks])
+    return [x for part in res for x in part], len(chunks)
 
 
 def ref_vtk_run(sc, seed: int, names, directory, variant: str = ""):

@@ -506,6 +506,49 @@ int spref_vtk_run(const sp_scenario *sc, const uint32_t *u0, uint64_t seed,
 }
 
 /*
+ * CPU baselines of the moving domain: the engine loop of spref_coupled
+ * (with_rdme: species on; else the flow alone) over steps [0, nt), timing
+ * steps [timed_from, nt) only (the set-up and the first steps excluded).
+ * counters: (reactions, diffusions) in the timed steps; *seconds: their wall
+ * time (steady clock).
+ */
+int spref_moving_bench(const sp_scenario *sc, const uint32_t *u0, uint64_t seed, int32_t with_rdme,
+                       int32_t timed_from, int64_t *counters, double *seconds) {
+    Built b;
+    const int rdme = with_rdme && sc->num_species > 0;
+    int rc = build(sc, b, rdme);
+    if (rc) return rc;
+    ParticleSystem *sys = b.sys;
+    if (sys->static_domain) return SP_E_UNSUPPORTED;
+    if (timed_from < 0 || timed_from >= (int)sc->num_steps) return SP_E_INVALID;
+    const int S = sc->num_species, N = sc->num_particles;
+    if (rdme) {
+        b.u0.assign(u0, u0 + (size_t)N * S);
+        rng = std::mt19937_64(seed);
+        initialize_rdme(sys, b.irN.data(), b.jcN.data(), b.prN.data(), b.irG.data(),
+                        b.jcG.data(), b.u0.data());
+    }
+    long long r0 = 0, d0 = 0;
+    auto t0 = std::chrono::steady_clock::now();
+    for (sys->current_step = 0; sys->current_step < sys->nt; sys->current_step++) {
+        if ((int)sys->current_step == timed_from) {
+            r0 = sys->total_reactions;
+            d0 = sys->total_diffusion;
+            t0 = std::chrono::steady_clock::now();
+        }
+        buildKDTree(sys);
+        for (unsigned sub = 0; sub < 3; sub++)
+            for (auto &p : sys->particles) take_step(&p, sys, sys->current_step, sub);
+        if (rdme) simulate_rdme(sys, sys->current_step);
+    }
+    const auto t1 = std::chrono::steady_clock::now();
+    counters[0] = sys->total_reactions - r0;
+    counters[1] = sys->total_diffusion - d0;
+    *seconds = std::chrono::duration<double>(t1 - t0).count();
+    return SP_OK;
+}
+
+/*
  * SDPD flow without species: nsteps engine steps (substeps 0,1,2 over all
  * particles in order, single-threaded).  Writes final x[N*3], v[N*3],
  * rho[N], and the last neighbour counts.

@@ -138,3 +138,28 @@ def test_gpu_solver_exports_reference_vtk(tmp_path):
     assert len(paths) == 11
     for k, p in enumerate(paths):
         np.testing.assert_array_equal(vtk.read_step(p)[1]["D[Rabbits]"], r.counts[k][:, 0])
+
+
+@pytest.mark.gpu
+def test_real_model_through_gpu_solver_subclass():
+    """The drop-in with a real spatialpy.Model: in a fresh interpreter whose
+    path holds the reference package, GpuSolver subclasses spatialpy.Solver
+    (Solver.__init__ enforces the subclass, solver.py:56-61) and runs the
+    reference's own birth-death test model through run(model,
+    solver=GpuSolver): Result instances, output 0 = u0, seed reproducibility,
+    and the exact immigration-death mean at every output for 200
+    trajectories (tests/gpu_model_dropin.py)."""
+    import os
+    import subprocess
+    import sys
+    from .refmodels import REF, STUBS
+    if REF is None:
+        pytest.skip("reference package not present")
+    here = os.path.dirname(os.path.abspath(__file__))
+    root = os.path.dirname(here)
+    env = dict(os.environ, PYTHONDONTWRITEBYTECODE="1",
+               PYTHONPATH=os.pathsep.join([root, STUBS, REF, os.path.join(REF, "test")]))
+    r = subprocess.run([sys.executable, os.path.join(here, "gpu_model_dropin.py")], env=env,
+                       capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
+    assert "drop-in ok" in r.stdout
