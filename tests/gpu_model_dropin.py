@@ -20,8 +20,12 @@ def main():
     assert len(res) == n
     u0 = res[0].read_step(0)[1]["D[Rabbits]"]
     assert u0.sum() == 100                                   # output 0 = u0 (test_solver.py:127)
-    again = run(model, solver=GpuSolver, number_of_trajectories=1, seed=11)
-    assert again[0] == res[0]                                # same seed, same trajectory
+    # the same compiled solver, same seed: the same trajectory (each compile
+    # scatters the initial condition anew from numpy's global generator,
+    # initialcondition.py:178-197, as the reference's does)
+    a = sol.run(number_of_trajectories=2, seed=5)
+    b = sol.run(number_of_trajectories=1, seed=5)
+    assert a[0] == b[0] and a[0] != a[1]
     tot = np.array([r.get_species("Rabbits").sum(axis=1) for r in res])   # [n, 11]
     # exact selection: immigration-death from 100 molecules, birth 10 x total
     # volume 1.21 (121 particles of volume 0.01), death 0.1 per molecule
