@@ -1079,7 +1079,7 @@ static int coupled_steps(sp_handle* h, int target, bool ref, long long budget, l
         launch_nsm_rebuild(h->d_trajs, h->d_insts, ntraj, R.max_leaf, R.max_levels,
                            h->dt * (double)R.step, (uint32_t)R.step, st);
         launch_groups(h, ref, R.step + 1, budget, max_ns);
-        h->launches += 3 + 1 + 1 + 3 + 1;
+        h->launches += kSdpdLaunchesPerStep + 1 + 1 + 3 + 1;
         R.step++;
     }
     cudaEventRecord(h->eb, st);

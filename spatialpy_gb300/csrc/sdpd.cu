@@ -4,23 +4,31 @@
 // with the kd-tree of :80-108): take_step1 (src/simulate.cpp:56-109),
 // find_neighbors + pairwiseForce (particle.cpp:240-294, model.cpp:39-191),
 // take_step2 with filterDensity and the boundary volume fraction
-// (simulate.cpp:132-173, model.cpp:194-329).  Per step, a memset and three
-// launches (replayed from a CUDA graph in blocks of 20 steps):
+// (simulate.cpp:132-173, model.cpp:194-329).  Per step, five launches
+// (replayed from a CUDA graph in blocks of 20 steps):
 //
-//   begin     cell of each particle at its start-of-step position (the
-//             kd-tree points of the step): the index and position go into
-//             the cell's slots (fixed capacity, atomic slot counter); then
-//             the predictor
-//   pairs     per particle: neighbour list of the moved position against the
-//             tree points, sorted by (r^2, j) in shared memory; pressure,
-//             viscous, background-pressure and transport forces and the
-//             density rate summed in list order
+//   begin     the predictor, then the cell of each particle's start-of-step
+//             position (the kd-tree points of the step) and its rank in that
+//             cell (atomic histogram)
+//   scan      exclusive scan of the cell counts into cell starts (one CTA);
+//             the counts are reset for the next step
+//   scatter   counting-sort scatter into cell-ordered, float4-packed copies
+//             of what the force pass reads: tree point (+ particle index),
+//             current position (+ mass), velocity, transport velocity and
+//             {rho, P/rho^2, m/rho, nu}
+//   pairs     one warp per particle, particles taken in cell order: the lanes
+//             stream the 3^dim neighbour cells (contiguous runs along the last
+//             axis) with coalesced loads, keep the tree points within h by
+//             ballot, rank-sort them by (r^2, j), evaluate the pressure,
+//             viscous, background-pressure and transport terms and the
+//             density rate one pair per lane, and sum them in list order
 //   corrector corrector, Shepard filter every 20 steps, boundary volume
 //             fraction and bounce-back
 //
 // Layout (HBM, structure of arrays): position, velocity, transport velocity,
 // force (+density rate in .w) and background force as 4-vectors of REAL;
-// rho, old_rho, mass, nu as REAL arrays; neighbour lists [N][KCAP].
+// rho, old_rho, mass, nu as REAL arrays; neighbour lists [N][KCAP] (one list
+// row is written by one warp, lane k writing entry k).
 //
 // The reference builds its kd-tree once per step, so in the force pass a
 // moved particle is searched against start-of-step points and finds its own
@@ -64,21 +72,31 @@ struct SdpdDev {
     int N, dim, step, stat;
     int self_step;   // self pair at |dt vt| (always in FP32)
     R h, dt, rho0, P0, alpha, g0, g1, g2;
+    R acc2;      // largest r^2 with r^2 <= h^2 and sqrt(r^2) <= h (list predicate)
+    double inv_cs;   // 1 / cell edge
     double rho0d;
     typename Vec4<R>::T *pos, *vel, *vt, *F, *Fbp, *pold;
-    typename Vec4<R>::T *plo, *pold_lo, *cpos_lo;   // lo parts (float only)
+    typename Vec4<R>::T *plo, *pold_lo;   // lo parts (float only)
     R *rho, *orho, *mass, *nu;
     R* rfull;    // float: rho0 + deviation; double: the densities themselves
     const uint8_t* fixed;
-    int *ccnt, *cidx;               // per cell: slot count, particle index [ncell][CAP]
-    typename Vec4<R>::T* cpos;      // per cell slot: start-of-step position
+    // counting sort of the tree points by cell
+    int *ccnt, *cstart;             // per cell: count (zero between steps), first sorted slot
+    int *ckey, *crank;              // per particle: cell, rank within the cell
+    int* qkey;                      // per particle: cell of the moved position
+    int* slot_of;                   // per particle: its slot in the cell order
+    // cell-ordered copies (slot = cstart[cell] + rank), written by the scatter
+    typename Vec4<R>::T *s_tp, *s_tplo;   // tree point (.w: particle index bits), lo part
+    typename Vec4<R>::T *s_x, *s_xlo;     // current position (.w: mass), lo part
+    typename Vec4<R>::T *s_v, *s_vt;      // velocity, transport velocity
+    typename Vec4<R>::T* s_aux;           // {rho, P/rho^2, m/rho, nu}
     int *ncnt, *nidx;
     R *ndist, *ndw;
     R* ndij;     // D_ij per list entry, or nullptr when no species diffuse
     R *pr, *wv;  // per particle after the predictor: P/rho^2 and m/rho (read by pairs)
     int kcap;
     CellGrid g;
-    int* flag;   // bit 1: list overflow, bit 2: NaN state, bit 4: cell overflow
+    int* flag;   // bit 1: list overflow, bit 2: NaN state
     // boundary conditions on v, nu, rho (boundarycondition.py:121-167)
     const int* type;
     int nbc;
@@ -133,14 +151,29 @@ __device__ __forceinline__ void comp_add(float& hi, float& lo, float b) {
     hi = s2;
 }
 
-constexpr int kCellCap = 16;
+// particle index carried in the .w of a cell-ordered tree point (bits only)
+__device__ __forceinline__ float idx_bits(float, int j) { return __int_as_float(j); }
+__device__ __forceinline__ double idx_bits(double, int j) {
+    return __longlong_as_double((long long)j);
+}
+__device__ __forceinline__ int bits_idx(float w) { return __float_as_int(w); }
+__device__ __forceinline__ int bits_idx(double w) { return (int)__double_as_longlong(w); }
 
+// Cell of a coordinate, clamped to the grid.  Binning multiplies by 1/cs
+// (cs = h (1 + 1e-7)): monotone in p and, with that margin, points within h
+// of each other still fall in the same or adjacent cells.
 template <typename R>
-__device__ __forceinline__ int cellc(R p, const CellGrid& g, int d) {
+__device__ __forceinline__ int cellc(R p, const CellGrid& g, double inv_cs, int d) {
     if (d >= g.dim) return 0;
-    int c = (int)floor(((double)p - g.lo[d]) / g.cs);
+    int c = (int)floor(((double)p - g.lo[d]) * inv_cs);
     c = c < 0 ? 0 : c;
     return c >= g.nc[d] ? g.nc[d] - 1 : c;
+}
+
+template <typename V>
+__device__ __forceinline__ int cell_key(const V& p, const CellGrid& g, double inv_cs) {
+    return (cellc(p.x, g, inv_cs, 0) * g.nc[1] + cellc(p.y, g, inv_cs, 1)) * g.nc[2] +
+           cellc(p.z, g, inv_cs, 2);
 }
 
 // take_step1 (simulate.cpp:56-109) + the cell key of the start-of-step point
@@ -159,16 +192,12 @@ __global__ void sdpd_begin(SdpdDev<R> D) {
         isnan((double)v.y) || isinf((double)v.y) || isnan((double)v.z) || isinf((double)v.z) ||
         isnan((double)rho) || isinf((double)rho))
         atomicOr(D.flag, 2);
-    const int c = (cellc<R>(p.x, D.g, 0) * D.g.nc[1] + cellc<R>(p.y, D.g, 1)) * D.g.nc[2] +
-                  cellc<R>(p.z, D.g, 2);
-    const int slot = atomicAdd(&D.ccnt[c], 1);
-    if (slot < kCellCap) {
-        D.cidx[c * kCellCap + slot] = i;
-        D.cpos[c * kCellCap + slot] = p;
-        if (kComp<R>) D.cpos_lo[c * kCellCap + slot] = pl;
-    } else {
-        atomicOr(D.flag, 4);
-    }
+    // positions change only in the predictor, so the cell of this step's
+    // start-of-step point is the cell of the last step's moved point
+    const int c = D.step == 0 ? cell_key(p, D.g, D.inv_cs) : D.qkey[i];
+    D.ckey[i] = c;
+    D.crank[i] = atomicAdd(&D.ccnt[c], 1);
+    int qc = c;
     D.pold[i] = p;
     if (kComp<R>) D.pold_lo[i] = pl;
     if (!D.stat && !D.fixed[i]) {
@@ -192,6 +221,7 @@ __global__ void sdpd_begin(SdpdDev<R> D) {
             p.y = p.y + D.dt * t.y;
             p.z = p.z + D.dt * t.z;
         }
+        qc = cell_key(p, D.g, D.inv_cs);
         rho = rho + hdt * F.w;
         D.vel[i] = v;
         D.vt[i] = t;
@@ -210,6 +240,7 @@ __global__ void sdpd_begin(SdpdDev<R> D) {
     Fb.x = 0; Fb.y = 0; Fb.z = 0; Fb.w = 0;
     D.Fbp[i] = Fb;
     D.orho[i] = rho;
+    D.qkey[i] = qc;
     // the pressure term P/rho^2 and the volume m/rho of this particle, as the
     // force pass evaluates them for every pair it is in (model.cpp:105-120)
     if constexpr (kComp<R>) {
@@ -225,119 +256,277 @@ __global__ void sdpd_begin(SdpdDev<R> D) {
     }
 }
 
-// find_neighbors against the step's tree points + pairwiseForce (model.cpp:39-191)
-template <typename R, int KCAP, int TB>
-__global__ void __launch_bounds__(TB) sdpd_pairs(SdpdDev<R> D, int first_step) {
-    // per-thread sorted candidate lists in shared memory, element k of
-    // thread t at [k * TB + t] (consecutive threads, consecutive banks)
-    __shared__ R sd2[KCAP * TB];
-    __shared__ int sj[KCAP * TB];
-    const int tid = threadIdx.x;
-    R* cd2 = sd2 + tid;
-    int* cj = sj + tid;
+// Exclusive scan of the per-cell counts into the cell starts (start[ncell_pad]
+// = number of particles), resetting the counts to zero for the next step.
+// One CTA of 32 warps; warp w owns a contiguous segment of cells, read as
+// int4 rows (coalesced).  Pass 1 sums each segment, one block-level scan
+// orders the 32 segment totals, pass 2 writes the starts.  ncell_pad is a
+// multiple of 16 and the padding cells stay empty.
+__global__ void __launch_bounds__(1024) sdpd_cell_scan(int* cnt, int* start, int ncell_pad) {
+    __shared__ int wsum[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int rows = ncell_pad / 4;                 // int4 rows
+    const int per = (rows + 31) / 32;               // rows per warp
+    const int r0 = wid * per, r1 = min(r0 + per, rows);
+    const int4* c4 = reinterpret_cast<const int4*>(cnt);
+    int tot = 0;
+    for (int r = r0 + lane; r < r1; r += 32) {
+        const int4 v = c4[r];
+        tot += v.x + v.y + v.z + v.w;
+    }
+#pragma unroll
+    for (int d = 16; d >= 1; d >>= 1) tot += __shfl_xor_sync(SP_FULL, tot, d);
+    if (lane == 0) wsum[wid] = tot;
+    __syncthreads();
+    if (wid == 0) {
+        const int v = wsum[lane];
+        int incl = v;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int t = __shfl_up_sync(SP_FULL, incl, d);
+            if (lane >= d) incl += t;
+        }
+        wsum[lane] = incl - v;
+        if (lane == 31) start[ncell_pad] = incl;
+    }
+    __syncthreads();
+    int carry = wsum[wid];
+    int4* s4 = reinterpret_cast<int4*>(start);
+    int4* w4 = reinterpret_cast<int4*>(cnt);
+    for (int b = r0; b < r1; b += 32) {
+        const int r = b + lane;
+        int4 v = make_int4(0, 0, 0, 0);
+        if (r < r1) v = c4[r];
+        const int row = v.x + v.y + v.z + v.w;
+        int incl = row;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int t = __shfl_up_sync(SP_FULL, incl, d);
+            if (lane >= d) incl += t;
+        }
+        if (r < r1) {
+            int run = carry + incl - row;
+            int4 o;
+            o.x = run; run += v.x;
+            o.y = run; run += v.y;
+            o.z = run; run += v.z;
+            o.w = run;
+            s4[r] = o;
+            w4[r] = make_int4(0, 0, 0, 0);
+        }
+        carry += __shfl_sync(SP_FULL, incl, 31);
+    }
+}
+
+// Counting-sort scatter: particle i goes to slot cstart[cell] + rank, with
+// the data the force pass and the corrector read about a neighbour packed
+// into float4s (velocity .w: post-predictor density; transport velocity .w:
+// 1 for a fixed particle).
+template <typename R>
+__global__ void sdpd_scatter(SdpdDev<R> D) {
+    using V = typename Vec4<R>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= D.N) return;
-    // at the first step of a run the lists come from the unmoved points (take_step1)
-    const auto q = first_step ? D.pold[i] : D.pos[i];
-    typename Vec4<R>::T ql{};
-    if (kComp<R>) ql = first_step ? D.pold_lo[i] : D.plo[i];
-    const R h = D.h, sq = h * h;
+    const int sl = D.cstart[D.ckey[i]] + D.crank[i];
+    D.slot_of[i] = sl;
+    V tp = D.pold[i];
+    tp.w = idx_bits((R)0, i);
+    D.s_tp[sl] = tp;
+    V x = D.pos[i];
+    x.w = D.mass[i];
+    D.s_x[sl] = x;
+    if (kComp<R>) {
+        D.s_tplo[sl] = D.pold_lo[i];
+        D.s_xlo[sl] = D.plo[i];
+    }
+    V v = D.vel[i];
+    v.w = D.orho[i];               // post-predictor density (Shepard filter)
+    D.s_v[sl] = v;
+    V t = D.vt[i];
+    t.w = D.fixed[i] ? (R)1 : (R)0;
+    D.s_vt[sl] = t;
+    V a;
+    a.x = D.rfull[i];
+    a.y = D.pr[i];
+    a.z = D.wv[i];
+    a.w = D.nu[i];
+    D.s_aux[sl] = a;
+}
+
+// Force pass of one step: find_neighbors against the step's tree points and
+// pairwiseForce (particle.cpp:240-294, model.cpp:39-191), and with CORRECT
+// the corrector take_step2 with filterDensity and the boundary volume
+// fraction (simulate.cpp:132-173, model.cpp:194-329).
+//
+// One thread per particle, threads taking particles in cell order, so a
+// warp's particles share neighbour cells and their cache lines.  The 3^dim
+// cells around the query point are nine runs of consecutive slots in the
+// cell-ordered copies; every tree point within h is insertion-sorted into the
+// thread's list in shared memory by the key (r^2, j), the reference's list
+// order.  The pairs are then evaluated in list order with the sums (forces,
+// background force, density rate and the corrector's list sums) kept in
+// registers, so the summation order is the reference's.  Every neighbour value
+// comes from the cell-ordered copies, which nothing writes during the pass,
+// so the corrector can run here: it writes only the particle's own state.
+// Force pass of one step: find_neighbors against the step's tree points and
+// pairwiseForce (particle.cpp:240-294, model.cpp:39-191), and with CORRECT
+// the corrector take_step2 with filterDensity and the boundary volume
+// fraction (simulate.cpp:132-173, model.cpp:194-329).
+//
+// One thread per particle, threads taking particles in cell order, so a
+// warp's particles share neighbour cells and their cache lines.  The 3^dim
+// cells around the query point are nine runs of consecutive slots in the
+// cell-ordered copies; every tree point within h is insertion-sorted into the
+// thread's list in shared memory by the key (r^2, j), the reference's list
+// order.  The pairs are then evaluated in list order with the sums (forces,
+// background force, density rate and the corrector's list sums) kept in
+// registers, so the summation order is the reference's.  Every neighbour value
+// comes from the cell-ordered copies, which nothing writes during the pass,
+// so the corrector can run here: it writes only the particle's own state.
+template <typename R> struct ListKey;
+template <> struct ListKey<float> {   // r^2 >= 0 orders like its bit pattern
+    using T = unsigned long long;
+    __device__ static T make(float d2, int j) {
+        return ((unsigned long long)__float_as_uint(d2) << 32) | (unsigned)j;
+    }
+    __device__ static float d2(T k) { return __uint_as_float((unsigned)(k >> 32)); }
+    __device__ static int j(T k) { return (int)(unsigned)k; }
+};
+template <> struct ListKey<double> {
+    using T = double2;   // (r^2, j as double)
+    __device__ static T make(double d2, int j) { return make_double2(d2, (double)j); }
+    __device__ static double d2(T k) { return k.x; }
+    __device__ static int j(T k) { return (int)k.y; }
+};
+__device__ __forceinline__ bool key_less(unsigned long long a, unsigned long long b) { return a < b; }
+__device__ __forceinline__ bool key_less(double2 a, double2 b) {
+    return a.x < b.x || (a.x == b.x && a.y < b.y);
+}
+
+template <typename R> struct PairShape;
+template <> struct PairShape<float> { static constexpr int TB = 64, MINB = 9; };
+template <> struct PairShape<double> { static constexpr int TB = 64, MINB = 5; };
+
+template <typename R, int KCAP, bool CORRECT>
+__global__ void __launch_bounds__(PairShape<R>::TB, PairShape<R>::MINB)
+    sdpd_pairs(SdpdDev<R> D, int first_step) {
+    using V = typename Vec4<R>::T;
+    using K = ListKey<R>;
+    constexpr int TB = PairShape<R>::TB;
+    // element k of thread t at [k * TB + t]: consecutive threads, consecutive banks
+    __shared__ typename K::T list_all[KCAP * TB];
+    typename K::T* list = list_all + threadIdx.x;
+    const int s = blockIdx.x * TB + threadIdx.x;
+    if (s >= D.N) return;
+    const int i = bits_idx(D.s_tp[s].w);
     const int dim = D.dim;
-    const int c0 = cellc<R>(q.x, D.g, 0), c1 = cellc<R>(q.y, D.g, 1), c2 = cellc<R>(q.z, D.g, 2);
-    int m = 0;
-    bool over = false;
+    const R h = D.h;
+    // at the first step of a run the lists come from the unmoved points (take_step1)
+    const V q = first_step ? D.pold[i] : D.pos[i];
+    V ql{};
+    if (kComp<R>) ql = first_step ? D.pold_lo[i] : D.plo[i];
+    const V ti = D.vt[i];
     R self_d2 = 0;
     if (D.self_step && !first_step) {
-        const auto t = D.vt[i];
-        const R a = D.dt * t.x, b = D.dt * t.y, c = D.dt * t.z;
+        const R a = D.dt * ti.x, b = D.dt * ti.y, c = D.dt * ti.z;
         self_d2 = a * a;
         if (dim > 1) self_d2 = self_d2 + b * b;
         if (dim > 2) self_d2 = self_d2 + c * c;
         if (D.stat || D.fixed[i]) self_d2 = 0;
     }
+    const int key = first_step ? D.ckey[i] : D.qkey[i];
+    const int n0 = D.g.nc[0], n1 = D.g.nc[1], n2 = D.g.nc[2];
+    const int c2 = key % n2, c1 = (key / n2) % n1, c0 = key / (n2 * n1);
+    const int zlo = c2 > 0 ? c2 - 1 : 0, zhi = c2 + 1 < n2 ? c2 + 1 : n2 - 1;
+    const int kc = KCAP < D.kcap ? KCAP : D.kcap;
+    const R acc2 = D.acc2;
+    int m = 0;
+    bool over = false;
     for (int a = c0 - 1; a <= c0 + 1; a++) {
-        if (a < 0 || a >= D.g.nc[0]) continue;
+        if (a < 0 || a >= n0) continue;
         for (int b = c1 - 1; b <= c1 + 1; b++) {
-            if (b < 0 || b >= D.g.nc[1]) continue;
-            for (int c = c2 - 1; c <= c2 + 1; c++) {
-                if (c < 0 || c >= D.g.nc[2]) continue;
-                const int cid = (a * D.g.nc[1] + b) * D.g.nc[2] + c;
-                int e = D.ccnt[cid];
-                e = e < kCellCap ? e : kCellCap;
-                for (int t = 0; t < e; t++) {
-                    const int j = D.cidx[cid * kCellCap + t];
-                    const auto p = D.cpos[cid * kCellCap + t];
-                    R t0 = q.x - p.x, t1 = q.y - p.y, t2 = q.z - p.z;
-                    if constexpr (kComp<R>) {
-                        const auto pl = D.cpos_lo[cid * kCellCap + t];
-                        t0 = t0 + (ql.x - pl.x);
-                        t1 = t1 + (ql.y - pl.y);
-                        t2 = t2 + (ql.z - pl.z);
-                    }
-                    R d2 = 0;
-                    d2 = d2 + t0 * t0;
-                    if (dim > 1) d2 = d2 + t1 * t1;
-                    if (dim > 2) d2 = d2 + t2 * t2;
-                    if (D.self_step && j == i) d2 = self_d2;
-                    if (d2 > sq || d2 == (R)0) continue;     // kd_fix_rad_search.cpp:160-174
-                    if (sqrt(d2) > h) continue;              // particle.cpp:160-162
-                    if (m >= KCAP || m >= D.kcap) { over = true; continue; }
-                    int k = m++;
-                    while (k > 0) {
-                        const R pd = cd2[(k - 1) * TB];
-                        const int pj = cj[(k - 1) * TB];
-                        if (!(d2 < pd || (d2 == pd && j < pj))) break;
-                        cd2[k * TB] = pd;
-                        cj[k * TB] = pj;
-                        k--;
-                    }
-                    cd2[k * TB] = d2;
-                    cj[k * TB] = j;
+            if (b < 0 || b >= n1) continue;
+            const int cb = (a * n1 + b) * n2;
+            const int e = D.cstart[cb + zhi + 1];
+            for (int sl = D.cstart[cb + zlo]; sl < e; sl++) {
+                const V pt = D.s_tp[sl];
+                const int j = bits_idx(pt.w);
+                R e0 = q.x - pt.x, e1 = q.y - pt.y, e2 = q.z - pt.z;
+                if constexpr (kComp<R>) {
+                    const V pl = D.s_tplo[sl];
+                    e0 = e0 + (ql.x - pl.x);
+                    e1 = e1 + (ql.y - pl.y);
+                    e2 = e2 + (ql.z - pl.z);
                 }
+                R d2 = 0;
+                d2 = d2 + e0 * e0;
+                if (dim > 1) d2 = d2 + e1 * e1;
+                if (dim > 2) d2 = d2 + e2 * e2;
+                if (D.self_step && j == i) d2 = self_d2;
+                // d2 <= h^2 (kd_fix_rad_search.cpp:160-174) and sqrt(d2) <= h
+                // (particle.cpp:160-162) in one compare: acc2 is the largest
+                // value passing both (sqrt is correctly rounded and monotone)
+                if (d2 > acc2 || d2 == (R)0) continue;
+                if (m >= kc) {
+                    over = true;
+                    continue;
+                }
+                const typename K::T kk = K::make(d2, j);
+                int k = m++;
+                while (k > 0) {
+                    const typename K::T prev = list[(k - 1) * TB];
+                    if (!key_less(kk, prev)) break;
+                    list[k * TB] = prev;
+                    k--;
+                }
+                list[k * TB] = kk;
             }
         }
     }
-    if (over) atomicOr(D.flag, 1);
-    D.ncnt[i] = m;
+    // pairs in list order
     const R alpha = D.alpha;
-    const auto xi = D.pos[i];
-    typename Vec4<R>::T xli{};
+    const V xi = D.pos[i];
+    V xli{};
     if (kComp<R>) xli = D.plo[i];
-    const auto vi = D.vel[i];
-    const auto ti = D.vt[i];
-    const R rhoi = D.rfull[i], mi = D.mass[i], nui = D.nu[i];
+    const V vi = D.vel[i];
+    const R rhoi = D.rfull[i], mi = D.mass[i], nui = D.nu[i], rho_i = D.rho[i];
     const R P0 = D.P0, rho0 = D.rho0;
-    const R Pi = kComp<R> ? P0 * (D.rho[i] / rho0) : P0 * (rhoi / rho0 - (R)1.0);
+    const R Pi = kComp<R> ? P0 * (rho_i / rho0) : P0 * (rhoi / rho0 - (R)1.0);
     const R pri = Pi / (rhoi * rhoi), npri = -Pi / (rhoi * rhoi), wi = D.wv[i];
+    const R imi = (R)1.0 / mi;
     R Fx = D.g0, Fy = D.g1, Fz = D.g2, Bx = 0, By = 0, Bz = 0, Fr = 0;
+    R num = 0, den = 0, vos = 0, vtot = 0, nw0 = 0, nw1 = 0, nw2 = 0;
+    const size_t row = (size_t)i * D.kcap;
     for (int k = 0; k < m; k++) {
-        const int j = cj[k * TB];
-        const R r = sqrt(cd2[k * TB]);
+        const typename K::T kk = list[k * TB];
+        const R d2 = K::d2(kk);
+        const int j = K::j(kk);
+        const int sl = D.slot_of[j];
+        const R r = sqrt(d2);
         const R R_ = r / h;
         const R dWdr = alpha * ((R)-12 * r / (h * h)) * (((R)1 - R_) * ((R)1 - R_));
-        const size_t o = (size_t)i * D.kcap + k;
-        D.nidx[o] = j;
-        D.ndist[o] = r;
-        D.ndw[o] = dWdr;
+        D.nidx[row + k] = j;
+        D.ndist[row + k] = r;
+        D.ndw[row + k] = dWdr;
+        const V xj = D.s_x[sl];      // .w: mass
+        const V aux = D.s_aux[sl];   // rho, P/rho^2, m/rho, nu
+        const R mj = xj.w, rhoj = aux.x;
         if (D.ndij) {
             // D_ij of add_to_neighbor_list (particle.cpp:181-187) from the
             // post-predictor densities, in the reference's operator order
-            const R r2 = cd2[k * TB];
             const R ih = (R)1.0 / h;
             const R ihsq = ih * ih;
             const R dhr = h - r;
             const R wfd = (R)-25.066903536973515383 * dhr * dhr * ihsq * ihsq * ihsq * ih;
-            const R mj = D.mass[j], rj = D.rfull[j];
-            D.ndij[o] = (R)-2.0 * (mi * mj) / (mi + mj) * (rhoi + rj) / (rhoi * rj) * r2 * wfd /
-                        (r2 + (R)0.01 * h * h);
+            D.ndij[row + k] = (R)-2.0 * (mi * mj) / (mi + mj) * (rhoi + rhoj) / (rhoi * rhoj) *
+                              d2 * wfd / (d2 + (R)0.01 * h * h);
         }
         if (R_ > (R)1.0 || r == (R)0) continue;
-        const auto xj = D.pos[j];
-        const auto vj4 = D.vel[j];
-        const auto tj = D.vt[j];
+        const V vj4 = D.s_v[sl];     // .w: post-predictor density
+        const V tj = D.s_vt[sl];     // .w: 1 when fixed
         R ex0 = xi.x - xj.x, ex1 = xi.y - xj.y, ex2 = xi.z - xj.z;
         if constexpr (kComp<R>) {
-            const auto xlj = D.plo[j];
+            const V xlj = D.s_xlo[sl];
             ex0 = ex0 + (xli.x - xlj.x);
             ex1 = ex1 + (xli.y - xlj.y);
             ex2 = ex2 + (xli.z - xlj.z);
@@ -346,16 +535,17 @@ __global__ void __launch_bounds__(TB) sdpd_pairs(SdpdDev<R> D, int first_step) {
         dx0 = ex0; dv0 = vi.x - vj4.x; dvdx = dvdx + dv0 * dx0;
         if (dim > 1) { dx1 = ex1; dv1 = vi.y - vj4.y; dvdx = dvdx + dv1 * dx1; }
         if (dim > 2) { dx2 = ex2; dv2 = vi.z - vj4.z; dvdx = dvdx + dv2 * dx2; }
-        const R rhoj = D.rfull[j], mj = D.mass[j], nuj = D.nu[j];
-        const R prj = D.pr[j];                 // Pj / (rhoj * rhoj)
+        const R nuj = aux.w;
+        const R prj = aux.y;                  // Pj / (rhoj * rhoj)
         R pg = pri + prj;
         if (pg < 0) pg = npri + prj;
         const R rh = r + (R)0.001 * h;
         const R fp = (R)-1.0 * mj * pg * dWdr / rh;
-        const R fv = mj * ((R)2.0 * (nui * nuj) / (nui + nuj)) * ((R)1 / rh) * dWdr / (rhoi * rhoj);
-        const R wj = D.wv[j];                   // mj / rhoj
+        const R fv = mj * ((R)2.0 * (nui * nuj) / (nui + nuj)) * ((R)1 / rh) * dWdr /
+                     (rhoi * rhoj);
+        const R wj = aux.z;                   // mj / rhoj
         const R ss = wi * wi + wj * wj;
-        const R fbp = (R)-10.0 * P0 * ((R)1.0 / mi) * ss * dWdr / rh;
+        const R fbp = (R)-10.0 * P0 * imi * ss * dWdr / rh;
         const R a0 = ti.x - vi.x, a1 = ti.y - vi.y, a2 = ti.z - vi.z;
         const R b0 = tj.x - vj4.x, b1 = tj.y - vj4.y, b2 = tj.z - vj4.z;
         R ft[3];
@@ -365,7 +555,7 @@ __global__ void __launch_bounds__(TB) sdpd_pairs(SdpdDev<R> D, int first_step) {
             const R T0 = (R)0.5 * ((rhoi * via[q2] * a0) + (rhoj * vja[q2] * b0));
             const R T1 = (R)0.5 * ((rhoi * via[q2] * a1) + (rhoj * vja[q2] * b1));
             const R T2 = (R)0.5 * ((rhoi * via[q2] * a2) + (rhoj * vja[q2] * b2));
-            ft[q2] = ((R)1.0 / mi) * ss * (T0 * dx0 + T1 * dx1 + T2 * dx2) * dWdr / rh;
+            ft[q2] = imi * ss * (T0 * dx0 + T1 * dx1 + T2 * dx2) * dWdr / rh;
         }
         Fx = Fx + (fp * dx0 + fv * dv0 + ft[0]);
         Bx = Bx + fbp * dx0;
@@ -375,13 +565,69 @@ __global__ void __launch_bounds__(TB) sdpd_pairs(SdpdDev<R> D, int first_step) {
         const R tvj = (vj4.x - tj.x) * dx0 + (vj4.y - tj.y) * dx1 + (vj4.z - tj.z) * dx2;
         Fr = Fr + rhoi * wj * dvdx * ((R)1 / rh) * dWdr -
              wj * (rhoi * tvi + rhoj * tvj) * ((R)1.0 / rh) * dWdr;
+        if constexpr (CORRECT) {
+            // the list sums of filterDensity and of the boundary volume fraction
+            const R omr = (R)1 - R_;
+            const R W = alpha * (((R)1 + (R)3 * R_) * (omr * omr * omr));
+            num = num + vj4.w * W;
+            den = den + W;
+            const R vv = wj * wj;
+            const bool solid = tj.w != (R)0;
+            if (solid) vos = vos + vv * W;
+            vtot = vtot + vv * W;
+            if (solid) {
+                nw0 = nw0 + vv * dx0 * dWdr / rh;
+                nw1 = nw1 + vv * dx1 * dWdr / rh;
+                nw2 = nw2 + vv * dx2 * dWdr / rh;
+            }
+        }
     }
-    auto F = D.F[i];
+    D.ncnt[i] = m;
+    if (over) atomicOr(D.flag, 1);
+    V F;
     F.x = Fx; F.y = Fy; F.z = Fz; F.w = Fr;
     D.F[i] = F;
-    auto B = D.Fbp[i];
-    B.x = Bx; B.y = By; B.z = Bz;
+    V B;   // .w is zero since the predictor
+    B.x = Bx; B.y = By; B.z = Bz; B.w = 0;
     D.Fbp[i] = B;
+    if constexpr (CORRECT) {
+        const bool fixed_i = D.fixed[i];
+        const bool fluid = !fixed_i && !D.stat, wall = fixed_i && !D.stat;
+        const R hdt = (R)0.5 * D.dt;
+        V v = vi;
+        R rho = rho_i;
+        if (fluid) {
+            v.x = v.x + hdt * F.x;
+            v.y = v.y + hdt * F.y;
+            v.z = v.z + hdt * F.z;
+        }
+        if ((fluid || wall) && D.step % 20 == 0) rho = num / den;
+        if (fluid) {
+            rho = rho + hdt * F.w;
+            nw0 = nw0 / vtot;
+            nw1 = nw1 / vtot;
+            nw2 = nw2 / vtot;
+            const R nn = sqrt(nw0 * nw0 + nw1 * nw1 + nw2 * nw2);
+            const R n0 = -nw0 / nn, n1 = -nw1 / nn, n2n = -nw2 / nn;
+            const R phi = fabs(vos / vtot);
+            const R vdn = v.x * n0 + v.y * n1 + v.z * n2n;
+            V t = ti;
+            t.x = 0;
+            if (dim > 1) t.y = 0;
+            if (dim > 2) t.z = 0;
+            D.vt[i] = t;
+            if (phi >= (R)0.5) {   // applyBoundaryVolumeFraction, model.cpp:316-329
+                const R mx = vdn > (R)0.0 ? vdn : (R)0.0;
+                v.x = -v.x + (R)2.0 * mx * n0;
+                if (dim > 1) v.y = -v.y + (R)2.0 * mx * n1;
+                if (dim > 2) v.z = -v.z + (R)2.0 * mx * n2n;
+            }
+        }
+        if (D.nbc) flow_bcs(D, i, xi, v, rho);   // applyBoundaryConditions, simulate.cpp:171
+        D.vel[i] = v;
+        D.rho[i] = rho;
+        if (kComp<R>) D.rfull[i] = D.rho0 + rho;
+    }
 }
 
 // take_step2 (simulate.cpp:132-173), filterDensity and the boundary volume
@@ -488,13 +734,19 @@ struct SdpdState {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     std::vector<void*> allocs;
     void *pos = nullptr, *vel = nullptr, *vt = nullptr, *F = nullptr, *Fbp = nullptr,
-         *pold = nullptr, *cpos = nullptr, *rho = nullptr, *orho = nullptr, *mass = nullptr,
+         *pold = nullptr, *rho = nullptr, *orho = nullptr, *mass = nullptr,
          *nu = nullptr, *ndist = nullptr, *ndw = nullptr, *pr = nullptr, *wv = nullptr;
-    // FP32 only: lo parts of positions (current, start of step, cell slots)
-    // and the float densities rho0 + deviation
-    void *plo = nullptr, *pold_lo = nullptr, *cpos_lo = nullptr, *rfull = nullptr;
+    // FP32 only: lo parts of positions (current, start of step) and the float
+    // densities rho0 + deviation
+    void *plo = nullptr, *pold_lo = nullptr, *rfull = nullptr;
+    // cell-ordered copies (the lo parts in FP32 only)
+    void *s_tp = nullptr, *s_tplo = nullptr, *s_x = nullptr, *s_xlo = nullptr, *s_v = nullptr,
+         *s_vt = nullptr, *s_aux = nullptr;
     uint8_t* fixed = nullptr;
-    int *ccnt = nullptr, *cidx = nullptr, *ncnt = nullptr, *nidx = nullptr, *flag = nullptr;
+    int *ccnt = nullptr, *cstart = nullptr, *ckey = nullptr, *crank = nullptr, *qkey = nullptr,
+        *slot_of = nullptr;
+    int ncell_pad = 0;   // cells rounded up to a multiple of 16 (the scan's int4 rows)
+    int *ncnt = nullptr, *nidx = nullptr, *flag = nullptr;
     void* ndij = nullptr;
     // initial state (REAL-typed 4-vectors and densities) for sdpd_reset
     std::vector<unsigned char> init_pos, init_vel, init_rho, init_nu, init_lo, init_rfull;
@@ -533,16 +785,28 @@ static SdpdDev<R> dev_view(SdpdState* s) {
     const R h = (R)s->h;
     D.alpha = s->dim == 3 ? (R)105 / ((R)16 * (R)M_PI * h * h * h)
             : s->dim == 2 ? (R)5 / ((R)M_PI * h * h) : h;
+    // the list predicate d2 <= h*h && sqrt(d2) <= h as one compare: sqrt is
+    // correctly rounded and monotone here and on the device, so the largest
+    // passing value is found by stepping down from h*h
+    {
+        R a2 = h * h;
+        while (a2 > (R)0 && std::sqrt(a2) > h) a2 = std::nextafter(a2, (R)0);
+        D.acc2 = a2;
+    }
     D.g0 = (R)s->g[0];
     D.g1 = (R)s->g[1];
     D.g2 = (R)s->g[2];
     D.pos = (V*)s->pos; D.vel = (V*)s->vel; D.vt = (V*)s->vt; D.F = (V*)s->F; D.Fbp = (V*)s->Fbp;
-    D.pold = (V*)s->pold; D.cpos = (V*)s->cpos;
-    D.plo = (V*)s->plo; D.pold_lo = (V*)s->pold_lo; D.cpos_lo = (V*)s->cpos_lo;
+    D.pold = (V*)s->pold;
+    D.plo = (V*)s->plo; D.pold_lo = (V*)s->pold_lo;
     D.rho = (R*)s->rho; D.orho = (R*)s->orho; D.mass = (R*)s->mass; D.nu = (R*)s->nu;
     D.rfull = kComp<R> ? (R*)s->rfull : (R*)s->rho;
     D.fixed = s->fixed;
-    D.ccnt = s->ccnt; D.cidx = s->cidx;
+    D.ccnt = s->ccnt; D.cstart = s->cstart; D.ckey = s->ckey; D.crank = s->crank;
+    D.qkey = s->qkey;
+    D.slot_of = s->slot_of;
+    D.s_tp = (V*)s->s_tp; D.s_tplo = (V*)s->s_tplo; D.s_x = (V*)s->s_x; D.s_xlo = (V*)s->s_xlo;
+    D.s_v = (V*)s->s_v; D.s_vt = (V*)s->s_vt; D.s_aux = (V*)s->s_aux;
     D.ncnt = s->ncnt; D.nidx = s->nidx; D.ndist = (R*)s->ndist; D.ndw = (R*)s->ndw;
     D.ndij = (R*)s->ndij;
     D.pr = (R*)s->pr;
@@ -555,6 +819,7 @@ static SdpdDev<R> dev_view(SdpdState* s) {
     D.bc_value = s->bc_value;
     D.kcap = s->kcap;
     D.g = s->grid;
+    D.inv_cs = 1.0 / s->grid.cs;
     D.flag = s->flag;
     return D;
 }
@@ -564,19 +829,17 @@ static bool upload(SdpdState* s, const sp_scenario& sc, std::string* err) {
     using V = typename Vec4<R>::T;
     const int N = sc.num_particles;
     const size_t v4 = sizeof(V) * N, r1 = sizeof(R) * N;
-    void** four[] = {&s->pos, &s->vel, &s->vt, &s->F, &s->Fbp, &s->pold};
+    void** four[] = {&s->pos, &s->vel, &s->vt, &s->F, &s->Fbp, &s->pold,
+                     &s->s_tp, &s->s_x, &s->s_v, &s->s_vt, &s->s_aux};
     for (void** p : four)
         if (!sd_alloc(s, p, v4, err)) return false;
-    if (!sd_alloc(s, &s->cpos, sizeof(V) * (size_t)s->grid.ncell * kCellCap, err)) return false;
     void** ones[] = {&s->rho, &s->orho, &s->mass, &s->nu, &s->pr, &s->wv};
     for (void** p : ones)
         if (!sd_alloc(s, p, r1, err)) return false;
     if (kComp<R>) {
-        void** lo[] = {&s->plo, &s->pold_lo};
+        void** lo[] = {&s->plo, &s->pold_lo, &s->s_tplo, &s->s_xlo};
         for (void** p : lo)
             if (!sd_alloc(s, p, v4, err)) return false;
-        if (!sd_alloc(s, &s->cpos_lo, sizeof(V) * (size_t)s->grid.ncell * kCellCap, err))
-            return false;
         if (!sd_alloc(s, &s->rfull, r1, err)) return false;
     }
     std::vector<V> pos(N), zero(N), vel(N), lo(N);
@@ -654,11 +917,16 @@ SdpdState* sdpd_create(const sp_scenario& sc, int precision, int self_step, cuda
         s->grid.nc[d] += 8;
     }
     s->grid.ncell = s->grid.nc[0] * s->grid.nc[1] * s->grid.nc[2];
+    s->ncell_pad = (s->grid.ncell + 15) / 16 * 16;
     const int N = s->N;
     bool ok = sd_alloc(s, (void**)&s->fixed, N, err) &&
               sd_alloc(s, (void**)&s->type, sizeof(int) * N, err) &&
-              sd_alloc(s, (void**)&s->ccnt, sizeof(int) * s->grid.ncell, err) &&
-              sd_alloc(s, (void**)&s->cidx, sizeof(int) * (size_t)s->grid.ncell * kCellCap, err) &&
+              sd_alloc(s, (void**)&s->ccnt, sizeof(int) * s->ncell_pad, err) &&
+              sd_alloc(s, (void**)&s->cstart, sizeof(int) * (s->ncell_pad + 4), err) &&
+              sd_alloc(s, (void**)&s->ckey, sizeof(int) * N, err) &&
+              sd_alloc(s, (void**)&s->crank, sizeof(int) * N, err) &&
+              sd_alloc(s, (void**)&s->qkey, sizeof(int) * N, err) &&
+              sd_alloc(s, (void**)&s->slot_of, sizeof(int) * N, err) &&
               sd_alloc(s, (void**)&s->ncnt, sizeof(int) * N, err) &&
               sd_alloc(s, (void**)&s->nidx, sizeof(int) * (size_t)N * s->kcap, err) &&
               sd_alloc(s, (void**)&s->flag, sizeof(int), err);
@@ -680,6 +948,7 @@ SdpdState* sdpd_create(const sp_scenario& sc, int precision, int self_step, cuda
         cudaMemcpyAsync(s->type, sc.type, sizeof(int) * N, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(s->fixed, sc.fixed, N, cudaMemcpyHostToDevice, st);
         cudaMemsetAsync(s->ncnt, 0, sizeof(int) * N, st);
+        cudaMemsetAsync(s->ccnt, 0, sizeof(int) * s->ncell_pad, st);   // the scan keeps it zero
         ok = s->prec == SP_PREC_F64 ? upload<double>(s, sc, err) : upload<float>(s, sc, err);
     }
     if (!ok) {
@@ -698,16 +967,35 @@ void sdpd_destroy(SdpdState* s) {
     delete s;
 }
 
+// one part of a step: 0 predictor (begin); 1 lists + forces (scan, scatter,
+// pairs), with the corrector fused into the pairs when `correct`; 2 the
+// corrector on its own (for callers that read the force-pass state in between)
 template <typename R>
-static void enqueue_step(SdpdState* s, int step) {
+static void enqueue_part(SdpdState* s, int step, int part, bool correct) {
     const int N = s->N, tb = 128, nb = (N + tb - 1) / tb;
     SdpdDev<R> D = dev_view<R>(s);
     D.step = step;
-    cudaMemsetAsync(s->ccnt, 0, sizeof(int) * s->grid.ncell, s->st);
-    sdpd_begin<R><<<nb, tb, 0, s->st>>>(D);
-    constexpr int TP = sizeof(R) == 4 ? 128 : 64;   // 48 KB of list slots per block
-    sdpd_pairs<R, 48, TP><<<(N + TP - 1) / TP, TP, 0, s->st>>>(D, step == 0 ? 1 : 0);
-    sdpd_corrector<R><<<nb, tb, 0, s->st>>>(D);
+    if (part == 0) {
+        sdpd_begin<R><<<nb, tb, 0, s->st>>>(D);
+    } else if (part == 1) {
+        sdpd_cell_scan<<<1, 1024, 0, s->st>>>(s->ccnt, s->cstart, s->ncell_pad);
+        sdpd_scatter<R><<<nb, tb, 0, s->st>>>(D);
+        constexpr int TB = PairShape<R>::TB;
+        const int grid = (N + TB - 1) / TB;
+        if (correct)
+            sdpd_pairs<R, 48, true><<<grid, TB, 0, s->st>>>(D, step == 0);
+        else
+            sdpd_pairs<R, 48, false><<<grid, TB, 0, s->st>>>(D, step == 0);
+    } else {
+        sdpd_corrector<R><<<nb, tb, 0, s->st>>>(D);
+    }
+}
+
+// one step: begin, scan, scatter, pairs + corrector (kSdpdLaunchesPerStep)
+template <typename R>
+static void enqueue_step(SdpdState* s, int step) {
+    enqueue_part<R>(s, step, 0, true);
+    enqueue_part<R>(s, step, 1, true);
 }
 
 template <typename R>
@@ -733,12 +1021,12 @@ static int advance_t(SdpdState* s, int nsteps, double* ms, long long* launches, 
                 }
             }
             cudaGraphLaunch(s->graph20, s->st);
-            l += 60;
+            l += 20 * kSdpdLaunchesPerStep;
             k += 20;
             s->step += 20;
         } else {
             enqueue_step<R>(s, s->step);
-            l += 3;
+            l += kSdpdLaunchesPerStep;
             k++;
             s->step++;
         }
@@ -757,10 +1045,6 @@ static int advance_t(SdpdState* s, int nsteps, double* ms, long long* launches, 
     *launches = l;
     if (flag & 1) {
         *err = "SDPD: a particle has more neighbours than the list capacity (48)";
-        return SP_E_UNSUPPORTED;
-    }
-    if (flag & 4) {
-        *err = "SDPD: more than 16 particles in one cell of edge h";
         return SP_E_UNSUPPORTED;
     }
     if (flag & 2) {
@@ -868,6 +1152,7 @@ int sdpd_reset(SdpdState* s, std::string* err) {
     if (s->rfull)
         cudaMemcpyAsync(s->rfull, s->init_rfull.data(), r1, cudaMemcpyHostToDevice, s->st);
     cudaMemsetAsync(s->ncnt, 0, sizeof(int) * s->N, s->st);
+    cudaMemsetAsync(s->ccnt, 0, sizeof(int) * s->ncell_pad, s->st);
     cudaMemsetAsync(s->flag, 0, sizeof(int), s->st);
     cudaError_t e = cudaStreamSynchronize(s->st);   // host staging buffers stay valid
     if (e != cudaSuccess) {
@@ -886,19 +1171,8 @@ void sdpd_enqueue_step(SdpdState* s) {
 
 template <typename R>
 static void enqueue_phase_t(SdpdState* s, int phase) {
-    const int N = s->N, tb = 128, nb = (N + tb - 1) / tb;
-    SdpdDev<R> D = dev_view<R>(s);
-    D.step = s->step;
-    if (phase == 0) {
-        cudaMemsetAsync(s->ccnt, 0, sizeof(int) * s->grid.ncell, s->st);
-        sdpd_begin<R><<<nb, tb, 0, s->st>>>(D);
-    } else if (phase == 1) {
-        constexpr int TP = sizeof(R) == 4 ? 128 : 64;
-        sdpd_pairs<R, 48, TP><<<(N + TP - 1) / TP, TP, 0, s->st>>>(D, s->step == 0 ? 1 : 0);
-    } else {
-        sdpd_corrector<R><<<nb, tb, 0, s->st>>>(D);
-        s->step++;
-    }
+    enqueue_part<R>(s, s->step, phase, false);
+    if (phase == 2) s->step++;
 }
 
 void sdpd_enqueue_phase(SdpdState* s, int phase) {
@@ -974,10 +1248,6 @@ int sdpd_check_flag(SdpdState* s, std::string* err) {
     }
     if (flag & 1) {
         *err = "SDPD: a particle has more neighbours than the list capacity (48)";
-        return SP_E_UNSUPPORTED;
-    }
-    if (flag & 4) {
-        *err = "SDPD: more than 16 particles in one cell of edge h";
         return SP_E_UNSUPPORTED;
     }
     if (flag & 2) {

@@ -41,8 +41,9 @@ struct SdpdLists {
 int sdpd_enable_dij(SdpdState* s, std::string* err);            // lists carry D_ij from now on
 int sdpd_reset(SdpdState* s, std::string* err);                 // back to the initial state, step 0
 void sdpd_enqueue_step(SdpdState* s);                           // one step, no host sync
+constexpr int kSdpdLaunchesPerStep = 4;                       // kernels of one step
 // one step in three parts: 0 predictor (take_step1), 1 lists + forces,
-// 2 corrector (take_step2; advances the step counter)
+// 2 corrector (take_step2; advances the step counter); five kernels in all
 void sdpd_enqueue_phase(SdpdState* s, int phase);
 SdpdLists sdpd_lists(SdpdState* s);
 // vol = m / rho, 1/vol = rho / m from the current densities (float)
