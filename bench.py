@@ -51,9 +51,10 @@ B_RXN = 8 * 3 + 16 * 4 + 24 + 4 * 5              # 132
 # in the captured launch; profiles/nsm_advance_batchw4_rdme40.txt)
 DRAM_BYTES_PER_EVENT = 748.0
 # DRAM bytes (read + write) per particle of one sdpd_pairs launch (the
-# step's dominant kernel) from one ncu capture of --profile-sdpd: 37.0 MB
-# for 84,696 particles (profiles/sdpd_pairs_dambreak.txt)
-SDPD_PAIRS_DRAM_BYTES_PER_PARTICLE = 437.0
+# step's dominant kernel) from one ncu capture of --profile-sdpd with the
+# caches as the step leaves them: 55.8 MB for 84,696 particles
+# (profiles/sdpd_pairs_dambreak.txt)
+SDPD_PAIRS_DRAM_BYTES_PER_PARTICLE = 659.0
 
 
 def workload(intervals: int | None = None):
@@ -307,7 +308,8 @@ def run_sdpd(args):
                          "frac": achieved / peak,
                          "traffic": SDPD_PAIRS_DRAM_BYTES_PER_PARTICLE * sc.num_particles,
                          "traffic_note": "ncu DRAM bytes of one sdpd_pairs launch (the step's "
-                                         "dominant kernel; state fits in L2)",
+                                         "dominant kernel, caches as the step leaves "
+                                         "them; state fits in L2)",
                          "peak_source": src, "bytes_per_particle_step": B_SDPD}}
 
 
