@@ -369,11 +369,13 @@ def run_coupled(args, with_cpu: bool):
 def run_uneven(args):
     """Batched uneven ensemble: 4,096 birth-death instances (2-D/3-D
     lattices, 400-40,000 voxels log-uniform, rates and D within +-1 decade),
-    one trajectory each, all in one persistent launch per output interval
-    (warps take trajectories from an atomic counter).  The ensemble's
-    propensity totals span 4 decades (up to 1e9 events per unit time in one
-    trajectory), so a bounded sample is timed: the first K output intervals
-    of 0.01 (t in [0, 10] cut into 1,000 intervals)."""
+    one trajectory each, all in one persistent launch per output interval and
+    kernel group (warps take trajectories from an atomic counter).  The
+    ensemble's propensity totals span 4 decades (up to 1e9 events per unit
+    time in one trajectory), so a bounded sample is timed: the first K output
+    intervals of 0.01 (t in [0, 10] cut into 1,000 intervals).  e2e: sp_run of
+    the same K intervals through the C ABI, host u0 in, host per-voxel moment
+    sums out."""
     from spatialpy_gb300 import scenario as S
     from spatialpy_gb300.engine import Engine
     K = args.uneven_intervals
@@ -382,16 +384,29 @@ def run_uneven(args):
     build_s = time.perf_counter() - t0
     n = len(scs)
     seeds = np.arange(SEED0, SEED0 + n, dtype=np.uint64)
+    inst = np.arange(n, dtype=np.int32)
     with Engine(scs) as eng:
-        eng.start(seeds, instance=np.arange(n, dtype=np.int32))
+        eng.start(seeds, instance=inst)
         eng.advance(K)
         prof = eng.profile()
         ev = sum(eng.status(j)["events"] for j in range(n))
         eng.finish()
     sec = prof["total_ms"] / 1e3
+    # the same K intervals end to end
+    outs = np.arange(K + 1, dtype=np.int32)
+    scs_k = [sc.copy(num_steps=K, output_steps=outs) for sc in scs]
+    with Engine(scs_k) as e2:
+        t1 = time.perf_counter()
+        r2 = e2.run(seeds, instance=inst, want_counts=False, want_moments=True)
+        e2e_s = time.perf_counter() - t1
+    e2e_ev = float(r2["events"].sum())
+    h2d = sum(sc.u0.nbytes for sc in scs_k) + seeds.nbytes + inst.nbytes
+    d2h = sum(m.nbytes for m in r2["moments"]) + r2["events"].nbytes
     vox = sum(sc.num_particles for sc in scs)
     return {"metric": "SSA events/s (uneven ensemble)", "value": ev / sec, "unit": "events/s",
             "intervals": K, "ms_per_interval": prof["total_ms"] / K,
+            "e2e": {"value": e2e_ev / e2e_s, "unit": "events/s", "seconds": e2e_s,
+                    "h2d_bytes_per_step": h2d / K, "d2h_bytes_per_step": d2h / K},
             "gpu_launches": int(prof["launches"]), "event_kernel": prof["kernel"],
             "config": {"workload": "4,096 birth-death instances, 2-D/3-D, 400-40,000 "
                                    "voxels log-uniform, one trajectory each, first "

@@ -398,6 +398,33 @@ def test_mixed_kernel_groups_bitexact(oracle_lib):
         np.testing.assert_array_equal(res["events"][j], ev)
 
 
+def test_heavy_group_bitexact(oracle_lib):
+    """With more batch-size trajectories than three per SM the batch group
+    runs narrower than 4 warps; its heaviest trajectories (initial total
+    propensity within 1/8 of the largest) then run in a group of their own,
+    4 warps each, beside the rest and the small domains (three kernel groups
+    on three streams).  Every trajectory stays bit-exact."""
+    kw = dict(t_end=0.01, num_points=3, dt=0.005)
+    scs = [S.config_birth_death_2d(n=48, count=2000, D=0.5, **kw),    # heavy, 2,304 voxels
+           S.config_birth_death_2d(n=48, count=100, D=0.02, **kw),    # light, 2,304 voxels
+           S.config_birth_death_2d(n=7, count=30, **kw)]              # small: sequential kernel
+    inst = np.array([0] * 40 + [1] * 600 + [2] * 20, np.int32)
+    inst = np.random.default_rng(3).permutation(inst)
+    seeds = np.arange(900, 900 + len(inst), dtype=np.uint64)
+    with _engine(scs) as eng:
+        res = eng.run(seeds, instance=inst)
+        kernel = eng.profile()["kernel"]
+    assert res["rc"] == abi.SP_OK, res.get("error")
+    assert kernel == "nsm_advance_batchw4+nsm_advance_batch+nsm_advance_small"
+    check = [j for j in range(len(inst)) if inst[j] == 0][:10]
+    check += [j for j in range(len(inst)) if inst[j] == 1][:12]
+    check += [j for j in range(len(inst)) if inst[j] == 2][:6]
+    for j in check:
+        out, ev, _ = oracle_lib.nsm_trajectory(scs[inst[j]], int(seeds[j]), 0)
+        np.testing.assert_array_equal(res["counts"][j], out, err_msg=f"trajectory {j}")
+        np.testing.assert_array_equal(res["events"][j], ev)
+
+
 def test_warp_tuner_keeps_trajectories(oracle_lib):
     """With the default policy a long run tries 4, 2 and 1 warps per
     trajectory on its first intervals and keeps the fastest; the events are
