@@ -338,18 +338,22 @@ def config_dam_break(spacing_div: int = 64, box=(1.0, 0.5, 0.5), fluid_frac_x: f
                      nu: float = 1e-3, dt: float = 1e-4, num_steps: int = 10000,
                      h_factor: float = 1.5, species_D: float = 1e-3, decay: float = 0.01,
                      molecules: int = 50000, top_frac: float = 0.1, seed: int = 3,
-                     num_outputs: int = 11) -> Scenario:
+                     num_outputs: int = 11, dims: int = 3) -> Scenario:
     """SDPD dam break in a walled box: fluid block at cell centres (i+1/2)s for
     x < fluid_frac_x*Lx, `wall_layers` layers of fixed wall particles around
     the box, m = rho0 s^3, gravity (0,0,-1), h = h_factor*s, non-static.
     One advected species (fluid-only diffusion, first-order decay) scattered
-    over the fluid particles in the top `top_frac` of the fluid column."""
+    over the fluid particles in the top `top_frac` of the fluid column.
+    dims=2: the same in the xy-plane (box[0] x box[2], z = 0), m = rho0 s^2,
+    gravity (0,-1,0)."""
     s = 1.0 / spacing_div
+    if dims == 2:
+        box = (box[0], box[2], s)
     nx, ny, nz = (int(round(L / s)) for L in box)
     L = wall_layers
     ix = np.arange(-L, nx + L)
     iy = np.arange(-L, ny + L)
-    iz = np.arange(-L, nz + L)
+    iz = np.arange(-L, nz + L) if dims == 3 else np.zeros(1)
     I = lattice([ix.astype(float), iy.astype(float), iz.astype(float)]).astype(np.int64)
     inside = ((I[:, 0] >= 0) & (I[:, 0] < nx) & (I[:, 1] >= 0) & (I[:, 1] < ny)
               & (I[:, 2] >= 0) & (I[:, 2] < nz))
@@ -360,6 +364,8 @@ def config_dam_break(spacing_div: int = 64, box=(1.0, 0.5, 0.5), fluid_frac_x: f
     I = I[keep]
     fluid = fluid[keep]
     x = (I.astype(np.float64) + 0.5) * s
+    if dims == 2:
+        x[:, 2] = 0.0
     N = x.shape[0]
     typ = np.where(fluid, 1, 2).astype(np.int32)
     species = ["S"]
@@ -367,16 +373,19 @@ def config_dam_break(spacing_div: int = 64, box=(1.0, 0.5, 0.5), fluid_frac_x: f
         species, [(decay, {"S": 1}, {}, None)], 2)
     diff = np.array([[species_D, 0.0]])
     # the top `top_frac` of the fluid column, at least one particle layer
-    layers = max(1, int(round(top_frac * nz)))
-    top = np.nonzero(fluid & (I[:, 2] >= nz - layers))[0]
+    up = 2 if dims == 3 else 1          # the vertical axis
+    layers = max(1, int(round(top_frac * (nz if dims == 3 else ny))))
+    top = np.nonzero(fluid & (I[:, up] >= (nz if dims == 3 else ny) - layers))[0]
     u0 = scatter({"S": molecules}, {"S": top}, N, species, seed)
     steps = np.unique(np.round(np.linspace(0, num_steps, num_outputs)).astype(np.int32))
-    return Scenario(dimension=3, x=x, type=typ, mass=rho0 * s ** 3, rho=rho0, nu=nu,
+    gravity = (0.0, 0.0, -1.0) if dims == 3 else (0.0, -1.0, 0.0)
+    return Scenario(dimension=dims, x=x, type=typ, mass=rho0 * s ** dims, rho=rho0, nu=nu,
                     fixed=(~fluid).astype(np.uint8), num_types=2, species=species,
                     rxn_rate=rate, rxn_kind=kind, rxn_reactants=reac, rxn_allowed=allowed,
                     jcN=jcN, irN=irN, prN=prN, diffusion=diff, h=h_factor * s, dt=dt,
                     num_steps=num_steps, output_steps=steps, static_domain=False, rho0=rho0,
-                    c0=c0, gravity=(0.0, 0.0, -1.0), u0=u0, name=f"dam_break_{N}")
+                    c0=c0, gravity=gravity, u0=u0,
+                    name=f"dam_break_{N}" if dims == 3 else f"dam_break_2d_{N}")
 
 
 def config_uneven_ensemble(num_instances: int = 4096, vmin: int = 400, vmax: int = 40000,

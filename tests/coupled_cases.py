@@ -6,13 +6,15 @@ from spatialpy_gb300 import scenario as S
 
 
 def dam_break_species(spacing_div=16, num_steps=60, num_outputs=4, D=0.05, molecules=2000,
-                      network="decay"):
+                      network="decay", dims=3):
     """The dam break (fluid type 1, walls type 2) with one species S diffusing
     in the fluid only.  network: "decay" (S -> 0), "full" (adds 0 -> S on
     fluid particles, whose rate k*vol follows the changing density, and
-    2S -> 0, whose rate uses 1/vol), "none" (diffusion only)."""
+    2S -> 0, whose rate uses 1/vol), "none" (diffusion only).  dims=2: the
+    dam break in the xy-plane."""
     sc = S.config_dam_break(spacing_div=spacing_div, num_steps=num_steps,
-                            num_outputs=num_outputs, species_D=D, molecules=molecules)
+                            num_outputs=num_outputs, species_D=D, molecules=molecules,
+                            dims=dims)
     rxns = {"decay": [(0.01, {"S": 1}, {}, None)],
             "full": [(0.5, {"S": 1}, {}, None), (2e5, {}, {"S": 1}, [1]),
                      (2e-7, {"S": 2}, {}, None)],

@@ -43,6 +43,24 @@ def test_coupled_bitexact_vs_oracle(oracle_lib, network, prec, mode, selection):
     np.testing.assert_array_equal(rho, pr)
 
 
+@pytest.mark.parametrize("prec,mode", [("f32", 6), ("f64", 2)])
+def test_coupled_2d_bitexact_vs_oracle(oracle_lib, prec, mode):
+    """The flow + species path on a 2-D moving domain (xy-plane dam break,
+    708 particles): trajectories, event counts and the flow bit for bit
+    against the coupled oracle."""
+    sc = dam_break_species(spacing_div=32, network="full", dims=2, molecules=1000)
+    res, _ = _run(sc, prec, abi.SP_SELECT_EXACT)
+    out, ev, st, px, pr = oracle_lib.coupled_ensemble(
+        sc, SEEDS, selection=abi.SP_SELECT_EXACT, precision=prec, mode=mode, kmax=48)
+    assert (st == 0).all()
+    np.testing.assert_array_equal(res["events"], ev)
+    for j in range(len(SEEDS)):
+        np.testing.assert_array_equal(res["counts"][j], out[j], err_msg=f"trajectory {j}")
+    x, v, rho = res["particles"][0]
+    np.testing.assert_array_equal(x, px)
+    np.testing.assert_array_equal(rho, pr)
+
+
 def test_coupled_rerun_and_sequential_kernel(oracle_lib):
     """A second run restarts the flow from its initial state; the
     sequential event kernel gives the trajectories of the speculative batch

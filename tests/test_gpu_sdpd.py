@@ -46,14 +46,37 @@ def test_sdpd_bitexact_vs_oracle(oracle_lib, div, prec, mode, self_pair):
 @pytest.mark.parametrize("prec,mode,self_pair", [("f32", 6, "position"), ("f64", 2, "position")])
 def test_sdpd_full_dam_break_bitexact_vs_oracle(oracle_lib, prec, mode, self_pair):
     """The bench's flow (84,696 particles) bit for bit against the oracle
-    after 1, 20 and 40 steps: the cell-ordered warp-per-particle force pass
-    with its fused corrector, the Shepard steps 0 and 20, and a 20-step block
-    replayed from the captured graph (steps 20-39)."""
+    after 1, 20 and 40 steps: the cell-ordered force pass (one thread per
+    particle) with its fused corrector, the Shepard steps 0 and 20, and a
+    20-step block replayed from the captured graph (steps 20-39)."""
     sc = S.config_dam_break(num_steps=40)
     st = oracle_lib.SdpdState(sc)
     with _engine(sc, prec, self_pair) as eng:
         done = 0
         for n in (1, 20, 40):
+            eng.sdpd_advance(n - done)
+            oracle_lib.sdpd(sc, st, n - done, prec, mode)
+            done = n
+            x, v, rho = eng.particles(0)
+            np.testing.assert_array_equal(x, st.x, err_msg=f"x step {n}")
+            np.testing.assert_array_equal(v, st.v, err_msg=f"v step {n}")
+            np.testing.assert_array_equal(rho, st.rho, err_msg=f"rho step {n}")
+        cnt, idx, dist, dw, _ = eng.neighbors(0, 48)
+        np.testing.assert_array_equal(cnt, st.nbr_count)
+
+
+@pytest.mark.parametrize("prec,mode,self_pair", [("f32", 6, "position"), ("f64", 2, "position"),
+                                                 ("f64", 6, "step")])
+def test_sdpd_2d_bitexact_vs_oracle(oracle_lib, prec, mode, self_pair):
+    """A 2-D dam break (xy-plane, 32 x 16 cells of fluid and walls, 708
+    particles): the cell runs of a 2-D grid are single cells, the distances
+    sum two axes.  Bit for bit against the oracle after 1, 20 and 41 steps,
+    with the neighbour counts."""
+    sc = S.config_dam_break(spacing_div=32, num_steps=41, dims=2)
+    st = oracle_lib.SdpdState(sc)
+    with _engine(sc, prec, self_pair) as eng:
+        done = 0
+        for n in (1, 20, 41):
             eng.sdpd_advance(n - done)
             oracle_lib.sdpd(sc, st, n - done, prec, mode)
             done = n
