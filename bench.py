@@ -416,16 +416,18 @@ def run_uneven(args):
 
 def run_surrogate(args):
     """Surrogate + SSA fallback against the plain GPU SSA over a held-out
-    parameter sweep (reduced sizes: 2-D 32 x 32 lattice, t in [0, 4] with 8
-    output times, 32 trajectories per point, 256 training and 64 held-out
-    points).  Errors are relative L2 of the ensemble mean and variance
+    parameter sweep (reduced sizes by default: 2-D 32 x 32 lattice, t in
+    [0, 4] with 8 output times, 32 trajectories per point, 256 training and
+    64 held-out points; --surrogate-n/-traj/-train/-test change them).  Errors are relative L2 of the ensemble mean and variance
     fields coarse-grained to whole-domain species totals per output time,
     next to the same metric between two independent SSA ensembles (the
     noise floor of the reference answer)."""
     from spatialpy_gb300 import surrogate as SG
-    cfg = SG.SweepConfig(n=32, molecules=1000, t_end=4.0, num_times=8, trajectories=32)
+    n, traj = args.surrogate_n, args.surrogate_traj
+    ntrain, ntest = args.surrogate_train, args.surrogate_test
+    cfg = SG.SweepConfig(n=n, molecules=1000, t_end=4.0, num_times=8, trajectories=traj)
     rng = np.random.default_rng(7)
-    tp, hp = SG.sample_parameters(256, rng), SG.sample_parameters(64, rng)
+    tp, hp = SG.sample_parameters(ntrain, rng), SG.sample_parameters(ntest, rng)
     tm, tv, train_s = SG.ssa_moments(tp, cfg, 10)
     hm, hv, ssa_s = SG.ssa_moments(hp, cfg, 10 ** 6)
     hm2, hv2, _ = SG.ssa_moments(hp, cfg, 2 * 10 ** 6)
@@ -434,9 +436,10 @@ def run_surrogate(args):
     loss = sur.fit(tp, tm, tv, epochs=300)
     fit_s = time.perf_counter() - t0
     out = {"metric": "sweep seconds (surrogate + SSA fallback vs plain GPU SSA)",
-           "config": {"workload": "2-D 32x32 RDME sweep, 5 parameters log-uniform +-1 decade, "
-                                  "64 held-out points x 32 trajectories, 8 output times",
-                      "train_points": 256,
+           "config": {"workload": f"2-D {n}x{n} RDME sweep, 5 parameters log-uniform +-1 "
+                                  f"decade, {ntest} held-out points x {traj} trajectories, "
+                                  "8 output times, 1,000 A and 1,000 B",
+                      "train_points": ntrain,
                       "fno": "4 layers, width 32, 12 modes, FiLM; bf16 weights, fp32 "
                              "accumulation; hand-written forward/backward/Adam kernels; "
                              "average of 3 independently trained networks"},
@@ -620,6 +623,11 @@ def main():
     ap.add_argument("--sdpd-steps", type=int, default=200)
     ap.add_argument("--surrogate", action="store_true",
                     help="add the learned-surrogate sweep line (about four minutes)")
+    ap.add_argument("--surrogate-n", type=int, default=32, help="lattice edge of the sweep")
+    ap.add_argument("--surrogate-traj", type=int, default=32,
+                    help="SSA trajectories per parameter point")
+    ap.add_argument("--surrogate-train", type=int, default=256, help="training points")
+    ap.add_argument("--surrogate-test", type=int, default=64, help="held-out points")
     ap.add_argument("--fno-steps", type=int, default=50,
                     help="timed training steps of the surrogate network (0 = skip)")
     ap.add_argument("--uneven-intervals", type=int, default=1,

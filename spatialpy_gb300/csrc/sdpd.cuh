@@ -50,7 +50,7 @@ SdpdLists sdpd_lists(SdpdState* s);
 void sdpd_launch_volumes(SdpdState* s, const double* mass, float* vol, float* ivol);
 // device copies of the state in double (any pointer may be null)
 void sdpd_launch_state_out(SdpdState* s, double* x, double* v, double* rho);
-// synchronises; SP_OK or the error a step flagged (list/cell overflow, NaN)
+// synchronises; SP_OK or the error a step flagged (list overflow, NaN)
 int sdpd_check_flag(SdpdState* s, std::string* err);
 
 }  // namespace spg
