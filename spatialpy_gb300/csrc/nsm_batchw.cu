@@ -417,22 +417,57 @@ __global__ void __launch_bounds__(32 * W, 1)
                         ci = tid == 0 ? ri : INT_MAX;
                     } else {
                         count = lgot;
+                        // order by (time, voxel); keys are distinct (one per
+                        // voxel).  Each warp sorts its 32 keys with a bitonic
+                        // network over shuffles (padding keys sort last); a
+                        // key's rank is its place in its warp plus the keys
+                        // of the other warps below it, found by binary search
+                        // of their sorted lists.
+                        long long kt = SP_INF_BITS;
+                        int ki = INT_MAX;
                         if (tid < count) {
-                            ct = lt[tid];
-                            ci = lv[tid];
+                            kt = lt[tid];
+                            ki = lv[tid];
                         }
-                        // order by rank: keys are distinct (one per voxel)
-                        int rank = 0;
-                        if (tid < count)
-                            for (int j = 0; j < count; j++) rank += kless(lt[j], lv[j], ct, ci);
-                        if (tid < count) {
-                            xt[rank] = ct;
-                            xi[rank] = ci;
+#pragma unroll
+                        for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+                            for (int j = k >> 1; j > 0; j >>= 1) {
+                                const long long pt = __shfl_xor_sync(SP_FULL, kt, j);
+                                const int pi = __shfl_xor_sync(SP_FULL, ki, j);
+                                // the lower index of an ascending pair keeps the
+                                // smaller key, of a descending pair the larger
+                                const bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
+                                if (kless(pt, pi, kt, ki) == keep_min) {
+                                    kt = pt;
+                                    ki = pi;
+                                }
+                            }
+                        }
+                        xt[tid] = kt;          // warp wid's sorted keys at [32 wid, 32 wid + 32)
+                        xi[tid] = ki;
+                        __syncthreads();
+                        int rank = lane;
+#pragma unroll
+                        for (int u = 0; u < W; u++) {
+                            if (u == wid) continue;
+                            const long long* Lt = xt + 32 * u;
+                            const int* Li = xi + 32 * u;
+                            int pos = 0;
+#pragma unroll
+                            for (int st2 = 16; st2 >= 1; st2 >>= 1)
+                                if (kless(Lt[pos + st2 - 1], Li[pos + st2 - 1], kt, ki)) pos += st2;
+                            if (kless(Lt[pos], Li[pos], kt, ki)) pos++;
+                            rank += pos;
+                        }
+                        if (ki != INT_MAX) {
+                            xt[NC + rank] = kt;
+                            xi[NC + rank] = ki;
                         }
                         __syncthreads();
                         if (tid < count) {
-                            ct = xt[tid];
-                            ci = xi[tid];
+                            ct = xt[NC + tid];
+                            ci = xi[NC + tid];
                         }
                     }
                     // every leaf below the horizon is a candidate: no group bound
@@ -640,8 +675,64 @@ __global__ void __launch_bounds__(32 * W, 1)
                     int* fl = flg + (I.level_off[l] - flg_base);
                     const bool lead_a = pa >= 0 && atomicExch(&fl[pa], 1) == 0;
                     const bool lead_b = pb >= 0 && atomicExch(&fl[pb], 1) == 0;
-                    if (lead_a) lane_node(I, NT, NI, l, pa);
-                    if (lead_b) lane_node(I, NT, NI, l, pb);
+                    {
+                        // the changed nodes, listed in fa, recomputed by 4
+                        // lanes each (8 children per lane, merged by shuffles)
+                        const int nl = (lead_a ? 1 : 0) + (lead_b ? 1 : 0);
+                        int linc = nl;
+#pragma unroll
+                        for (int o = 1; o < 32; o <<= 1) {
+                            const int u = __shfl_up_sync(SP_FULL, linc, o);
+                            if (lane >= o) linc += u;
+                        }
+                        if (lane == 31) s_wcnt[wid] = linc;
+                        __syncthreads();
+                        int lb = 0, ltot = 0;
+#pragma unroll
+                        for (int u = 0; u < W; u++) {
+                            if (u < wid) lb += s_wcnt[u];
+                            ltot += s_wcnt[u];
+                        }
+                        int pos = lb + linc - nl;
+                        if (lead_a) fa[pos++] = pa;
+                        if (lead_b) fa[pos] = pb;
+                        __syncthreads();
+                        const int offc = I.level_off[l - 1], szc = I.level_size[l - 1];
+                        const int sg = tid >> 2, l4 = tid & 3;
+                        for (int r0 = 0; r0 < ltot; r0 += NC / 4) {
+                            const int node = r0 + sg < ltot ? fa[r0 + sg] : -1;
+                            const int c0 = (node >= 0 ? node : 0) * 32 + 8 * l4;
+                            long long t8[8];
+                            int i8[8];
+#pragma unroll
+                            for (int q = 0; q < 8; q++) {
+                                const bool ok = node >= 0 && c0 + q < szc;
+                                t8[q] = ok ? NT[offc + c0 + q] : SP_INF_BITS;
+                                i8[q] = ok ? NI[offc + c0 + q] : INT_MAX;
+                            }
+#pragma unroll
+                            for (int w2 = 4; w2 >= 1; w2 >>= 1)
+#pragma unroll
+                                for (int q = 0; q < w2; q++)
+                                    if (kless(t8[q + w2], i8[q + w2], t8[q], i8[q])) {
+                                        t8[q] = t8[q + w2];
+                                        i8[q] = i8[q + w2];
+                                    }
+#pragma unroll
+                            for (int o = 1; o < 4; o <<= 1) {
+                                const long long ot = __shfl_xor_sync(SP_FULL, t8[0], o);
+                                const int oi = __shfl_xor_sync(SP_FULL, i8[0], o);
+                                if (kless(ot, oi, t8[0], i8[0])) {
+                                    t8[0] = ot;
+                                    i8[0] = oi;
+                                }
+                            }
+                            if (l4 == 0 && node >= 0) {
+                                NT[I.level_off[l] + node] = t8[0];
+                                NI[I.level_off[l] + node] = i8[0];
+                            }
+                        }
+                    }
                     __syncthreads();
                     if (lead_a) fl[pa] = 0;
                     if (lead_b) fl[pb] = 0;
