@@ -13,8 +13,10 @@
 //     included).  Each group's minimum, runner-up (time and voxel) and third
 //     smallest time are kept in shared memory, so a group's 32 leaf times
 //     are read from global memory only when three or more of them lie below
-//     the horizon.  The candidates are ordered by rank: thread g counts the
-//     candidates whose (time, voxel) key is smaller than its own.
+//     the horizon.  The candidates are ordered by (time, voxel): each warp
+//     sorts its 32 keys with a bitonic network over shuffles, and a key's
+//     rank adds the keys of the other warps below it (binary search of their
+//     sorted lists).  Each candidate's counts line is prefetched into L1.
 //  2. thread g executes candidate g as event number n+g.
 //  3. the accepted prefix: time bounds by prefix minima of the redrawn times
 //     (warp shuffles, then the minima of earlier warps); voxel conflicts
@@ -27,8 +29,10 @@
 //  4. accepted events are written and, after a CTA barrier (a group may
 //     hold several accepted events), their voxel groups are listed and
 //     rescanned, 4 lanes per group (8 leaves per lane, merged by shuffles)
-//     and two rounds of groups per pass with all their loads in flight;
-//     then the tree is repaired level by level, one thread per changed node.
+//     and two rounds of groups per pass with all their loads in flight (the
+//     source's and destination's groups were prefetched into L1 during the
+//     execution); then the tree is repaired level by level, the changed
+//     nodes of a large level listed and recomputed by 4 lanes each.
 //
 // Scalars that steer the loop (clock, counters, running propensity total)
 // are kept in every thread and updated from the same shared values in the
@@ -428,6 +432,9 @@ __global__ void __launch_bounds__(32 * W, 1)
                         if (tid < count) {
                             kt = lt[tid];
                             ki = lv[tid];
+                            // the candidate's counts, read first by its
+                            // execution: start bringing the line into L1
+                            asm volatile("prefetch.global.L1 [%0];" ::"l"(X + (size_t)ki * Q.S));
                         }
 #pragma unroll
                         for (int k = 2; k <= 32; k <<= 1) {
@@ -490,6 +497,12 @@ __global__ void __launch_bounds__(32 * W, 1)
                 batch_execute<REF, MS, MR, EX>(I, Q, X, act, ci, ct, evn + (uint64_t)tid, T.key0,
                                                T.key1, Cd);
                 const int v = Cd.v, w = Cd.w, sp = Cd.sp, err = Cd.err;
+                if (act && w >= 0) {
+                    // the destination's leaf group, rescanned after the commit
+                    const long long* gq = LF + (size_t)(w >> 5) * 32;
+                    asm volatile("prefetch.global.L1 [%0];" ::"l"(gq));
+                    asm volatile("prefetch.global.L1 [%0];" ::"l"(gq + 16));
+                }
                 // ---- 3. the accepted prefix ------------------------------------
                 long long bound = act ? ct2 : SP_INF_BITS;
                 if (Cd.tv < bound) bound = Cd.tv;
@@ -652,23 +665,28 @@ __global__ void __launch_bounds__(32 * W, 1)
                 int pa = acc ? gv : -1, pb = acc ? gw : -1;
                 for (int l = 2; l <= L; l++) {
                     if (I.level_size[l] <= 8) {
+                        // this level and every one above it (all smaller):
+                        // warp 0 alone, one CTA barrier for all of them
                         if (wid == 0) {
-                            const int offc = I.level_off[l - 1], szc = I.level_size[l - 1];
-                            for (int p = 0; p < I.level_size[l]; p++) {
-                                const int c = p * 32 + lane;
-                                const long long t = c < szc ? NT[offc + c] : SP_INF_BITS;
-                                const int i = c < szc ? NI[offc + c] : INT_MAX;
-                                long long mt;
-                                int mi;
-                                argmin_redux(t, i, mt, mi);
-                                if (lane == 0) {
-                                    NT[I.level_off[l] + p] = mt;
-                                    NI[I.level_off[l] + p] = mi;
+                            for (int l2 = l; l2 <= L; l2++) {
+                                const int offc = I.level_off[l2 - 1], szc = I.level_size[l2 - 1];
+                                for (int p = 0; p < I.level_size[l2]; p++) {
+                                    const int c = p * 32 + lane;
+                                    const long long t = c < szc ? NT[offc + c] : SP_INF_BITS;
+                                    const int i = c < szc ? NI[offc + c] : INT_MAX;
+                                    long long mt;
+                                    int mi;
+                                    argmin_redux(t, i, mt, mi);
+                                    if (lane == 0) {
+                                        NT[I.level_off[l2] + p] = mt;
+                                        NI[I.level_off[l2] + p] = mi;
+                                    }
                                 }
+                                __syncwarp();
                             }
                         }
                         __syncthreads();
-                        continue;
+                        break;
                     }
                     pa = pa >= 0 ? pa >> 5 : -1;
                     pb = pb >= 0 ? pb >> 5 : -1;
