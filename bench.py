@@ -47,9 +47,9 @@ B_DIFF = 2 * (8 * 3 + 16 * 4 + 24) + 8 * 32      # 480
 B_RXN = 8 * 3 + 16 * 4 + 24 + 4 * 5              # 132
 # DRAM bytes (read + write) per event of the event-loop kernel the default
 # policy runs here (nsm_advance_batchw, 4 warps per trajectory), from one ncu
-# capture of the profile case (--profile-case: 6.654 GB over 8,894,255 events
+# capture of the profile case (--profile-case: 6.864 GB over 8,894,255 events
 # in the captured launch; profiles/nsm_advance_batchw4_rdme40.txt)
-DRAM_BYTES_PER_EVENT = 748.0
+DRAM_BYTES_PER_EVENT = 772.0
 # DRAM bytes (read + write) per particle of one sdpd_pairs launch (the
 # step's dominant kernel) from one ncu capture of --profile-sdpd with the
 # caches as the step leaves them: 55.8 MB for 84,696 particles
@@ -288,15 +288,16 @@ def run_sdpd(args):
         # (one flow does not gain from its threads: SURVEY F5), steps [2, 4)
         import oracle
         cores = os.cpu_count() or 1
-        scb = S.config_dam_break(num_steps=4)
+        scb = S.config_dam_break(num_steps=2 + REF_FLOW_STEPS)
         runs, used = oracle.ref_moving_bench(scb, np.arange(cores, dtype=np.uint64), False, 2,
                                              "_exact", cores)
-        per_run = [scb.num_particles * 2 / sec for _, sec in runs]
+        per_run = [scb.num_particles * REF_FLOW_STEPS / sec for _, sec in runs]
         cpu = {"value": float(sum(per_run)), "unit": "particle-steps/s", "cores": int(used),
                "kind": "reference",
                "single_flow": float(np.mean(per_run)),
                "sample": f"reference engine -O2, {used} independent flows (one per core), "
-                         f"steps 2-3 timed after set-up; single_flow = one flow on one core"}
+                         f"steps 2-{1 + REF_FLOW_STEPS} timed after set-up; single_flow = one "
+                         f"flow on one core"}
     return {"metric": "SDPD particle-steps/s", "value": ps, "unit": "particle-steps/s",
             **({"cpu_baseline": cpu} if cpu else {}),
             "steps": args.sdpd_steps, "warmup": 20, "ms_per_step": ms / args.sdpd_steps,
@@ -314,6 +315,9 @@ def run_sdpd(args):
 
 
 COUPLED_TRAJ = 64
+# steps of the dam break the reference engine times per flow, after set-up
+# and two untimed steps
+REF_FLOW_STEPS = 20
 
 
 def run_coupled(args, with_cpu: bool):
@@ -351,17 +355,18 @@ def run_coupled(args, with_cpu: bool):
         # timed after set-up
         import oracle
         cores = os.cpu_count() or 1
-        scb = S.config_dam_break(num_steps=4)
+        scb = S.config_dam_break(num_steps=2 + REF_FLOW_STEPS)
         runs, used = oracle.ref_moving_bench(scb, np.arange(cores, dtype=np.uint64) + SEED0, True,
                                              2, "_exact", cores)
         mean_s = float(np.mean([sec for _, sec in runs]))
         out["cpu_baseline"] = {
-            "value": scb.num_particles * 2 / (COUPLED_TRAJ * mean_s / used),
+            "value": scb.num_particles * REF_FLOW_STEPS / (COUPLED_TRAJ * mean_s / used),
             "unit": "particle-steps/s",
             "events_per_s": float(sum(ev / sec for ev, sec in runs)),
             "cores": int(used), "kind": "reference",
             "sample": f"reference engine -O2, {used} trajectories (one per core, each with its "
-                      f"own flow), steps 2-3 timed after set-up ({mean_s:.2f} s per trajectory); "
+                      f"own flow), steps 2-{1 + REF_FLOW_STEPS} timed after set-up "
+                      f"({mean_s:.2f} s per trajectory); "
                       f"value scales to the {COUPLED_TRAJ} trajectories over {used} cores"}
     return out
 
