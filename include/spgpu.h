@@ -307,9 +307,6 @@ typedef struct sp_profile {
                                     nsm_advance_small for the rest, concurrently */
 #define SP_KERNEL_BATCH_W2 5     /* nsm_advance_batchw: 2 warps per trajectory, 64-event batches */
 #define SP_KERNEL_BATCH_W4 6     /* nsm_advance_batchw: 4 warps per trajectory, 128-event batches */
-#define SP_KERNEL_MIXED_HEAVY 7  /* as SP_KERNEL_MIXED, with the heaviest batch trajectories
-                                    (initial total propensity within 1/8 of the largest, at
-                                    most two per SM) on nsm_advance_batchw with 4 warps each */
 int sp_last_profile(sp_handle* h, sp_profile* p);
 
 /*

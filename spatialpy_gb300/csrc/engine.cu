@@ -115,9 +115,8 @@ struct RunState {
     bool want_counts = false, want_mom = false;
     int next_out = 0, result = SP_OK;
     // kernel groups, each on its own stream: with the default policy the
-    // heaviest batch trajectories (4 warps each), the other batch trajectories,
-    // and the small domains (sequential kernel)
-    KernelGroup grp[3];
+    // batch trajectories and the small domains (sequential kernel)
+    KernelGroup grp[2];
     int ngroups = 1;
     WarpTuner tune;
     long long ctot = 0, mtot = 0;
@@ -139,9 +138,9 @@ struct RunState {
 struct sp_handle {
     int device = 0;
     int num_sms = 0;
-    cudaStream_t st = nullptr, st2 = nullptr, st3 = nullptr;   // kernel groups 0, 1, 2
+    cudaStream_t st = nullptr, st2 = nullptr;   // st2: the second kernel group
     cudaEvent_t e0 = nullptr, e1 = nullptr, ea = nullptr, eb = nullptr, fork = nullptr,
-                join = nullptr, join3 = nullptr;
+                join = nullptr;
     sp_options opt{};
     std::vector<Instance> inst;
     std::vector<void*> allocs;
@@ -583,8 +582,6 @@ int sp_create(const sp_scenario* scenarios, int32_t num_scenarios, const sp_opti
     SP_CUDA_TRY(cudaStreamCreateWithFlags(&h->st2, cudaStreamNonBlocking));
     SP_CUDA_TRY(cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming));
     SP_CUDA_TRY(cudaEventCreateWithFlags(&h->join, cudaEventDisableTiming));
-    SP_CUDA_TRY(cudaStreamCreateWithFlags(&h->st3, cudaStreamNonBlocking));
-    SP_CUDA_TRY(cudaEventCreateWithFlags(&h->join3, cudaEventDisableTiming));
     h->dt = s0.dt;
     h->num_steps = s0.num_steps;
     h->output_steps.assign(s0.output_steps, s0.output_steps + s0.num_outputs);
@@ -597,7 +594,7 @@ int sp_create(const sp_scenario* scenarios, int32_t num_scenarios, const sp_opti
     }
     int rc = dev_upload(h, &h->d_insts, descs.data(), descs.size());
     if (rc) return rc;
-    if ((rc = dev_alloc(h, &h->d_work, 3))) return rc;
+    if ((rc = dev_alloc(h, &h->d_work, 2))) return rc;
     SP_CUDA_TRY(cudaStreamSynchronize(h->st));
     return SP_OK;
 }
@@ -693,8 +690,7 @@ static void set_warps(sp_handle* h, const RunState& R, KernelGroup& G, int W) {
 }
 
 static int kernel_kind(const RunState& R) {
-    return R.ngroups == 3 ? SP_KERNEL_MIXED_HEAVY
-         : R.ngroups == 2 ? SP_KERNEL_MIXED
+    return R.ngroups == 2 ? SP_KERNEL_MIXED
          : R.grp[0].batch && R.grp[0].warps == 2 ? SP_KERNEL_BATCH_W2
          : R.grp[0].batch && R.grp[0].warps == 4 ? SP_KERNEL_BATCH_W4
          : R.grp[0].batch ? SP_KERNEL_BATCH
@@ -734,19 +730,21 @@ static int choose_group(sp_handle* h, const RunState& R, const std::vector<int>&
     return SP_OK;
 }
 
-// one launch of every kernel group, to step_end; group g runs on stream g
-// (st, st2, st3), in group order so the heaviest trajectories are placed first
+// one launch of every kernel group, to step_end; group 1 runs on st2
 static void launch_groups(sp_handle* h, bool ref, int step_end, long long budget,
                           long long max_ns) {
     RunState& R = h->run;
     const int ntraj = R.args.num_trajectories;
-    if (R.ngroups >= 2) cudaEventRecord(h->fork, h->st);
     for (int g = 0; g < R.ngroups; g++) {
         KernelGroup& G = R.grp[g];
-        cudaStream_t s = g == 0 ? h->st : g == 1 ? h->st2 : h->st3;
-        if (g >= 1) cudaStreamWaitEvent(s, h->fork, 0);
-        const int n = R.ngroups == 1 ? ntraj : (int)G.list.size();
-        const int* tl = R.ngroups == 1 ? nullptr : G.d_list;
+        cudaStream_t s = g == 0 ? h->st : h->st2;
+        if (g == 1) {
+            cudaEventRecord(h->fork, h->st);
+            cudaStreamWaitEvent(h->st2, h->fork, 0);
+        }
+        // a group without a device list runs trajectories 0 .. ntraj-1
+        const int n = G.d_list ? (int)G.list.size() : ntraj;
+        const int* tl = G.d_list;
         if (G.batch && G.warps > 1)
             launch_nsm_batchw(ref, G.variant, G.warps, G.warp_smem, h->d_trajs, h->d_insts, n,
                               step_end, h->dt, budget, max_ns, h->d_work + g, h->num_sms, tl, s);
@@ -758,13 +756,9 @@ static void launch_groups(sp_handle* h, bool ref, int step_end, long long budget
                                h->d_insts, n, step_end, h->dt, budget, max_ns, h->d_work + g,
                                h->num_sms, tl, s);
     }
-    if (R.ngroups >= 2) {
+    if (R.ngroups == 2) {
         cudaEventRecord(h->join, h->st2);
         cudaStreamWaitEvent(h->st, h->join, 0);
-    }
-    if (R.ngroups == 3) {
-        cudaEventRecord(h->join3, h->st3);
-        cudaStreamWaitEvent(h->st, h->join3, 0);
     }
 }
 
@@ -929,28 +923,36 @@ int sp_run_start(sp_handle* h, const sp_run_args* a, sp_outputs* out) {
                 return h->h_trajs[a].a_tot > h->h_trajs[b].a_tot;
             });
         }
-        // Heavy trajectories: when the batch group runs narrower than 4 warps
-        // per trajectory, the trajectories whose initial total propensity is
-        // at least 1/8 of the largest (at most two per SM) move to a group of
-        // their own with 4 warps each, so the longest dependent chains run
-        // about three times faster while the rest share the GPU with them.
-        KernelGroup& B = R.grp[0];
-        if (h->opt.nsm_variant == 0 && B.batch && B.warps < 4 && B.list.size() > 1) {
-            const double amax = h->h_trajs[B.list[0]].a_tot;
-            size_t nh = 0;
-            while (nh < B.list.size() - 1 && nh < (size_t)(2 * h->num_sms) &&
-                   h->h_trajs[B.list[nh]].a_tot >= amax / 8)
-                nh++;
-            KernelGroup heavy = B;
-            heavy.list.assign(B.list.begin(), B.list.begin() + nh);
-            set_warps(h, R, heavy, 4);
-            if (nh > 0 && heavy.warps > B.warps) {
-                KernelGroup rest = B;
-                rest.list.assign(B.list.begin() + nh, B.list.end());
-                R.grp[2] = R.grp[1];
-                R.grp[1] = rest;
-                R.grp[0] = heavy;
-                R.ngroups = 3;
+        // Skewed ensembles: when the largest initial total propensity is at
+        // least 8 times the 90th percentile, the run takes as long as its
+        // heaviest dependent chains.  Every trajectory then runs on the 4-warp
+        // batch kernel in one group, heaviest first, so that no concurrent
+        // kernel group shares the SMs of those chains (measured on the
+        // 4,096-instance uneven ensemble: 10.4 s per interval of 0.01 against
+        // 11.2 s with the heaviest trajectories in a 4-warp group of their own
+        // beside the other groups, 11.7 s on one warp each).
+        if (h->opt.nsm_variant == 0) {
+            std::vector<double> at(ntraj);
+            for (int j = 0; j < ntraj; j++) at[j] = h->h_trajs[j].a_tot;
+            std::vector<double> srt = at;
+            const size_t k90 = (size_t)(0.9 * (double)(ntraj - 1));
+            std::nth_element(srt.begin(), srt.begin() + k90, srt.end());
+            const double p90 = srt[k90];
+            const double amax = *std::max_element(at.begin(), at.end());
+            if (amax > 0.0 && amax >= 8.0 * p90) {
+                // (kept as two groups when one batch group cannot hold every
+                // domain's queue in shared memory)
+                KernelGroup one;
+                const std::string err0 = h->err;
+                if (choose_group(h, R, all, true, one) == SP_OK && one.batch) {
+                    set_warps(h, R, one, 4);
+                    std::stable_sort(one.list.begin(), one.list.end(),
+                                     [&](int a, int b) { return at[a] > at[b]; });
+                    R.grp[0] = one;
+                    R.grp[1] = KernelGroup{};
+                    R.ngroups = 1;
+                }
+                h->err = err0;
             }
         }
         h->last_kernel = kernel_kind(R);
@@ -1365,8 +1367,6 @@ void sp_destroy(sp_handle* h) {
     if (h->eb) cudaEventDestroy(h->eb);
     if (h->fork) cudaEventDestroy(h->fork);
     if (h->join) cudaEventDestroy(h->join);
-    if (h->join3) cudaEventDestroy(h->join3);
-    if (h->st3) cudaStreamDestroy(h->st3);
     if (h->st2) cudaStreamDestroy(h->st2);
     if (h->st) cudaStreamDestroy(h->st);
     delete h;

@@ -17,8 +17,7 @@ from .abi import SpOptions, SpOutputs, SpRunArgs, SpTrajStatus, ptr
 
 KERNEL_NAMES = {1: "nsm_advance_generic", 2: "nsm_advance_small", 3: "nsm_advance_batch",
                 4: "nsm_advance_batch+nsm_advance_small", 5: "nsm_advance_batchw2",
-                6: "nsm_advance_batchw4",
-                7: "nsm_advance_batchw4+nsm_advance_batch+nsm_advance_small"}
+                6: "nsm_advance_batchw4"}
 
 
 class EngineError(RuntimeError):
