@@ -925,12 +925,14 @@ int sp_run_start(sp_handle* h, const sp_run_args* a, sp_outputs* out) {
         }
         // Skewed ensembles: when the largest initial total propensity is at
         // least 8 times the 90th percentile, the run takes as long as its
-        // heaviest dependent chains.  Every trajectory then runs on the 4-warp
+        // heaviest dependent chains.  Every trajectory then runs on the 2-warp
         // batch kernel in one group, heaviest first, so that no concurrent
-        // kernel group shares the SMs of those chains (measured on the
-        // 4,096-instance uneven ensemble: 10.4 s per interval of 0.01 against
-        // 11.2 s with the heaviest trajectories in a 4-warp group of their own
-        // beside the other groups, 11.7 s on one warp each).
+        // kernel group shares the SMs of those chains.  Measured on the
+        // 4,096-instance uneven ensemble, one interval of 0.01: every
+        // trajectory on 2 warps 9.0 s, on 4 warps 10.4 s, on 1 warp 11.7 s;
+        // the heaviest on 4 warps beside a 1-warp group 11.2 s.  Those chains
+        // are sparse: a batch accepts about 11 events whatever its width, and
+        // a 2-warp batch costs less.
         if (h->opt.nsm_variant == 0) {
             std::vector<double> at(ntraj);
             for (int j = 0; j < ntraj; j++) at[j] = h->h_trajs[j].a_tot;
@@ -945,7 +947,7 @@ int sp_run_start(sp_handle* h, const sp_run_args* a, sp_outputs* out) {
                 KernelGroup one;
                 const std::string err0 = h->err;
                 if (choose_group(h, R, all, true, one) == SP_OK && one.batch) {
-                    set_warps(h, R, one, 4);
+                    set_warps(h, R, one, 2);
                     std::stable_sort(one.list.begin(), one.list.end(),
                                      [&](int a, int b) { return at[a] > at[b]; });
                     R.grp[0] = one;

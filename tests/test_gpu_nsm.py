@@ -401,7 +401,7 @@ def test_mixed_kernel_groups_bitexact(oracle_lib):
 def test_skewed_ensemble_bitexact(oracle_lib):
     """An ensemble whose largest initial total propensity is at least 8x its
     90th percentile (40 heavy trajectories among 600 light ones on domains
-    of 2,304 voxels, and 20 small domains) runs in one group on the 4-warp
+    of 2,304 voxels, and 20 small domains) runs in one group on the 2-warp
     batch kernel, heaviest first: its time is that of its heaviest chains.
     Every trajectory stays bit-exact, small domains included."""
     kw = dict(t_end=0.01, num_points=3, dt=0.005)
@@ -415,7 +415,7 @@ def test_skewed_ensemble_bitexact(oracle_lib):
         res = eng.run(seeds, instance=inst)
         kernel = eng.profile()["kernel"]
     assert res["rc"] == abi.SP_OK, res.get("error")
-    assert kernel == "nsm_advance_batchw4"
+    assert kernel == "nsm_advance_batchw2"
     check = [j for j in range(len(inst)) if inst[j] == 0][:10]
     check += [j for j in range(len(inst)) if inst[j] == 1][:12]
     check += [j for j in range(len(inst)) if inst[j] == 2][:6]
