@@ -10,8 +10,9 @@
 //   begin     the predictor, then the cell of each particle's start-of-step
 //             position (the kd-tree points of the step) and its rank in that
 //             cell (atomic histogram)
-//   scan      exclusive scan of the cell counts into cell starts (one CTA);
-//             the counts are reset for the next step
+//   scan      exclusive scan of the cell counts into cell starts, one CTA
+//             per tile of cells offset by the tile totals begin counted; the
+//             counts are reset for the next step
 //   scatter   counting-sort scatter into cell-ordered, float4-packed copies
 //             of what the force pass reads: tree point (+ particle index),
 //             current position (+ mass), velocity, transport velocity and
@@ -82,6 +83,8 @@ struct SdpdDev {
     const uint8_t* fixed;
     // counting sort of the tree points by cell
     int *ccnt, *cstart;             // per cell: count (zero between steps), first sorted slot
+    int* tcnt;                      // per tile of kScanTile cells: count, two buffers by step parity
+    int ntile;
     int *ckey, *crank;              // per particle: cell, rank within the cell
     int* qkey;                      // per particle: cell of the moved position
     int* slot_of;                   // per particle: its slot in the cell order
@@ -151,6 +154,9 @@ __device__ __forceinline__ void comp_add(float& hi, float& lo, float b) {
     hi = s2;
 }
 
+constexpr int kScanThreads = 256;                 // cell scan: threads per CTA
+constexpr int kScanTile = 4 * kScanThreads;       // cells per scan CTA (one int4 per thread)
+
 // particle index carried in the .w of a cell-ordered tree point (bits only)
 __device__ __forceinline__ float idx_bits(float, int j) { return __int_as_float(j); }
 __device__ __forceinline__ double idx_bits(double, int j) {
@@ -197,6 +203,13 @@ __global__ void sdpd_begin(SdpdDev<R> D) {
     const int c = D.step == 0 ? cell_key(p, D.g, D.inv_cs) : D.qkey[i];
     D.ckey[i] = c;
     D.crank[i] = atomicAdd(&D.ccnt[c], 1);
+    {
+        // the tile's count, one atomic per group of lanes on the same tile
+        const int tile = c / kScanTile;
+        const unsigned same = __match_any_sync(__activemask(), tile);
+        if ((threadIdx.x & 31) == __ffs(same) - 1)
+            atomicAdd(&D.tcnt[(D.step & 1) * D.ntile + tile], __popc(same));
+    }
     int qc = c;
     D.pold[i] = p;
     if (kComp<R>) D.pold_lo[i] = pl;
@@ -258,63 +271,63 @@ __global__ void sdpd_begin(SdpdDev<R> D) {
 
 // Exclusive scan of the per-cell counts into the cell starts (start[ncell_pad]
 // = number of particles), resetting the counts to zero for the next step.
-// One CTA of 32 warps; warp w owns a contiguous segment of cells, read as
-// int4 rows (coalesced).  Pass 1 sums each segment, one block-level scan
-// orders the 32 segment totals, pass 2 writes the starts.  ncell_pad is a
-// multiple of 16 and the padding cells stay empty.
-__global__ void __launch_bounds__(1024) sdpd_cell_scan(int* cnt, int* start, int ncell_pad) {
-    __shared__ int wsum[32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int rows = ncell_pad / 4;                 // int4 rows
-    const int per = (rows + 31) / 32;               // rows per warp
-    const int r0 = wid * per, r1 = min(r0 + per, rows);
-    const int4* c4 = reinterpret_cast<const int4*>(cnt);
-    int tot = 0;
-    for (int r = r0 + lane; r < r1; r += 32) {
-        const int4 v = c4[r];
-        tot += v.x + v.y + v.z + v.w;
-    }
+// One CTA per tile of kScanTile cells, with no waiting between CTAs: a tile's
+// offset is the sum of the totals of the tiles before it, which sdpd_begin
+// counted (buffer `par` = step parity); each CTA also zeroes its tile's count
+// in the other buffer, the one the next step fills.  ncell_pad is a multiple
+// of 16 and the padding cells stay empty.
+__global__ void __launch_bounds__(kScanThreads) sdpd_cell_scan(int* cnt, int* start, int* tcnt,
+                                                               int ntile, int par, int ncell_pad) {
+    __shared__ int wsum[kScanThreads / 32];
+    __shared__ int s_off;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int tile = blockIdx.x;
+    const int* tc = tcnt + par * ntile;
+    // the tiles before this one
+    int before = 0;
+    for (int t = tid; t < tile; t += kScanThreads) before += tc[t];
 #pragma unroll
-    for (int d = 16; d >= 1; d >>= 1) tot += __shfl_xor_sync(SP_FULL, tot, d);
-    if (lane == 0) wsum[wid] = tot;
+    for (int d = 16; d >= 1; d >>= 1) before += __shfl_xor_sync(SP_FULL, before, d);
+    if (lane == 0) wsum[wid] = before;
     __syncthreads();
-    if (wid == 0) {
-        const int v = wsum[lane];
-        int incl = v;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const int t = __shfl_up_sync(SP_FULL, incl, d);
-            if (lane >= d) incl += t;
-        }
-        wsum[lane] = incl - v;
-        if (lane == 31) start[ncell_pad] = incl;
+    if (tid == 0) {
+        int o = 0;
+        for (int w = 0; w < kScanThreads / 32; w++) o += wsum[w];
+        s_off = o;
+        tcnt[(1 - par) * ntile + tile] = 0;
     }
     __syncthreads();
-    int carry = wsum[wid];
-    int4* s4 = reinterpret_cast<int4*>(start);
-    int4* w4 = reinterpret_cast<int4*>(cnt);
-    for (int b = r0; b < r1; b += 32) {
-        const int r = b + lane;
-        int4 v = make_int4(0, 0, 0, 0);
-        if (r < r1) v = c4[r];
-        const int row = v.x + v.y + v.z + v.w;
-        int incl = row;
+    const int off = s_off;
+    // this tile: 4 cells per thread as one int4 row
+    const int c0 = tile * kScanTile + 4 * tid;
+    int4 v = make_int4(0, 0, 0, 0);
+    if (c0 < ncell_pad) v = reinterpret_cast<const int4*>(cnt)[c0 / 4];
+    const int row = v.x + v.y + v.z + v.w;
+    int incl = row;
 #pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const int t = __shfl_up_sync(SP_FULL, incl, d);
-            if (lane >= d) incl += t;
-        }
-        if (r < r1) {
-            int run = carry + incl - row;
-            int4 o;
-            o.x = run; run += v.x;
-            o.y = run; run += v.y;
-            o.z = run; run += v.z;
-            o.w = run;
-            s4[r] = o;
-            w4[r] = make_int4(0, 0, 0, 0);
-        }
-        carry += __shfl_sync(SP_FULL, incl, 31);
+    for (int d = 1; d < 32; d <<= 1) {
+        const int t = __shfl_up_sync(SP_FULL, incl, d);
+        if (lane >= d) incl += t;
+    }
+    __syncthreads();   // wsum is reused
+    if (lane == 31) wsum[wid] = incl;
+    __syncthreads();
+    int wbefore = 0;
+    for (int w = 0; w < wid; w++) wbefore += wsum[w];
+    if (c0 < ncell_pad) {
+        int run = off + wbefore + incl - row;
+        int4 o;
+        o.x = run; run += v.x;
+        o.y = run; run += v.y;
+        o.z = run; run += v.z;
+        o.w = run;
+        reinterpret_cast<int4*>(start)[c0 / 4] = o;
+        reinterpret_cast<int4*>(cnt)[c0 / 4] = make_int4(0, 0, 0, 0);
+    }
+    if (tile == ntile - 1 && tid == kScanThreads - 1) {
+        int tot = 0;
+        for (int w = 0; w < kScanThreads / 32; w++) tot += wsum[w];
+        start[ncell_pad] = off + tot;
     }
 }
 
@@ -746,6 +759,8 @@ struct SdpdState {
     int *ccnt = nullptr, *cstart = nullptr, *ckey = nullptr, *crank = nullptr, *qkey = nullptr,
         *slot_of = nullptr;
     int ncell_pad = 0;   // cells rounded up to a multiple of 16 (the scan's int4 rows)
+    int ntile = 0;       // scan tiles of kScanTile cells
+    int* tcnt = nullptr; // per tile counts, two buffers [2][ntile]
     int *ncnt = nullptr, *nidx = nullptr, *flag = nullptr;
     void* ndij = nullptr;
     // initial state (REAL-typed 4-vectors and densities) for sdpd_reset
@@ -803,6 +818,7 @@ static SdpdDev<R> dev_view(SdpdState* s) {
     D.rfull = kComp<R> ? (R*)s->rfull : (R*)s->rho;
     D.fixed = s->fixed;
     D.ccnt = s->ccnt; D.cstart = s->cstart; D.ckey = s->ckey; D.crank = s->crank;
+    D.tcnt = s->tcnt; D.ntile = s->ntile;
     D.qkey = s->qkey;
     D.slot_of = s->slot_of;
     D.s_tp = (V*)s->s_tp; D.s_tplo = (V*)s->s_tplo; D.s_x = (V*)s->s_x; D.s_xlo = (V*)s->s_xlo;
@@ -918,11 +934,13 @@ SdpdState* sdpd_create(const sp_scenario& sc, int precision, int self_step, cuda
     }
     s->grid.ncell = s->grid.nc[0] * s->grid.nc[1] * s->grid.nc[2];
     s->ncell_pad = (s->grid.ncell + 15) / 16 * 16;
+    s->ntile = (s->ncell_pad + kScanTile - 1) / kScanTile;
     const int N = s->N;
     bool ok = sd_alloc(s, (void**)&s->fixed, N, err) &&
               sd_alloc(s, (void**)&s->type, sizeof(int) * N, err) &&
               sd_alloc(s, (void**)&s->ccnt, sizeof(int) * s->ncell_pad, err) &&
               sd_alloc(s, (void**)&s->cstart, sizeof(int) * (s->ncell_pad + 4), err) &&
+              sd_alloc(s, (void**)&s->tcnt, sizeof(int) * 2 * s->ntile, err) &&
               sd_alloc(s, (void**)&s->ckey, sizeof(int) * N, err) &&
               sd_alloc(s, (void**)&s->crank, sizeof(int) * N, err) &&
               sd_alloc(s, (void**)&s->qkey, sizeof(int) * N, err) &&
@@ -949,6 +967,7 @@ SdpdState* sdpd_create(const sp_scenario& sc, int precision, int self_step, cuda
         cudaMemcpyAsync(s->fixed, sc.fixed, N, cudaMemcpyHostToDevice, st);
         cudaMemsetAsync(s->ncnt, 0, sizeof(int) * N, st);
         cudaMemsetAsync(s->ccnt, 0, sizeof(int) * s->ncell_pad, st);   // the scan keeps it zero
+        cudaMemsetAsync(s->tcnt, 0, sizeof(int) * 2 * s->ntile, st);
         ok = s->prec == SP_PREC_F64 ? upload<double>(s, sc, err) : upload<float>(s, sc, err);
     }
     if (!ok) {
@@ -978,7 +997,8 @@ static void enqueue_part(SdpdState* s, int step, int part, bool correct) {
     if (part == 0) {
         sdpd_begin<R><<<nb, tb, 0, s->st>>>(D);
     } else if (part == 1) {
-        sdpd_cell_scan<<<1, 1024, 0, s->st>>>(s->ccnt, s->cstart, s->ncell_pad);
+        sdpd_cell_scan<<<s->ntile, kScanThreads, 0, s->st>>>(s->ccnt, s->cstart, s->tcnt,
+                                                             s->ntile, step & 1, s->ncell_pad);
         sdpd_scatter<R><<<nb, tb, 0, s->st>>>(D);
         constexpr int TB = PairShape<R>::TB;
         const int grid = (N + TB - 1) / TB;
@@ -1153,6 +1173,7 @@ int sdpd_reset(SdpdState* s, std::string* err) {
         cudaMemcpyAsync(s->rfull, s->init_rfull.data(), r1, cudaMemcpyHostToDevice, s->st);
     cudaMemsetAsync(s->ncnt, 0, sizeof(int) * s->N, s->st);
     cudaMemsetAsync(s->ccnt, 0, sizeof(int) * s->ncell_pad, s->st);
+    cudaMemsetAsync(s->tcnt, 0, sizeof(int) * 2 * s->ntile, s->st);
     cudaMemsetAsync(s->flag, 0, sizeof(int), s->st);
     cudaError_t e = cudaStreamSynchronize(s->st);   // host staging buffers stay valid
     if (e != cudaSuccess) {
