@@ -10,10 +10,9 @@
 //     level-2 frontier (up to 32*W nodes) is expanded by all warps, one node
 //     per lane, into the leaf groups whose minimum lies below the horizon,
 //     and EVERY leaf below the horizon is a candidate (a group's runner-up
-//     included).  Each group's minimum, runner-up (time and voxel) and third
-//     smallest time are kept in shared memory, so a group's 32 leaf times
-//     are read from global memory only when three or more of them lie below
-//     the horizon.  The candidates are ordered by (time, voxel): each warp
+//     included).  Each group keeps its two or three smallest leaves (time
+//     and voxel) in shared memory, so a group's 32 leaf times are read from
+//     global memory only when all of them lie below the horizon.  The candidates are ordered by (time, voxel): each warp
 //     sorts its 32 keys with a bitonic network over shuffles, and a key's
 //     rank adds the keys of the other warps below it (binary search of their
 //     sorted lists).  Each candidate's counts line is prefetched into L1.
@@ -26,13 +25,15 @@
 //     runner-up had to stay above every later candidate, which cut batches
 //     near the birthday bound of the 2,000 groups (about 48 events of 128);
 //     with leaves only the 64,000 voxels' conflicts and redrawn times do.
-//  4. accepted events are written and, after a CTA barrier (a group may
-//     hold several accepted events), their voxel groups are listed and
-//     rescanned, 4 lanes per group (8 leaves per lane, merged by shuffles)
-//     and two rounds of groups per pass with all their loads in flight (the
-//     source's and destination's groups were prefetched into L1 during the
-//     execution); then the tree is repaired level by level, the changed
-//     nodes of a large level listed and recomputed by 4 lanes each.
+//  4. accepted events are written and, after a CTA barrier, each group
+//     changed by one event has its list updated in place by that event's
+//     thread; a group changed by several events, or whose list falls below
+//     two entries, is rescanned from its leaves, 4 lanes per group (8
+//     leaves per lane, merged by shuffles) with all loads in flight (a
+//     source group likely to need it was prefetched into L1 during the
+//     execution).  Then the level-2 nodes above changed group minima,
+//     listed before the rescans, are recomputed by 4 lanes each, and
+//     warp 0 recomputes the small levels above.
 //
 // Scalars that steer the loop (clock, counters, running propensity total)
 // are kept in every thread and updated from the same shared values in the
@@ -42,9 +43,9 @@
 
 namespace spg {
 
-constexpr int kHash = 2048;   // conflict table slots (power of two, > 2 * 32 * W)
+constexpr int kHash = 1024;   // conflict table slots (power of two, >= 4 * 2 * 32 * W)
 
-__device__ __forceinline__ int hslot(int v) { return (int)(((unsigned)v * 2654435761u) >> 21); }
+__device__ __forceinline__ int hslot(int v) { return (int)(((unsigned)v * 2654435761u) >> 22); }
 
 // conflict table: open addressing with linear probing, key = voxel, value =
 // the smallest candidate index touching it.  At most 2 * 32 * W keys per
@@ -70,11 +71,10 @@ __device__ __forceinline__ int ctab_find(const int* key, int v) {
     return -1;
 }
 
-// The three smallest leaf times of a group and the voxels of the first two,
-// ordered by (time, voxel).
+// The three smallest leaves of a group, (time, voxel) in (time, voxel) order.
 struct Top3 {
     long long t0, t1, t2;
-    int i0, i1;
+    int i0, i1, i2;
 };
 
 __device__ __forceinline__ Top3 merge3(const Top3& a, const Top3& b) {
@@ -85,11 +85,15 @@ __device__ __forceinline__ Top3 merge3(const Top3& a, const Top3& b) {
     const long long ha = fa ? a.t1 : a.t0, hb = fa ? b.t0 : b.t1;   // the lists' next heads
     const int hai = fa ? a.i1 : a.i0, hbi = fa ? b.i0 : b.i1;
     const long long na = fa ? a.t2 : a.t1, nb = fa ? b.t1 : b.t2;   // and the items after them
+    const int nai = fa ? a.i2 : a.i1, nbi = fa ? b.i1 : b.i2;
     const bool fs = kless(ha, hai, hb, hbi);
     r.t1 = fs ? ha : hb;
     r.i1 = fs ? hai : hbi;
     const long long c1 = fs ? na : ha, c2 = fs ? hb : nb;
-    r.t2 = c1 < c2 ? c1 : c2;
+    const int c1i = fs ? nai : hai, c2i = fs ? hbi : nbi;
+    const bool f3 = kless(c1, c1i, c2, c2i);
+    r.t2 = f3 ? c1 : c2;
+    r.i2 = f3 ? c1i : c2i;
     return r;
 }
 
@@ -105,6 +109,7 @@ __device__ __forceinline__ Top3 top3_half(const longlong2* p, int base) {
         v[q].t2 = SP_INF_BITS;
         v[q].i0 = a ? base + 2 * q : base + 2 * q + 1;
         v[q].i1 = a ? base + 2 * q + 1 : base + 2 * q;
+        v[q].i2 = INT_MAX;
     }
 #pragma unroll
     for (int w = 4; w >= 1; w >>= 1)
@@ -113,11 +118,16 @@ __device__ __forceinline__ Top3 top3_half(const longlong2* p, int base) {
     return v[0];
 }
 
-// Level-1 node g (the group's minimum), its runner-up time T2 (as the other
-// kernels keep it) and voxel I2, and its third-smallest time T3, from the
-// group's 32 leaf times.
+// Each group keeps a list of its k smallest leaves, (time, voxel) in order:
+// the first is the level-1 node (NT, NI), the second the runner-up (T2, I2;
+// the other event kernels keep T2 too), the third (T3, I3).  Every leaf of
+// the group outside the list has a larger key than the list's last entry.
+// KC holds k in its low byte; between batches k is 2 or 3.
+
+// The full list (k = 3) of group g from its 32 leaf times.
 __device__ __forceinline__ void rescan3(const NsmInstance& I, const long long* LF, long long* NT,
-                                        int* NI, long long* T2, int* I2, long long* T3, int g) {
+                                        int* NI, long long* T2, int* I2, long long* T3, int* I3,
+                                        int* KC, int g) {
     const longlong2* p = (const longlong2*)(LF + (size_t)g * 32);
     const Top3 a = top3_half(p, g * 32);
     const Top3 b = top3_half(p + 8, g * 32 + 16);
@@ -127,6 +137,59 @@ __device__ __forceinline__ void rescan3(const NsmInstance& I, const long long* L
     T2[g] = r.t1;
     I2[g] = r.i1;
     T3[g] = r.t2;
+    I3[g] = r.i2;
+    KC[g] = 3;
+}
+
+// Group g's list after voxel vn's leaf time became tn, without reading the
+// leaves: vn leaves the list if it was in it, and enters it when its new
+// key is below the old last entry (the entry then dropped, if the list was
+// full, is the largest of the four).  Returns the new k; the list stays
+// exact, but below 2 entries the group must be rescanned.  N1t, N1i point
+// at level 1 of the tree.
+__device__ __forceinline__ int list_update(long long* N1t, int* N1i, long long* T2, int* I2,
+                                           long long* T3, int* I3, int g, int k, long long tn,
+                                           int vn) {
+    long long t[3] = {N1t[g], T2[g], T3[g]};
+    int i[3] = {N1i[g], I2[g], I3[g]};
+    const long long Mt = k >= 3 ? t[2] : k == 2 ? t[1] : t[0];
+    const int Mi = k >= 3 ? i[2] : k == 2 ? i[1] : i[0];
+    const bool ins = k > 0 && kless(tn, vn, Mt, Mi);
+    int p = -1;
+#pragma unroll
+    for (int q = 0; q < 3; q++)
+        if (q < k && i[q] == vn) p = q;
+    if (p >= 0) {
+#pragma unroll
+        for (int q = 0; q < 2; q++)
+            if (q >= p && q + 1 < k) { t[q] = t[q + 1]; i[q] = i[q + 1]; }
+        k--;
+    } else if (ins && k == 3) {
+        k = 2;
+    }
+    if (ins) {
+        int pos = 0;
+#pragma unroll
+        for (int q = 0; q < 3; q++)
+            if (q < k && kless(t[q], i[q], tn, vn)) pos++;
+#pragma unroll
+        for (int q = 2; q >= 1; q--)
+            if (q <= k && q > pos) { t[q] = t[q - 1]; i[q] = i[q - 1]; }
+#pragma unroll
+        for (int q = 0; q < 3; q++)
+            if (q == pos) { t[q] = tn; i[q] = vn; }
+        k++;
+    }
+#pragma unroll
+    for (int q = 0; q < 3; q++)
+        if (q >= k) { t[q] = SP_INF_BITS; i[q] = INT_MAX; }
+    N1t[g] = t[0];
+    N1i[g] = i[0];
+    T2[g] = t[1];
+    I2[g] = i[1];
+    T3[g] = t[2];
+    I3[g] = i[2];
+    return k;
 }
 
 // Top3 of two adjacent leaves `base`, `base` + 1
@@ -138,6 +201,7 @@ __device__ __forceinline__ Top3 pair3(const longlong2 u, int base) {
     r.t2 = SP_INF_BITS;
     r.i0 = a ? base : base + 1;
     r.i1 = a ? base + 1 : base;
+    r.i2 = INT_MAX;
     return r;
 }
 
@@ -148,13 +212,14 @@ __device__ __forceinline__ Top3 shfl_xor3(const Top3& t, int o) {
     q.t2 = __shfl_xor_sync(SP_FULL, t.t2, o);
     q.i0 = __shfl_xor_sync(SP_FULL, t.i0, o);
     q.i1 = __shfl_xor_sync(SP_FULL, t.i1, o);
+    q.i2 = __shfl_xor_sync(SP_FULL, t.i2, o);
     return q;
 }
 
 static size_t batchw_smem_bytes(const NsmInstance& d, int W) {
     const size_t NN = d.num_nodes, N1 = d.level_size[1];
     size_t b = NN * 8 + N1 * 8 + NN * 4;      // tree times, second minima, indices
-    b += N1 * 12;                              // third minima, runner-up voxels
+    b += N1 * 20;                              // third minima, runner-up and third voxels, k
     b += 2 * (size_t)(64 * W) * 4;             // frontiers
     b += (NN - N1) * 4;                        // repair flags, levels >= 2
     b += (size_t)kHash * 8;                    // conflict table: keys, values
@@ -174,7 +239,7 @@ __global__ void __launch_bounds__(32 * W, 1)
                        const int* tlist) {
     constexpr int NC = 32 * W;    // candidates per batch at most
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ int s_jt, s_nf, s_tflag;
+    __shared__ int s_jt, s_nf, s_tflag, s_nr, s_nl;
     __shared__ int s_wcnt[W], s_wfi[W], s_werr[W], s_werrc[W], s_werrv[W], s_wnrx[W], s_wndf[W];
     __shared__ long long s_wmin[W], s_tl;
     __shared__ double s_wdA[W];
@@ -212,7 +277,9 @@ __global__ void __launch_bounds__(32 * W, 1)
         long long* T3 = T2 + N1;                   // third-smallest leaf time per group
         int* NI = (int*)(T3 + N1);
         int* I2 = NI + NN;                         // runner-up voxel per group
-        int* fa = I2 + N1;
+        int* I3 = I2 + N1;                         // third voxel per group
+        int* KC = I3 + N1;                         // list length k | changes << 8
+        int* fa = KC + N1;
         int* fb = fa + 64 * W;
         int* flg = fb + 64 * W;
         int* hkey = flg + (NN - N1);
@@ -228,9 +295,9 @@ __global__ void __launch_bounds__(32 * W, 1)
         for (int e = tid; e < kHash; e += NC) { hkey[e] = -1; hval[e] = INT_MAX; }
         for (int e = tid; e < NN; e += NC) { NT[e] = T.node_t[e]; NI[e] = T.node_i[e]; }
         __syncthreads();
-        // level 1 with runner-ups and third minima from the leaves (the
-        // other event kernels keep only the runner-up times)
-        for (int g = tid; g < N1; g += NC) rescan3(I, T.leaf, NT, NI, T2, I2, T3, g);
+        // level 1 with the groups' lists from the leaves (the other event
+        // kernels keep only the runner-up times)
+        for (int g = tid; g < N1; g += NC) rescan3(I, T.leaf, NT, NI, T2, I2, T3, I3, KC, g);
         __syncthreads();
         long long* LF = T.leaf;
         int32_t* X = T.x;
@@ -270,6 +337,7 @@ __global__ void __launch_bounds__(32 * W, 1)
                     if (tf) { status = SP_TRAJ_BUDGET_EXHAUSTED; break; }
                 }
                 // ---- 1. candidates -------------------------------------------
+                if (tid == 0) { s_nr = 0; s_nl = 0; }   // list lengths of step 5
                 long long ct = SP_INF_BITS, ct2 = SP_INF_BITS;
                 int ci = INT_MAX, count = 1;
                 if (over) {   // the reference's one event past the step end, alone
@@ -355,8 +423,9 @@ __global__ void __launch_bounds__(32 * W, 1)
                     __syncthreads();
                     // level 1 -> leaves: group clist[tid] per thread.  Its
                     // minimum is below the horizon; its runner-up too when
-                    // T2 < horizon; only when T3 < horizon are its 32 leaf
-                    // times read (16-byte loads; padded leaves hold infinity)
+                    // T2 < horizon; only when the list's last entry lies
+                    // below the horizon are its 32 leaf times read (16-byte
+                    // loads; padded leaves hold infinity)
                     int lgot = NC + 1;
                     if (got <= NC) {
                         unsigned lm = 0u;
@@ -365,7 +434,8 @@ __global__ void __launch_bounds__(32 * W, 1)
                         if (tid < got) {
                             g = clist[tid];
                             gb = g * 32;
-                            if (T3[g] < thb) {
+                            const bool k3 = (KC[g] & 255) == 3;   // else k = 2
+                            if ((k3 ? T3[g] : T2[g]) < thb) {
                                 scan = true;
                                 const longlong2* lp = (const longlong2*)(LF + gb);
 #pragma unroll
@@ -376,7 +446,7 @@ __global__ void __launch_bounds__(32 * W, 1)
                                 }
                                 nl = __popc(lm);
                             } else {
-                                nl = T2[g] < thb ? 2 : 1;
+                                nl = k3 && T2[g] < thb ? 2 : 1;
                             }
                         }
                         int li = nl;
@@ -486,9 +556,10 @@ __global__ void __launch_bounds__(32 * W, 1)
                 stat_c += count;
                 // ---- 2. speculative execution, one candidate per thread -------
                 const bool act = tid < count;
-                if (act) {
-                    // the source's leaf group, read again by the rescan after the
-                    // commit: start bringing its two lines into L1 now
+                if (act && (KC[ci >> 5] & 255) == 2) {
+                    // the source's leaf group, whose list the event will likely
+                    // leave at one entry, so that the group is rescanned after
+                    // the commit: start bringing its two lines into L1 now
                     const long long* gp = LF + (size_t)(ci >> 5) * 32;
                     asm volatile("prefetch.global.L1 [%0];" ::"l"(gp));
                     asm volatile("prefetch.global.L1 [%0];" ::"l"(gp + 16));
@@ -497,12 +568,6 @@ __global__ void __launch_bounds__(32 * W, 1)
                 batch_execute<REF, MS, MR, EX>(I, Q, X, act, ci, ct, evn + (uint64_t)tid, T.key0,
                                                T.key1, Cd);
                 const int v = Cd.v, w = Cd.w, sp = Cd.sp, err = Cd.err;
-                if (act && w >= 0) {
-                    // the destination's leaf group, rescanned after the commit
-                    const long long* gq = LF + (size_t)(w >> 5) * 32;
-                    asm volatile("prefetch.global.L1 [%0];" ::"l"(gq));
-                    asm volatile("prefetch.global.L1 [%0];" ::"l"(gq + 16));
-                }
                 // ---- 3. the accepted prefix ------------------------------------
                 long long bound = act ? ct2 : SP_INF_BITS;
                 if (Cd.tv < bound) bound = Cd.tv;
@@ -583,33 +648,68 @@ __global__ void __launch_bounds__(32 * W, 1)
                 if (m > 0 && tid == m - 1) s_tl = ct;
                 // ---- 5. rescan and tree repair ------------------------------------
                 const int off1r = I.level_off[1];
-                // a group may hold several accepted events: every commit is
-                // stored before any rescan reads the group
-                __syncthreads();
                 const int gv = v >> 5;
                 const int gw = (w >= 0 && (w >> 5) != gv) ? w >> 5 : -1;
+                // the accepted events' changes per group: a group changed by
+                // one event is updated in place by that event's thread, a
+                // group changed by several is rescanned, and so is a group
+                // whose list falls below two entries
+                if (acc) {
+                    atomicAdd(&KC[gv], 256);
+                    if (gw >= 0) atomicAdd(&KC[gw], 256);
+                }
+                // a group may hold several accepted events: every commit and
+                // count is stored before any rescan reads the group
+                __syncthreads();
+                bool need_a = false, need_b = false, ch_a = false, ch_b = false;
+                if (acc) {
+                    long long* N1t = NT + off1r;
+                    int* N1i = NI + off1r;
+                    const int ca = atomicAnd(&KC[gv], 255);   // the first to ask takes the group
+                    if (ca >= 512) {
+                        need_a = ch_a = true;
+                    } else if (ca >= 256) {
+                        const long long m0 = N1t[gv];
+                        const int m0i = N1i[gv];
+                        int k = list_update(N1t, N1i, T2, I2, T3, I3, gv, ca & 255, Cd.tv, v);
+                        if (w >= 0 && gw < 0)
+                            k = list_update(N1t, N1i, T2, I2, T3, I3, gv, k, Cd.tw, w);
+                        KC[gv] = k;
+                        need_a = k < 2;
+                        ch_a = need_a || N1t[gv] != m0 || N1i[gv] != m0i;
+                    }
+                    if (gw >= 0) {
+                        const int cb = atomicAnd(&KC[gw], 255);
+                        if (cb >= 512) {
+                            need_b = ch_b = true;
+                        } else if (cb >= 256) {
+                            const long long m0 = N1t[gw];
+                            const int m0i = N1i[gw];
+                            const int k =
+                                list_update(N1t, N1i, T2, I2, T3, I3, gw, cb & 255, Cd.tw, w);
+                            KC[gw] = k;
+                            need_b = k < 2;
+                            ch_b = need_b || N1t[gw] != m0 || N1i[gw] != m0i;
+                        }
+                    }
+                }
+                // the level-2 parents of groups whose minimum changed, one
+                // leader each, listed in fb while the groups to rescan are
+                // listed in fa (both free after the walk; any order)
+                const bool big2 = L >= 2 && I.level_size[2] > 8;
+                int* fl2 = flg + (I.level_off[2] - flg_base);
+                const int p2a = ch_a ? gv >> 5 : -1, p2b = ch_b ? gw >> 5 : -1;
+                const bool lead_a = big2 && p2a >= 0 && atomicExch(&fl2[p2a], 1) == 0;
+                const bool lead_b = big2 && p2b >= 0 && atomicExch(&fl2[p2b], 1) == 0;
+                if (lead_a) fb[atomicAdd(&s_nl, 1)] = p2a;
+                if (lead_b) fb[atomicAdd(&s_nl, 1)] = p2b;
+                if (need_a) fa[atomicAdd(&s_nr, 1)] = gv;
+                if (need_b) fa[atomicAdd(&s_nr, 1)] = gw;
+                __syncthreads();
+                if (lead_a) fl2[p2a] = 0;    // elections are over until the next batch
+                if (lead_b) fl2[p2b] = 0;
                 {
-                    // the groups to rescan, listed in fa (free after the walk)
-                    const int nr = acc ? (gw >= 0 ? 2 : 1) : 0;
-                    int rinc = nr;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const int u = __shfl_up_sync(SP_FULL, rinc, o);
-                        if (lane >= o) rinc += u;
-                    }
-                    if (lane == 31) s_wcnt[wid] = rinc;
-                    __syncthreads();
-                    int rbase = 0, rtot = 0;
-#pragma unroll
-                    for (int u = 0; u < W; u++) {
-                        if (u < wid) rbase += s_wcnt[u];
-                        rtot += s_wcnt[u];
-                    }
-                    if (nr) {
-                        fa[rbase + rinc - nr] = gv;
-                        if (nr == 2) fa[rbase + rinc - 1] = gw;
-                    }
-                    __syncthreads();
+                    const int rtot = s_nr;
                     // 4 lanes per group (lane l4 reads leaves 8*l4 .. 8*l4+7),
                     // two rounds of NC/4 groups with all their loads in flight
                     const int sg = tid >> 2, l4 = tid & 3;
@@ -642,6 +742,8 @@ __global__ void __launch_bounds__(32 * W, 1)
                             T2[ga] = ta.t1;
                             I2[ga] = ta.i1;
                             T3[ga] = ta.t2;
+                            I3[ga] = ta.i2;
+                            KC[ga] = 3;
                         }
                         if (l4 == 0 && gb2 >= 0) {
                             NT[off1r + gb2] = tb.t0;
@@ -649,6 +751,8 @@ __global__ void __launch_bounds__(32 * W, 1)
                             T2[gb2] = tb.t1;
                             I2[gb2] = tb.i1;
                             T3[gb2] = tb.t2;
+                            I3[gb2] = tb.i2;
+                            KC[gb2] = 3;
                         }
                     }
                 }
@@ -662,100 +766,71 @@ __global__ void __launch_bounds__(32 * W, 1)
                 evn += (uint64_t)m;
                 nev += m;
                 if (m > 0) tlast = __longlong_as_double(s_tl);
-                int pa = acc ? gv : -1, pb = acc ? gw : -1;
-                for (int l = 2; l <= L; l++) {
-                    if (I.level_size[l] <= 8) {
-                        // this level and every one above it (all smaller):
-                        // warp 0 alone, one CTA barrier for all of them
-                        if (wid == 0) {
-                            for (int l2 = l; l2 <= L; l2++) {
-                                const int offc = I.level_off[l2 - 1], szc = I.level_size[l2 - 1];
-                                for (int p = 0; p < I.level_size[l2]; p++) {
-                                    const int c = p * 32 + lane;
-                                    const long long t = c < szc ? NT[offc + c] : SP_INF_BITS;
-                                    const int i = c < szc ? NI[offc + c] : INT_MAX;
-                                    long long mt;
-                                    int mi;
-                                    argmin_redux(t, i, mt, mi);
-                                    if (lane == 0) {
-                                        NT[I.level_off[l2] + p] = mt;
-                                        NI[I.level_off[l2] + p] = mi;
-                                    }
+                if (big2) {
+                    // the listed level-2 nodes recomputed by 4 lanes each (8
+                    // children per lane, merged by shuffles)
+                    const int ltot = s_nl;
+                    const int offc = I.level_off[1], szc = I.level_size[1];
+                    const int sg = tid >> 2, l4 = tid & 3;
+                    for (int r0 = 0; r0 < ltot; r0 += NC / 4) {
+                        const int node = r0 + sg < ltot ? fb[r0 + sg] : -1;
+                        const int c0 = (node >= 0 ? node : 0) * 32 + 8 * l4;
+                        long long t8[8];
+                        int i8[8];
+#pragma unroll
+                        for (int q = 0; q < 8; q++) {
+                            const bool ok = node >= 0 && c0 + q < szc;
+                            t8[q] = ok ? NT[offc + c0 + q] : SP_INF_BITS;
+                            i8[q] = ok ? NI[offc + c0 + q] : INT_MAX;
+                        }
+#pragma unroll
+                        for (int w2 = 4; w2 >= 1; w2 >>= 1)
+#pragma unroll
+                            for (int q = 0; q < w2; q++)
+                                if (kless(t8[q + w2], i8[q + w2], t8[q], i8[q])) {
+                                    t8[q] = t8[q + w2];
+                                    i8[q] = i8[q + w2];
                                 }
-                                __syncwarp();
+#pragma unroll
+                        for (int o = 1; o < 4; o <<= 1) {
+                            const long long ot = __shfl_xor_sync(SP_FULL, t8[0], o);
+                            const int oi = __shfl_xor_sync(SP_FULL, i8[0], o);
+                            if (kless(ot, oi, t8[0], i8[0])) {
+                                t8[0] = ot;
+                                i8[0] = oi;
                             }
                         }
-                        __syncthreads();
-                        break;
-                    }
-                    pa = pa >= 0 ? pa >> 5 : -1;
-                    pb = pb >= 0 ? pb >> 5 : -1;
-                    int* fl = flg + (I.level_off[l] - flg_base);
-                    const bool lead_a = pa >= 0 && atomicExch(&fl[pa], 1) == 0;
-                    const bool lead_b = pb >= 0 && atomicExch(&fl[pb], 1) == 0;
-                    {
-                        // the changed nodes, listed in fa, recomputed by 4
-                        // lanes each (8 children per lane, merged by shuffles)
-                        const int nl = (lead_a ? 1 : 0) + (lead_b ? 1 : 0);
-                        int linc = nl;
-#pragma unroll
-                        for (int o = 1; o < 32; o <<= 1) {
-                            const int u = __shfl_up_sync(SP_FULL, linc, o);
-                            if (lane >= o) linc += u;
-                        }
-                        if (lane == 31) s_wcnt[wid] = linc;
-                        __syncthreads();
-                        int lb = 0, ltot = 0;
-#pragma unroll
-                        for (int u = 0; u < W; u++) {
-                            if (u < wid) lb += s_wcnt[u];
-                            ltot += s_wcnt[u];
-                        }
-                        int pos = lb + linc - nl;
-                        if (lead_a) fa[pos++] = pa;
-                        if (lead_b) fa[pos] = pb;
-                        __syncthreads();
-                        const int offc = I.level_off[l - 1], szc = I.level_size[l - 1];
-                        const int sg = tid >> 2, l4 = tid & 3;
-                        for (int r0 = 0; r0 < ltot; r0 += NC / 4) {
-                            const int node = r0 + sg < ltot ? fa[r0 + sg] : -1;
-                            const int c0 = (node >= 0 ? node : 0) * 32 + 8 * l4;
-                            long long t8[8];
-                            int i8[8];
-#pragma unroll
-                            for (int q = 0; q < 8; q++) {
-                                const bool ok = node >= 0 && c0 + q < szc;
-                                t8[q] = ok ? NT[offc + c0 + q] : SP_INF_BITS;
-                                i8[q] = ok ? NI[offc + c0 + q] : INT_MAX;
-                            }
-#pragma unroll
-                            for (int w2 = 4; w2 >= 1; w2 >>= 1)
-#pragma unroll
-                                for (int q = 0; q < w2; q++)
-                                    if (kless(t8[q + w2], i8[q + w2], t8[q], i8[q])) {
-                                        t8[q] = t8[q + w2];
-                                        i8[q] = i8[q + w2];
-                                    }
-#pragma unroll
-                            for (int o = 1; o < 4; o <<= 1) {
-                                const long long ot = __shfl_xor_sync(SP_FULL, t8[0], o);
-                                const int oi = __shfl_xor_sync(SP_FULL, i8[0], o);
-                                if (kless(ot, oi, t8[0], i8[0])) {
-                                    t8[0] = ot;
-                                    i8[0] = oi;
-                                }
-                            }
-                            if (l4 == 0 && node >= 0) {
-                                NT[I.level_off[l] + node] = t8[0];
-                                NI[I.level_off[l] + node] = i8[0];
-                            }
+                        if (l4 == 0 && node >= 0) {
+                            NT[I.level_off[2] + node] = t8[0];
+                            NI[I.level_off[2] + node] = i8[0];
                         }
                     }
                     __syncthreads();
-                    if (lead_a) fl[pa] = 0;
-                    if (lead_b) fl[pb] = 0;
-                    if (!lead_a) pa = -1;
-                    if (!lead_b) pb = -1;
+                }
+                // the levels above (at most 8 nodes each within the shared
+                // memory this kernel takes; any size stays correct): warp 0
+                // recomputes every node, one CTA barrier for all of them
+                {
+                    const int l0 = big2 ? 3 : 2;
+                    if (wid == 0) {
+                        for (int l2 = l0; l2 <= L; l2++) {
+                            const int offc = I.level_off[l2 - 1], szc = I.level_size[l2 - 1];
+                            for (int p = 0; p < I.level_size[l2]; p++) {
+                                const int c = p * 32 + lane;
+                                const long long t = c < szc ? NT[offc + c] : SP_INF_BITS;
+                                const int i = c < szc ? NI[offc + c] : INT_MAX;
+                                long long mt;
+                                int mi;
+                                argmin_redux(t, i, mt, mi);
+                                if (lane == 0) {
+                                    NT[I.level_off[l2] + p] = mt;
+                                    NI[I.level_off[l2] + p] = mi;
+                                }
+                            }
+                            __syncwarp();
+                        }
+                    }
+                    __syncthreads();
                 }
                 rt = NT[I.level_off[L]];
                 ri = NI[I.level_off[L]];
