@@ -12,7 +12,8 @@
 //     and EVERY leaf below the horizon is a candidate (a group's runner-up
 //     included).  Each group keeps its two or three smallest leaves (time
 //     and voxel) in shared memory, so a group's 32 leaf times are read from
-//     global memory only when all of them lie below the horizon.  The candidates are ordered by (time, voxel): each warp
+//     global memory only when every leaf of its list lies below the
+//     horizon.  The candidates are ordered by (time, voxel): each warp
 //     sorts its 32 keys with a bitonic network over shuffles, and a key's
 //     rank adds the keys of the other warps below it (binary search of their
 //     sorted lists).  Each candidate's counts line is prefetched into L1.
