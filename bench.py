@@ -47,9 +47,9 @@ B_DIFF = 2 * (8 * 3 + 16 * 4 + 24) + 8 * 32      # 480
 B_RXN = 8 * 3 + 16 * 4 + 24 + 4 * 5              # 132
 # DRAM bytes (read + write) per event of the event-loop kernel the default
 # policy runs here (nsm_advance_batchw, 4 warps per trajectory), from one ncu
-# capture of the profile case (--profile-case: 6.864 GB over 8,894,255 events
+# capture of the profile case (--profile-case: 4.907 GB over 8,894,255 events
 # in the captured launch; profiles/nsm_advance_batchw4_rdme40.txt)
-DRAM_BYTES_PER_EVENT = 772.0
+DRAM_BYTES_PER_EVENT = 551.6
 # DRAM bytes (read + write) per particle of one sdpd_pairs launch (the
 # step's dominant kernel) from one ncu capture of --profile-sdpd with the
 # caches as the step leaves them: 55.8 MB for 84,696 particles
