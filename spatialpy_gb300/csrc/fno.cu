@@ -7,24 +7,28 @@
 //
 // Work per sample is small and the contractions are width-32 channel mixes
 // (2 x 32 x 32 flops per voxel and layer against 256 bytes of field traffic,
-// 8 flop/byte): below the FP32 CUDA-core ridge, so every kernel here is
-// bound by memory and launch latency, not by arithmetic, and none uses the
-// tensor cores.  A training step (about 70 launches) is captured once per
+// 8 flop/byte), so the kernels are bound by memory and launch latency.  The
+// channel mixes and their weight gradients run on the tensor cores (mma.sync
+// TF32 with fp32 operands split into high and low TF32 parts, so the sums
+// keep fp32-level accuracy); the DFTs and the per-mode mixing are fp32
+// CUDA-core code.  A training step (about 70 launches) is captured once per
 // batch size as a CUDA graph and replayed.
 //
 // Kernels:
 //   fno_pointwise    channel mix at every voxel (lift, the layers' linear
 //                    paths, the projection, and their transposes in the
 //                    backward pass), with fused bias, spectral addend, FiLM,
-//                    GELU and GELU' epilogues
+//                    GELU and GELU' epilogues; fno_pointwise_tc on the
+//                    tensor cores where cout is a multiple of 16
 //   fno_analysis     truncated 2-D DFT of each channel plane (rfft2 on the
 //                    kept modes), scaled per ky
 //   fno_synthesis    its adjoint / the truncated inverse real DFT
 //   fno_mix          per-mode complex channel mixing (forward, and the
 //                    conjugate transpose for the backward pass)
 //   fno_mix_wgrad    per-mode weight gradient, a reduction over the batch
-//   fno_wgrad_*      pointwise weight gradients: per-tile partial products,
-//                    then an ordered reduction (deterministic)
+//   fno_wgrad_*      pointwise weight gradients: per-tile partial products
+//                    on the tensor cores, then an ordered reduction
+//                    (deterministic)
 //   fno_film_back    GELU' and the FiLM scale/shift gradients per plane
 //   fno_dense*       the conditioning MLP and its gradients
 //   fno_mse*         loss and output gradient
@@ -132,6 +136,122 @@ __global__ void __launch_bounds__(128) fno_pointwise(PW a) {
         else if (a.act == 2) r = z * gelu_d(a.gate[k]);
         a.out[k] = a.accumulate ? a.out[k] + r : r;
     }
+}
+
+// The channel mix on the tensor cores, for cout % 16 == 0 (cout <= 64) and
+// P % 32 == 0 (cin is padded to a multiple of 8 with zero weights and zero
+// inputs): each warp takes 32 voxels of one sample and
+// forms out[o][p] = sum_i W[o][i] in[i][p] with mma.sync m16n8k8 TF32
+// (fp32 accumulation), then runs the same epilogue as fno_pointwise.  The
+// bf16 weights are exact in TF32; each input value is split into its TF32
+// rounding and the TF32 rounding of the remainder, and both products are
+// accumulated, so the sums keep fp32-level accuracy.
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ void mma_tf32(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t a2,
+                                         uint32_t a3, uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+        "{%8,%9}, {%0,%1,%2,%3};"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+template <int MT>   // cout / 16
+__global__ void __launch_bounds__(128) fno_pointwise_tc(PW a) {
+    extern __shared__ float ws[];          // [cout][ci8 + 4] weights, then [cout] bias
+    const int ci8 = (a.cin + 7) & ~7;
+    const int ld = ci8 + 4;                // row pad: the A-fragment loads hit 32 banks
+    for (int e = threadIdx.x; e < a.cout * ci8; e += blockDim.x) {
+        const int o = e / ci8, i = e % ci8;
+        ws[o * ld + i] = i < a.cin ? bfv(a.w[a.trans ? i * a.cout + o : o * a.cin + i]) : 0.0f;
+    }
+    float* bs = ws + a.cout * ld;
+    for (int o = threadIdx.x; o < a.cout; o += blockDim.x) bs[o] = a.bias ? bfv(a.bias[o]) : 0.0f;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const long long v0 = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
+    if (v0 >= (long long)a.B * a.P) return;
+    const int b = (int)(v0 / a.P), p0 = (int)(v0 % a.P);
+    const float* src = a.in + (long long)b * a.in_bs + p0 + g;
+    float c[MT][4][4];
+#pragma unroll
+    for (int mt = 0; mt < MT; mt++)
+#pragma unroll
+        for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+            for (int q = 0; q < 4; q++) c[mt][nt][q] = 0.0f;
+    for (int i0 = 0; i0 < ci8; i0 += 8) {
+        // B fragments: rows i0 + t and i0 + t + 4, voxel column g of each 8
+        uint32_t bh[4][2], bl[4][2];
+#pragma unroll
+        for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int ii = i0 + t + 4 * h;
+                const float x = ii < a.cin ? src[(long long)ii * a.P + nt * 8] : 0.0f;
+                bh[nt][h] = to_tf32(x);
+                bl[nt][h] = to_tf32(x - __uint_as_float(bh[nt][h]));
+            }
+#pragma unroll
+        for (int mt = 0; mt < MT; mt++) {
+            const float* wr = ws + (mt * 16 + g) * ld + i0 + t;
+            const uint32_t a0 = __float_as_uint(wr[0]), a1 = __float_as_uint(wr[8 * ld]);
+            const uint32_t a2 = __float_as_uint(wr[4]), a3 = __float_as_uint(wr[8 * ld + 4]);
+#pragma unroll
+            for (int nt = 0; nt < 4; nt++) {
+                mma_tf32(c[mt][nt], a0, a1, a2, a3, bh[nt][0], bh[nt][1]);
+                mma_tf32(c[mt][nt], a0, a1, a2, a3, bl[nt][0], bl[nt][1]);
+            }
+        }
+    }
+    // epilogue: accumulator q holds (o, p) = (16 mt + g + 8 (q >> 1), p0 + 8 nt + 2 t + (q & 1))
+#pragma unroll
+    for (int mt = 0; mt < MT; mt++)
+#pragma unroll
+        for (int r = 0; r < 2; r++) {
+            const int o = mt * 16 + g + 8 * r;
+            const float bo = bs[o];
+            float f0 = 0.0f, f1 = 0.0f;
+            if (a.film) {
+                f0 = a.film[(long long)b * a.fs + o];
+                f1 = a.film[(long long)b * a.fs + a.cout + o];
+            }
+#pragma unroll
+            for (int nt = 0; nt < 4; nt++) {
+                const long long k = ((long long)b * a.cout + o) * a.P + p0 + nt * 8 + 2 * t;
+                float u[2] = {c[mt][nt][2 * r] + bo, c[mt][nt][2 * r + 1] + bo};
+                if (a.add) {
+                    const float2 ad = *reinterpret_cast<const float2*>(a.add + k);
+                    u[0] += ad.x;
+                    u[1] += ad.y;
+                }
+                if (a.pre) *reinterpret_cast<float2*>(a.pre + k) = make_float2(u[0], u[1]);
+                float2 gt = make_float2(0.0f, 0.0f);
+                if (a.act == 2) gt = *reinterpret_cast<const float2*>(a.gate + k);
+                float rr[2];
+#pragma unroll
+                for (int j = 0; j < 2; j++) {
+                    float z = u[j];
+                    if (a.film) z = u[j] * (1.0f + f0) + f1;
+                    float q = z;
+                    if (a.act == 1) q = gelu(z);
+                    else if (a.act == 2) q = z * gelu_d(j ? gt.y : gt.x);
+                    rr[j] = q;
+                }
+                float2* op = reinterpret_cast<float2*>(a.out + k);
+                if (a.accumulate) {
+                    const float2 prev = *op;
+                    rr[0] = prev.x + rr[0];
+                    rr[1] = prev.y + rr[1];
+                }
+                *op = make_float2(rr[0], rr[1]);
+            }
+        }
 }
 
 // ---------------------------------------------------------------------------
@@ -330,36 +450,72 @@ __global__ void fno_mix_wgrad(const float2* X, const float2* dY, float* gw, int 
 // db[o] = sum dY.  Partial sums per (sample, tile of kTile voxels), then an
 // ordered reduction over the tiles.
 // ---------------------------------------------------------------------------
-__global__ void fno_wgrad_partial(const float* dy, const float* x, long long x_bs, int O, int I,
-                                  int P, int tiles, float* part) {
+// The weight products run on the tensor cores: the tile's dY rows (A, O
+// padded to 16) and x rows (B, I padded to 8) are staged in shared memory,
+// each warp takes 16 x 8 output tiles, mma.sync m16n8k8 TF32 over the
+// tile's 128 voxels.  Both operands are split into TF32 high and low parts
+// and lo*hi + hi*lo + hi*hi accumulated in fp32 (fp32-level accuracy).
+// Partial rows: [O*I weights, O biases] per CTA.
+constexpr int kLdTc = kTile + 4;   // row pad: fragment loads hit 32 banks
+
+__global__ void __launch_bounds__(256) fno_wgrad_partial_tc(const float* dy, const float* x,
+                                                            long long x_bs, int O, int I, int P,
+                                                            int tiles, float* part) {
     extern __shared__ float sm[];
-    constexpr int LD = kTile + 1;
-    float* ys = sm;                  // [O][LD]
-    float* xs = sm + O * LD;         // [I][LD]
-    const int b = blockIdx.x / tiles, t = blockIdx.x % tiles;
-    const int p0 = t * kTile;
-    for (int e = threadIdx.x; e < O * kTile; e += blockDim.x) {
+    const int Op = (O + 15) & ~15, Ip = (I + 7) & ~7;
+    float* ys = sm;                  // [Op][kLdTc]
+    float* xs = sm + Op * kLdTc;     // [Ip][kLdTc]
+    const int b = blockIdx.x / tiles, tt = blockIdx.x % tiles;
+    const int p0 = tt * kTile;
+    for (int e = threadIdx.x; e < Op * kTile; e += blockDim.x) {
         const int o = e / kTile, pp = e % kTile, p = p0 + pp;
-        ys[o * LD + pp] = p < P ? dy[((long long)b * O + o) * P + p] : 0.0f;
+        ys[o * kLdTc + pp] = (o < O && p < P) ? dy[((long long)b * O + o) * P + p] : 0.0f;
     }
-    for (int e = threadIdx.x; e < I * kTile; e += blockDim.x) {
+    for (int e = threadIdx.x; e < Ip * kTile; e += blockDim.x) {
         const int i = e / kTile, pp = e % kTile, p = p0 + pp;
-        xs[i * LD + pp] = p < P ? x[(long long)b * x_bs + (long long)i * P + p] : 0.0f;
+        xs[i * kLdTc + pp] = (i < I && p < P) ? x[(long long)b * x_bs + (long long)i * P + p] : 0.0f;
     }
     __syncthreads();
-    const int E = O * I + O;
-    float* dst = part + (long long)blockIdx.x * E;
-    for (int e = threadIdx.x; e < E; e += blockDim.x) {
+    float* dst = part + (long long)blockIdx.x * (O * I + O);
+    for (int o = threadIdx.x; o < O; o += blockDim.x) {
+        const float* yr = ys + o * kLdTc;
         float s = 0.0f;
-        if (e < O * I) {
-            const float* yr = ys + (e / I) * LD;
-            const float* xr = xs + (e % I) * LD;
-            for (int pp = 0; pp < kTile; pp++) s += yr[pp] * xr[pp];
-        } else {
-            const float* yr = ys + (e - O * I) * LD;
-            for (int pp = 0; pp < kTile; pp++) s += yr[pp];
+        for (int pp = 0; pp < kTile; pp++) s += yr[pp];
+        dst[O * I + o] = s;
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int ntl = Ip / 8, ntiles = (Op / 16) * ntl;
+    for (int tile = warp; tile < ntiles; tile += (int)(blockDim.x >> 5)) {
+        const int mt = tile / ntl, nt = tile % ntl;
+        const float* ar = ys + (mt * 16 + g) * kLdTc + t;
+        const float* br = xs + (nt * 8 + g) * kLdTc + t;
+        float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll 4
+        for (int k0 = 0; k0 < kTile; k0 += 8) {
+            const float av[4] = {ar[k0], ar[k0 + 8 * kLdTc], ar[k0 + 4], ar[k0 + 8 * kLdTc + 4]};
+            const float bv[2] = {br[k0], br[k0 + 4]};
+            uint32_t ah[4], al[4], bh[2], bl[2];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                ah[q] = to_tf32(av[q]);
+                al[q] = to_tf32(av[q] - __uint_as_float(ah[q]));
+            }
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                bh[q] = to_tf32(bv[q]);
+                bl[q] = to_tf32(bv[q] - __uint_as_float(bh[q]));
+            }
+            mma_tf32(c, al[0], al[1], al[2], al[3], bh[0], bh[1]);
+            mma_tf32(c, ah[0], ah[1], ah[2], ah[3], bl[0], bl[1]);
+            mma_tf32(c, ah[0], ah[1], ah[2], ah[3], bh[0], bh[1]);
         }
-        dst[e] = s;
+        const int o = mt * 16 + g, i = nt * 8 + 2 * t;
+#pragma unroll
+        for (int r = 0; r < 2; r++)
+            if (o + 8 * r < O) {
+                if (i < I) dst[(o + 8 * r) * I + i] = c[2 * r];
+                if (i + 1 < I) dst[(o + 8 * r) * I + i + 1] = c[2 * r + 1];
+            }
     }
 }
 
@@ -636,6 +792,16 @@ void pointwise(sp_fno* f, PW a) {
     const long long n = (long long)a.B * a.P;
     const size_t smem = sizeof(float) * (a.cin * a.cout + a.cout);
     const int nb = (int)((n + tb - 1) / tb);
+    if (a.cout % 16 == 0 && a.cout <= 64 && a.cin <= 64 && a.P % 32 == 0) {
+        const size_t tsm = sizeof(float) * (a.cout * (((a.cin + 7) & ~7) + 4) + a.cout);
+        switch (a.cout / 16) {
+            case 1: fno_pointwise_tc<1><<<nb, tb, tsm, f->st>>>(a); break;
+            case 2: fno_pointwise_tc<2><<<nb, tb, tsm, f->st>>>(a); break;
+            case 3: fno_pointwise_tc<3><<<nb, tb, tsm, f->st>>>(a); break;
+            default: fno_pointwise_tc<4><<<nb, tb, tsm, f->st>>>(a); break;
+        }
+        return;
+    }
     if (a.cout <= 8) fno_pointwise<8><<<nb, tb, smem, f->st>>>(a);
     else if (a.cout <= 16) fno_pointwise<16><<<nb, tb, smem, f->st>>>(a);
     else if (a.cout <= 32) fno_pointwise<32><<<nb, tb, smem, f->st>>>(a);
@@ -665,8 +831,8 @@ void wgrad(sp_fno* f, const float* dy, const float* x, long long x_bs, int O, in
            float* gw, float* gb) {
     const int tiles = (f->P + kTile - 1) / kTile;
     const int nblk = B * tiles;
-    const size_t smem = sizeof(float) * (O + I) * (kTile + 1);
-    fno_wgrad_partial<<<nblk, 256, smem, f->st>>>(dy, x, x_bs, O, I, f->P, tiles, f->part);
+    const size_t smem = sizeof(float) * (((O + 15) & ~15) + ((I + 7) & ~7)) * kLdTc;
+    fno_wgrad_partial_tc<<<nblk, 256, smem, f->st>>>(dy, x, x_bs, O, I, f->P, tiles, f->part);
     const int E = O * I + O;
     fno_wgrad_reduce<<<(E + 31) / 32, 256, 0, f->st>>>(f->part, nblk, O, I, gw, gb);
 }
@@ -896,8 +1062,8 @@ int sp_fno_create(const sp_fno_shape* shape, sp_fno** out) {
         return SP_E_CUDA;
     }
     // the weight-gradient tiles of 64 x 64 channel pairs take 66 KB
-    e = cudaFuncSetAttribute(fno_wgrad_partial, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)(sizeof(float) * 128 * (kTile + 1)));
+    e = cudaFuncSetAttribute(fno_wgrad_partial_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(sizeof(float) * 128 * kLdTc));
     if (e != cudaSuccess) {
         sp_fno_destroy(f);
         return SP_E_CUDA;
