@@ -361,6 +361,243 @@ __global__ void fno_synthesis(const float2* in, float* out, const float2* tw_g, 
     }
 }
 
+// The same truncated DFTs on the tensor cores, one warp per channel plane,
+// for n % 16 == 0 and 2m <= 32 (n <= 64: at most 102 KB of shared memory).  Each is two real GEMMs against twiddle
+// matrices (fp32, computed in double) staged in shared memory, mma.sync
+// m16n8k8 TF32 with both operands split into high and low TF32 parts
+// (lo*hi + hi*lo + hi*hi in fp32):
+//   analysis   R[x][c] = sum_y f[x][y] T1[y][c], c < m: cos, m <= c < 2m: -sin
+//              (of 2 pi ky y / n); P[r][c] = sum_x T2[r][x] R[x][c], rows
+//              r < 2m: cos, 2m <= r < 4m: sin (of 2 pi kx x / n); then
+//              Re = P[kxi][ky] + P[2m+kxi][m+ky], Im = P[kxi][m+ky] - P[2m+kxi][ky]
+//   synthesis  Z[x][c] = sum_k U[x][k] V[k][c] with U = T2 transposed and V
+//              holding (Fr, Fi | -Fi, Fr) of the scaled modes, so Z = (Zr | Zi);
+//              f[x][y] = sum_c Z[x][c] W[c][y] with W = T1 transposed.
+// Padding rows and columns of the matrices are zero.  Row strides are chosen
+// so that every fragment load from shared memory touches 32 banks.
+constexpr int kDftWarps = 4;
+
+struct DftTc {
+    int N2, R4;       // 2m rounded up to 8, 4m rounded up to 16
+    int ld1, ld2;     // analysis T1 [y][c], T2 [r][x]
+    int ldR, ldP;     // analysis per-warp R [x][c], P [r][c]
+    int ldU, ldW;     // synthesis U [x][k], W [c][y]
+    int ldV, ldZ;     // synthesis per-warp V [k][c], Z [x][c]
+};
+
+__host__ __device__ inline DftTc dft_tc_layout(int n, int m) {
+    DftTc L;
+    L.N2 = (2 * m + 7) & ~7;
+    L.R4 = (4 * m + 15) & ~15;
+    const int r = L.N2 & 31;
+    L.ld1 = (r == 8 || r == 24) ? L.N2 : L.N2 + 8;   // B reads: (ld t + g) in 32 banks
+    L.ld2 = n + 4;                                   // A reads: (ld g + t) in 32 banks
+    L.ldR = L.ld1;
+    L.ldP = L.N2;
+    L.ldU = L.R4 + 4;
+    L.ldW = n + 8;
+    L.ldV = L.ld1;
+    L.ldZ = L.N2 + 4;
+    return L;
+}
+
+inline bool dft_tc_ok(int n, int m) { return n % 16 == 0 && 2 * m <= 32; }
+
+inline size_t dft_tc_smem(int n, int m, bool synthesis) {
+    const DftTc L = dft_tc_layout(n, m);
+    const size_t fl = synthesis
+        ? (size_t)n * L.ldU + (size_t)L.N2 * L.ldW + kDftWarps * ((size_t)L.R4 * L.ldV + (size_t)n * L.ldZ)
+        : (size_t)n * L.ld1 + (size_t)L.R4 * L.ld2 + kDftWarps * ((size_t)n * L.ldR + (size_t)L.R4 * L.ldP);
+    return sizeof(float) * fl;
+}
+
+__device__ __forceinline__ void split_tf32(float x, uint32_t& h, uint32_t& l) {
+    h = to_tf32(x);
+    l = to_tf32(x - __uint_as_float(h));
+}
+
+// c += a * b with a, b given as (high, low) TF32 parts
+__device__ __forceinline__ void mma3(float (&c)[4], const uint32_t (&ah)[4], const uint32_t (&al)[4],
+                                     const uint32_t (&bh)[2], const uint32_t (&bl)[2]) {
+    mma_tf32(c, al[0], al[1], al[2], al[3], bh[0], bh[1]);
+    mma_tf32(c, ah[0], ah[1], ah[2], ah[3], bl[0], bl[1]);
+    mma_tf32(c, ah[0], ah[1], ah[2], ah[3], bh[0], bh[1]);
+}
+
+// A fragment of rows g, g + 8 and columns t, t + 4 from row-major p (stride ld),
+// p pointing at [row g][column t]
+__device__ __forceinline__ void frag_a(const float* p, int ld, uint32_t (&h)[4], uint32_t (&l)[4]) {
+    split_tf32(p[0], h[0], l[0]);
+    split_tf32(p[8 * ld], h[1], l[1]);
+    split_tf32(p[4], h[2], l[2]);
+    split_tf32(p[8 * ld + 4], h[3], l[3]);
+}
+
+// B fragment of rows (k) t, t + 4 and column (n) g from row-major [k][n] p
+// (stride ld), p pointing at [row t][column g]
+__device__ __forceinline__ void frag_b(const float* p, int ld, uint32_t (&h)[2], uint32_t (&l)[2]) {
+    split_tf32(p[0], h[0], l[0]);
+    split_tf32(p[4 * ld], h[1], l[1]);
+}
+
+// the 16 x 8 accumulator tile (rows r0 + g, r0 + g + 8; columns c0 + 2t, + 1)
+__device__ __forceinline__ void store_c(float* p, int ld, int r0, int c0, int g, int t,
+                                        const float (&c)[4]) {
+    float* q = p + (r0 + g) * ld + c0 + 2 * t;
+    q[0] = c[0];
+    q[1] = c[1];
+    q[8 * ld] = c[2];
+    q[8 * ld + 1] = c[3];
+}
+
+__global__ void __launch_bounds__(32 * kDftWarps) fno_analysis_tc(const float* in, float2* out,
+                                                                   const float* tA1,
+                                                                   const float* tA2,
+                                                                   const float* s_g, int n,
+                                                                   int m, int planes) {
+    extern __shared__ float sd[];
+    const DftTc L = dft_tc_layout(n, m);
+    float* T1 = sd;                        // [n][ld1]
+    float* T2 = T1 + n * L.ld1;            // [R4][ld2]
+    float* scr = T2 + L.R4 * L.ld2;
+    for (int e = threadIdx.x; e < n * L.N2; e += blockDim.x) T1[(e / L.N2) * L.ld1 + e % L.N2] = tA1[e];
+    for (int e = threadIdx.x; e < L.R4 * n; e += blockDim.x) T2[(e / n) * L.ld2 + e % n] = tA2[e];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const long long plane = (long long)blockIdx.x * kDftWarps + warp;
+    if (plane >= planes) return;
+    float* R = scr + warp * (n * L.ldR + L.R4 * L.ldP);
+    float* Pm = R + n * L.ldR;
+    const float* f = in + plane * n * n;
+    const int NT = L.N2 / 8;
+    uint32_t ah[4], al[4], bh[2], bl[2];
+    // R = f T1: M = n (x), K = n (y), N = N2 (c)
+    for (int mt = 0; mt < n / 16; mt++) {
+        float c[4][4] = {};
+        for (int k0 = 0; k0 < n; k0 += 8) {
+            frag_a(f + (mt * 16 + g) * n + k0 + t, n, ah, al);
+#pragma unroll
+            for (int nt = 0; nt < 4; nt++)
+                if (nt < NT) {
+                    frag_b(T1 + (k0 + t) * L.ld1 + nt * 8 + g, L.ld1, bh, bl);
+                    mma3(c[nt], ah, al, bh, bl);
+                }
+        }
+#pragma unroll
+        for (int nt = 0; nt < 4; nt++)
+            if (nt < NT) store_c(R, L.ldR, mt * 16, nt * 8, g, t, c[nt]);
+    }
+    __syncwarp();
+    // P = T2 R: M = R4 (r), K = n (x), N = N2 (c)
+    for (int mt = 0; mt < L.R4 / 16; mt++) {
+        float c[4][4] = {};
+        for (int k0 = 0; k0 < n; k0 += 8) {
+            frag_a(T2 + (mt * 16 + g) * L.ld2 + k0 + t, L.ld2, ah, al);
+#pragma unroll
+            for (int nt = 0; nt < 4; nt++)
+                if (nt < NT) {
+                    frag_b(R + (k0 + t) * L.ldR + nt * 8 + g, L.ldR, bh, bl);
+                    mma3(c[nt], ah, al, bh, bl);
+                }
+        }
+#pragma unroll
+        for (int nt = 0; nt < 4; nt++)
+            if (nt < NT) store_c(Pm, L.ldP, mt * 16, nt * 8, g, t, c[nt]);
+    }
+    __syncwarp();
+    const int M = 2 * m * m;
+    float2* dst = out + plane * M;
+    for (int q = lane; q < M; q += 32) {
+        const int kxi = q / m, ky = q % m;
+        const float re = Pm[kxi * L.ldP + ky] + Pm[(2 * m + kxi) * L.ldP + m + ky];
+        const float im = Pm[kxi * L.ldP + m + ky] - Pm[(2 * m + kxi) * L.ldP + ky];
+        const float sc = s_g[ky];
+        dst[q] = make_float2(sc * re, sc * im);
+    }
+}
+
+__global__ void __launch_bounds__(32 * kDftWarps) fno_synthesis_tc(const float2* in, float* out,
+                                                                    const float* tS1,
+                                                                    const float* tS2,
+                                                                    const float* s_g, int n,
+                                                                    int m, int planes,
+                                                                    int accumulate) {
+    extern __shared__ float sd[];
+    const DftTc L = dft_tc_layout(n, m);
+    float* U = sd;                         // [n][ldU]
+    float* W = U + n * L.ldU;              // [N2][ldW]
+    float* scr = W + L.N2 * L.ldW;
+    for (int e = threadIdx.x; e < n * L.R4; e += blockDim.x) U[(e / L.R4) * L.ldU + e % L.R4] = tS1[e];
+    for (int e = threadIdx.x; e < L.N2 * n; e += blockDim.x) W[(e / n) * L.ldW + e % n] = tS2[e];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const long long plane = (long long)blockIdx.x * kDftWarps + warp;
+    if (plane >= planes) return;
+    float* V = scr + warp * (L.R4 * L.ldV + n * L.ldZ);
+    float* Z = V + L.R4 * L.ldV;
+    const int M = 2 * m * m, NT = L.N2 / 8;
+    for (int e = lane; e < L.R4 * L.ldV; e += 32) V[e] = 0.0f;
+    __syncwarp();
+    const float2* src = in + plane * M;
+    for (int q = lane; q < M; q += 32) {
+        const int kxi = q / m, ky = q % m;
+        const float2 v = src[q];
+        const float sc = s_g[ky];
+        const float vr = sc * v.x, vi = sc * v.y;
+        V[kxi * L.ldV + ky] = vr;
+        V[kxi * L.ldV + m + ky] = vi;
+        V[(2 * m + kxi) * L.ldV + ky] = -vi;
+        V[(2 * m + kxi) * L.ldV + m + ky] = vr;
+    }
+    __syncwarp();
+    uint32_t ah[4], al[4], bh[2], bl[2];
+    // Z = U V: M = n (x), K = R4 (k), N = N2 (c)
+    for (int mt = 0; mt < n / 16; mt++) {
+        float c[4][4] = {};
+        for (int k0 = 0; k0 < L.R4; k0 += 8) {
+            frag_a(U + (mt * 16 + g) * L.ldU + k0 + t, L.ldU, ah, al);
+#pragma unroll
+            for (int nt = 0; nt < 4; nt++)
+                if (nt < NT) {
+                    frag_b(V + (k0 + t) * L.ldV + nt * 8 + g, L.ldV, bh, bl);
+                    mma3(c[nt], ah, al, bh, bl);
+                }
+        }
+#pragma unroll
+        for (int nt = 0; nt < 4; nt++)
+            if (nt < NT) store_c(Z, L.ldZ, mt * 16, nt * 8, g, t, c[nt]);
+    }
+    __syncwarp();
+    // f = Z W: M = n (x), K = N2 (c), N = n (y), two column tiles at a time
+    float* dst = out + plane * n * n;
+    for (int mt = 0; mt < n / 16; mt++)
+        for (int nt0 = 0; nt0 < n / 8; nt0 += 2) {
+            float c[2][4] = {};
+            for (int k0 = 0; k0 < L.N2; k0 += 8) {
+                frag_a(Z + (mt * 16 + g) * L.ldZ + k0 + t, L.ldZ, ah, al);
+#pragma unroll
+                for (int j = 0; j < 2; j++) {
+                    frag_b(W + (k0 + t) * L.ldW + (nt0 + j) * 8 + g, L.ldW, bh, bl);
+                    mma3(c[j], ah, al, bh, bl);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < 2; j++)
+#pragma unroll
+                for (int r = 0; r < 2; r++) {
+                    float2* q = reinterpret_cast<float2*>(dst + (mt * 16 + g + 8 * r) * n +
+                                                          (nt0 + j) * 8 + 2 * t);
+                    float2 v = make_float2(c[j][2 * r], c[j][2 * r + 1]);
+                    if (accumulate) {
+                        const float2 o = *q;
+                        v.x = o.x + v.x;
+                        v.y = o.y + v.y;
+                    }
+                    *q = v;
+                }
+        }
+}
+
 // ---------------------------------------------------------------------------
 // per-mode channel mixing (one CTA per mode q)
 // conj_t = 0: Y[b][o][q] = sum_i X[b][i][q] W[q][i][o]
@@ -707,6 +944,8 @@ struct sp_fno {
     uint16_t* pb = nullptr;
     float2* tw = nullptr;
     float *s_one = nullptr, *s_inv = nullptr;
+    // twiddle matrices of the tensor-core DFTs (null when the shape does not fit them)
+    float *tA1 = nullptr, *tA2 = nullptr, *tS1 = nullptr, *tS2 = nullptr;
     // activations [layers+1] h, [layers] u, [layers] X
     float *h = nullptr, *u = nullptr, *sbuf = nullptr, *q = nullptr, *a = nullptr;
     float2 *X = nullptr, *Y = nullptr;
@@ -817,12 +1056,24 @@ PW pw_base(const sp_fno* f, int B) {
 
 void analysis(sp_fno* f, const float* in, float2* out, int planes, const float* scale) {
     const int n = f->s.n, m = f->s.modes;
+    if (f->tA1) {
+        fno_analysis_tc<<<(planes + kDftWarps - 1) / kDftWarps, 32 * kDftWarps,
+                          dft_tc_smem(n, m, false), f->st>>>(in, out, f->tA1, f->tA2, scale, n, m,
+                                                            planes);
+        return;
+    }
     const size_t smem = sizeof(float) * ((n * n + 1) & ~1) + sizeof(float2) * (n * m + n);
     fno_analysis<<<planes, 256, smem, f->st>>>(in, out, f->tw, scale, n, m);
 }
 
 void synthesis(sp_fno* f, const float2* in, float* out, int planes, const float* scale, int acc) {
     const int n = f->s.n, m = f->s.modes;
+    if (f->tS1) {
+        fno_synthesis_tc<<<(planes + kDftWarps - 1) / kDftWarps, 32 * kDftWarps,
+                           dft_tc_smem(n, m, true), f->st>>>(in, out, f->tS1, f->tS2, scale, n, m,
+                                                            planes, acc);
+        return;
+    }
     const size_t smem = sizeof(float2) * (2 * m * m + n * m + n);
     fno_synthesis<<<planes, 256, smem, f->st>>>(in, out, f->tw, scale, n, m, acc);
 }
@@ -1015,6 +1266,14 @@ int sp_fno_create(const sp_fno_shape* shape, sp_fno** out) {
     f->pb = dalloc<uint16_t>(f, np, ok);
     f->hyper = dalloc<float>(f, 8, ok);
     f->tw = dalloc<float2>(f, s.n, ok);
+    const DftTc DL = dft_tc_layout(s.n, s.modes);
+    const bool dft_tc = dft_tc_ok(s.n, s.modes);
+    if (dft_tc) {
+        f->tA1 = dalloc<float>(f, (long long)s.n * DL.N2, ok);
+        f->tA2 = dalloc<float>(f, (long long)DL.R4 * s.n, ok);
+        f->tS1 = dalloc<float>(f, (long long)s.n * DL.R4, ok);
+        f->tS2 = dalloc<float>(f, (long long)DL.N2 * s.n, ok);
+    }
     f->s_one = dalloc<float>(f, s.modes, ok);
     f->s_inv = dalloc<float>(f, s.modes, ok);
     const long long FC = Bm * C * P;
@@ -1078,6 +1337,45 @@ int sp_fno_create(const sp_fno_shape* shape, sp_fno** out) {
     for (int k = 0; k < s.modes; k++)
         inv[k] = (float)((k == 0 ? 1.0 : 2.0) / ((double)s.n * (double)s.n));
     e = cudaMemcpy(f->tw, tw.data(), sizeof(float2) * s.n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && dft_tc) {
+        // the DFT matrices of the tensor-core kernels, from double precision
+        const int n = s.n, m = s.modes, N2 = DL.N2, R4 = DL.R4;
+        auto cs = [n](long long k, bool sine) {
+            const double th = 6.283185307179586477 * (double)(((k % n) + n) % n) / (double)n;
+            return (float)(sine ? std::sin(th) : std::cos(th));
+        };
+        auto kx_of = [n, m](int kxi) { return kxi < m ? kxi : n - 2 * m + kxi; };
+        std::vector<float> a1((size_t)n * N2, 0.0f), a2((size_t)R4 * n, 0.0f);
+        std::vector<float> s1((size_t)n * R4), s2((size_t)N2 * n);
+        for (int y = 0; y < n; y++)
+            for (int c = 0; c < 2 * m; c++)
+                a1[(size_t)y * N2 + c] = c < m ? cs((long long)c * y, false)
+                                               : -cs((long long)(c - m) * y, true);
+        for (int r = 0; r < 4 * m; r++)
+            for (int x = 0; x < n; x++)
+                a2[(size_t)r * n + x] = r < 2 * m ? cs((long long)kx_of(r) * x, false)
+                                                  : cs((long long)kx_of(r - 2 * m) * x, true);
+        for (int x = 0; x < n; x++)
+            for (int k = 0; k < R4; k++) s1[(size_t)x * R4 + k] = a2[(size_t)k * n + x];
+        for (int c = 0; c < N2; c++)
+            for (int y = 0; y < n; y++) s2[(size_t)c * n + y] = a1[(size_t)y * N2 + c];
+        e = cudaMemcpy(f->tA1, a1.data(), sizeof(float) * a1.size(), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(f->tA2, a2.data(), sizeof(float) * a2.size(), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(f->tS1, s1.data(), sizeof(float) * s1.size(), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(f->tS2, s2.data(), sizeof(float) * s2.size(), cudaMemcpyHostToDevice);
+        // the attribute is per kernel, not per network: the largest shape
+        // of the tensor-core path (n = 64, 2m = 32), so that networks of
+        // several shapes can share a process
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(fno_analysis_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)dft_tc_smem(64, 16, false));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(fno_synthesis_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)dft_tc_smem(64, 16, true));
+    }
     if (e == cudaSuccess)
         e = cudaMemcpy(f->s_one, one.data(), sizeof(float) * s.modes, cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
