@@ -513,18 +513,18 @@ def run_fno(args):
             pass
         return {"metric": "surrogate training samples/s", "value": B / (ms / 1e3),
                 "unit": "samples/s", "steps": K, "warmup": W, "ms_per_step": ms,
-                "dtype": "bf16 weights, f32 data (tensor-core products on split TF32 operands)",
+                "dtype": "bf16 weights, f32 data (tensor-core products on split operands)",
                 "gpu_launches": 69 * K,
                 "config": {"workload": "FiLM FNO training step, 32x32 lattice, width 32, "
                                        "12 modes, 4 layers, batch 64", "loss": loss},
                 "roofline": {"bound": "tensor", "achieved": tflops, "peak": peak,
                              "unit": "TFLOP/s", "frac": tflops / peak, "traffic": None,
                              "peak_source": peak_src,
-                             "note": "algorithmic flops; the channel mixes, their weight "
-                                     "gradients and the DFTs run as mma.sync TF32 with split "
-                                     "operands (2-3 products per multiply), the per-mode mixes "
-                                     "on CUDA cores; small contractions at ~8 flop/byte are "
-                                     "latency bound"}}
+                             "note": "algorithmic flops; the channel mixes and DFTs run as "
+                                     "mma.sync bf16, the weight gradients as mma.sync TF32, "
+                                     "with split operands (2-3 products per multiply), the "
+                                     "per-mode mixes on CUDA cores; small contractions at ~8 "
+                                     "flop/byte are latency bound"}}
     except Exception as ex:         # a secondary line never takes the headline down
         return {"metric": "surrogate training samples/s", "error": repr(ex)}
 

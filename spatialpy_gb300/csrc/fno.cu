@@ -8,9 +8,10 @@
 // Work per sample is small and the contractions are width-32 channel mixes
 // (2 x 32 x 32 flops per voxel and layer against 256 bytes of field traffic,
 // 8 flop/byte), so the kernels are bound by memory and launch latency.  The
-// channel mixes and their weight gradients run on the tensor cores (mma.sync
-// TF32 with fp32 operands split into high and low TF32 parts, so the sums
-// keep fp32-level accuracy); the DFTs and the per-mode mixing are fp32
+// channel mixes and the truncated DFTs run on the tensor cores as mma.sync
+// bf16, the channel mixes' weight gradients as mma.sync TF32, with fp32
+// operands split into a high part and the rounding of the remainder so that
+// the sums keep fp32-level accuracy; the per-mode complex mixing is fp32
 // CUDA-core code.  A training step (about 70 launches) is captured once per
 // batch size as a CUDA graph and replayed.
 //
@@ -21,8 +22,10 @@
 //                    GELU and GELU' epilogues; fno_pointwise_tc on the
 //                    tensor cores where cout is a multiple of 16
 //   fno_analysis     truncated 2-D DFT of each channel plane (rfft2 on the
-//                    kept modes), scaled per ky
-//   fno_synthesis    its adjoint / the truncated inverse real DFT
+//                    kept modes), scaled per ky; fno_analysis_tc on the
+//                    tensor cores where n % 16 == 0 and 2m <= 32
+//   fno_synthesis    its adjoint / the truncated inverse real DFT (and
+//                    fno_synthesis_tc)
 //   fno_mix          per-mode complex channel mixing (forward, and the
 //                    conjugate transpose for the backward pass)
 //   fno_mix_wgrad    per-mode weight gradient, a reduction over the batch
@@ -138,14 +141,10 @@ __global__ void __launch_bounds__(128) fno_pointwise(PW a) {
     }
 }
 
-// The channel mix on the tensor cores, for cout % 16 == 0 (cout <= 64) and
-// P % 32 == 0 (cin is padded to a multiple of 8 with zero weights and zero
-// inputs): each warp takes 32 voxels of one sample and
-// forms out[o][p] = sum_i W[o][i] in[i][p] with mma.sync m16n8k8 TF32
-// (fp32 accumulation), then runs the same epilogue as fno_pointwise.  The
-// bf16 weights are exact in TF32; each input value is split into its TF32
-// rounding and the TF32 rounding of the remainder, and both products are
-// accumulated, so the sums keep fp32-level accuracy.
+// Tensor-core helpers: mma.sync m16n8k8 TF32 and m16n8k16 bf16, fp32
+// accumulation.  fp32 operands are split into a high part and the rounding
+// of the remainder, and the partial products summed, so that the sums keep
+// fp32-level accuracy.
 __device__ __forceinline__ uint32_t to_tf32(float x) {
     uint32_t r;
     asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
@@ -161,16 +160,42 @@ __device__ __forceinline__ void mma_tf32(float (&c)[4], uint32_t a0, uint32_t a1
         : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
+__device__ __forceinline__ void mma_bf16(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t a2,
+                                         uint32_t a3, uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+        "{%8,%9}, {%0,%1,%2,%3};"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// (e0, e1) -> bf16 pairs (lower index in the low half): h = rn(e), l = rn(e - h)
+__device__ __forceinline__ void split_bf16x2(float e0, float e1, uint32_t& h, uint32_t& l) {
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(h) : "f"(e1), "f"(e0));
+    const float h0 = __uint_as_float(h << 16), h1 = __uint_as_float(h & 0xffff0000u);
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(l) : "f"(e1 - h1), "f"(e0 - h0));
+}
+
+// The channel mix on the tensor cores, for cout % 16 == 0 (cout <= 64) and
+// P % 32 == 0 (cin padded to a multiple of 16 with zero weights and zero
+// inputs): each warp takes 32 voxels of one sample and forms
+// out[o][p] = sum_i W[o][i] in[i][p] with mma.sync m16n8k16 bf16, then runs
+// the same epilogue as fno_pointwise.  The weights are bf16 already; each
+// input is split into two bf16 parts (16 significant bits) and both
+// products accumulated in fp32.
 template <int MT>   // cout / 16
 __global__ void __launch_bounds__(128) fno_pointwise_tc(PW a) {
-    extern __shared__ float ws[];          // [cout][ci8 + 4] weights, then [cout] bias
-    const int ci8 = (a.cin + 7) & ~7;
-    const int ld = ci8 + 4;                // row pad: the A-fragment loads hit 32 banks
-    for (int e = threadIdx.x; e < a.cout * ci8; e += blockDim.x) {
-        const int o = e / ci8, i = e % ci8;
-        ws[o * ld + i] = i < a.cin ? bfv(a.w[a.trans ? i * a.cout + o : o * a.cin + i]) : 0.0f;
+    extern __shared__ uint32_t wp[];       // [cout][ci16 / 2 + 4] bf16 weight pairs, then [cout] bias
+    const int ci16 = (a.cin + 15) & ~15;
+    const int ldp = ci16 / 2 + 4;          // pairs per row: the A-fragment loads hit 32 banks
+    for (int e = threadIdx.x; e < a.cout * (ci16 / 2); e += blockDim.x) {
+        const int o = e / (ci16 / 2), i = 2 * (e % (ci16 / 2));
+        uint32_t lo = 0, hi = 0;
+        if (i < a.cin) lo = a.w[a.trans ? i * a.cout + o : o * a.cin + i];
+        if (i + 1 < a.cin) hi = a.w[a.trans ? (i + 1) * a.cout + o : o * a.cin + i + 1];
+        wp[o * ldp + e % (ci16 / 2)] = lo | (hi << 16);
     }
-    float* bs = ws + a.cout * ld;
+    float* bs = reinterpret_cast<float*>(wp + a.cout * ldp);
     for (int o = threadIdx.x; o < a.cout; o += blockDim.x) bs[o] = a.bias ? bfv(a.bias[o]) : 0.0f;
     __syncthreads();
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
@@ -185,27 +210,26 @@ __global__ void __launch_bounds__(128) fno_pointwise_tc(PW a) {
         for (int nt = 0; nt < 4; nt++)
 #pragma unroll
             for (int q = 0; q < 4; q++) c[mt][nt][q] = 0.0f;
-    for (int i0 = 0; i0 < ci8; i0 += 8) {
-        // B fragments: rows i0 + t and i0 + t + 4, voxel column g of each 8
+    for (int i0 = 0; i0 < ci16; i0 += 16) {
+        // B fragments: rows (2t, 2t+1) and (2t+8, 2t+9) of this K step, voxel column g
         uint32_t bh[4][2], bl[4][2];
 #pragma unroll
         for (int nt = 0; nt < 4; nt++)
 #pragma unroll
             for (int h = 0; h < 2; h++) {
-                const int ii = i0 + t + 4 * h;
-                const float x = ii < a.cin ? src[(long long)ii * a.P + nt * 8] : 0.0f;
-                bh[nt][h] = to_tf32(x);
-                bl[nt][h] = to_tf32(x - __uint_as_float(bh[nt][h]));
+                const int ii = i0 + 2 * t + 8 * h;
+                const float x0 = ii < a.cin ? src[(long long)ii * a.P + nt * 8] : 0.0f;
+                const float x1 = ii + 1 < a.cin ? src[(long long)(ii + 1) * a.P + nt * 8] : 0.0f;
+                split_bf16x2(x0, x1, bh[nt][h], bl[nt][h]);
             }
 #pragma unroll
         for (int mt = 0; mt < MT; mt++) {
-            const float* wr = ws + (mt * 16 + g) * ld + i0 + t;
-            const uint32_t a0 = __float_as_uint(wr[0]), a1 = __float_as_uint(wr[8 * ld]);
-            const uint32_t a2 = __float_as_uint(wr[4]), a3 = __float_as_uint(wr[8 * ld + 4]);
+            const uint32_t* wr = wp + (mt * 16 + g) * ldp + i0 / 2 + t;
+            const uint32_t a0 = wr[0], a1 = wr[8 * ldp], a2 = wr[4], a3 = wr[8 * ldp + 4];
 #pragma unroll
             for (int nt = 0; nt < 4; nt++) {
-                mma_tf32(c[mt][nt], a0, a1, a2, a3, bh[nt][0], bh[nt][1]);
-                mma_tf32(c[mt][nt], a0, a1, a2, a3, bl[nt][0], bl[nt][1]);
+                mma_bf16(c[mt][nt], a0, a1, a2, a3, bl[nt][0], bl[nt][1]);
+                mma_bf16(c[mt][nt], a0, a1, a2, a3, bh[nt][0], bh[nt][1]);
             }
         }
     }
@@ -362,10 +386,10 @@ __global__ void fno_synthesis(const float2* in, float* out, const float2* tw_g, 
 }
 
 // The same truncated DFTs on the tensor cores, one warp per channel plane,
-// for n % 16 == 0 and 2m <= 32 (n <= 64: at most 102 KB of shared memory).  Each is two real GEMMs against twiddle
-// matrices (fp32, computed in double) staged in shared memory, mma.sync
-// m16n8k8 TF32 with both operands split into high and low TF32 parts
-// (lo*hi + hi*lo + hi*hi in fp32):
+// for n % 16 == 0 and 2m <= 32 (n <= 64: at most 103 KB of shared memory).
+// Each is two real GEMMs against twiddle matrices (fp32, computed in
+// double) staged in shared memory, mma.sync m16n8k16 bf16 with both
+// operands split into two bf16 parts (lo*hi + hi*lo + hi*hi in fp32):
 //   analysis   R[x][c] = sum_y f[x][y] T1[y][c], c < m: cos, m <= c < 2m: -sin
 //              (of 2 pi ky y / n); P[r][c] = sum_x T2[r][x] R[x][c], rows
 //              r < 2m: cos, 2m <= r < 4m: sin (of 2 pi kx x / n); then
@@ -374,30 +398,32 @@ __global__ void fno_synthesis(const float2* in, float* out, const float2* tw_g, 
 //              holding (Fr, Fi | -Fi, Fr) of the scaled modes, so Z = (Zr | Zi);
 //              f[x][y] = sum_c Z[x][c] W[c][y] with W = T1 transposed.
 // Padding rows and columns of the matrices are zero.  Row strides are chosen
-// so that every fragment load from shared memory touches 32 banks.
+// so that every fragment load from shared memory touches 32 banks: A
+// fragments (float pairs at [g][2t]) want a stride of 8 mod 16 words, B
+// fragments (rows 2t, 2t+1 at column g) 4 mod 8.
 constexpr int kDftWarps = 4;
 
 struct DftTc {
-    int N2, R4;       // 2m rounded up to 8, 4m rounded up to 16
-    int ld1, ld2;     // analysis T1 [y][c], T2 [r][x]
-    int ldR, ldP;     // analysis per-warp R [x][c], P [r][c]
-    int ldU, ldW;     // synthesis U [x][k], W [c][y]
-    int ldV, ldZ;     // synthesis per-warp V [k][c], Z [x][c]
+    int N2, K2, R4;   // 2m rounded up to 8 and to 16, 4m rounded up to 16
+    int ld1, ld2;     // analysis T1 [y][c] (B), T2 [r][x] (A)
+    int ldR, ldP;     // analysis per-warp R [x][c] (B), P [r][c]
+    int ldU, ldW;     // synthesis U [x][k] (A), W [c][y] (B)
+    int ldV, ldZ;     // synthesis per-warp V [k][c] (B), Z [x][c] (A)
 };
 
 __host__ __device__ inline DftTc dft_tc_layout(int n, int m) {
     DftTc L;
     L.N2 = (2 * m + 7) & ~7;
+    L.K2 = (2 * m + 15) & ~15;
     L.R4 = (4 * m + 15) & ~15;
-    const int r = L.N2 & 31;
-    L.ld1 = (r == 8 || r == 24) ? L.N2 : L.N2 + 8;   // B reads: (ld t + g) in 32 banks
-    L.ld2 = n + 4;                                   // A reads: (ld g + t) in 32 banks
-    L.ldR = L.ld1;
+    L.ld1 = L.N2 + 4;
+    L.ld2 = n + 8;
+    L.ldR = L.N2 + 4;
     L.ldP = L.N2;
-    L.ldU = L.R4 + 4;
-    L.ldW = n + 8;
-    L.ldV = L.ld1;
-    L.ldZ = L.N2 + 4;
+    L.ldU = L.R4 + 8;
+    L.ldW = n + 4;
+    L.ldV = L.N2 + 4;
+    L.ldZ = L.K2 + 8;
     return L;
 }
 
@@ -406,38 +432,37 @@ inline bool dft_tc_ok(int n, int m) { return n % 16 == 0 && 2 * m <= 32; }
 inline size_t dft_tc_smem(int n, int m, bool synthesis) {
     const DftTc L = dft_tc_layout(n, m);
     const size_t fl = synthesis
-        ? (size_t)n * L.ldU + (size_t)L.N2 * L.ldW + kDftWarps * ((size_t)L.R4 * L.ldV + (size_t)n * L.ldZ)
+        ? (size_t)n * L.ldU + (size_t)L.K2 * L.ldW + kDftWarps * ((size_t)L.R4 * L.ldV + (size_t)n * L.ldZ)
         : (size_t)n * L.ld1 + (size_t)L.R4 * L.ld2 + kDftWarps * ((size_t)n * L.ldR + (size_t)L.R4 * L.ldP);
     return sizeof(float) * fl;
 }
 
-__device__ __forceinline__ void split_tf32(float x, uint32_t& h, uint32_t& l) {
-    h = to_tf32(x);
-    l = to_tf32(x - __uint_as_float(h));
-}
-
-// c += a * b with a, b given as (high, low) TF32 parts
+// c += a * b with a, b given as (high, low) bf16 parts
 __device__ __forceinline__ void mma3(float (&c)[4], const uint32_t (&ah)[4], const uint32_t (&al)[4],
                                      const uint32_t (&bh)[2], const uint32_t (&bl)[2]) {
-    mma_tf32(c, al[0], al[1], al[2], al[3], bh[0], bh[1]);
-    mma_tf32(c, ah[0], ah[1], ah[2], ah[3], bl[0], bl[1]);
-    mma_tf32(c, ah[0], ah[1], ah[2], ah[3], bh[0], bh[1]);
+    mma_bf16(c, al[0], al[1], al[2], al[3], bh[0], bh[1]);
+    mma_bf16(c, ah[0], ah[1], ah[2], ah[3], bl[0], bl[1]);
+    mma_bf16(c, ah[0], ah[1], ah[2], ah[3], bh[0], bh[1]);
 }
 
-// A fragment of rows g, g + 8 and columns t, t + 4 from row-major p (stride ld),
-// p pointing at [row g][column t]
+// A fragment (16 x 16) of rows g, g + 8 and column pairs 2t, 2t + 8 from
+// row-major p (stride ld, even), p pointing at [row g][column 2t]
 __device__ __forceinline__ void frag_a(const float* p, int ld, uint32_t (&h)[4], uint32_t (&l)[4]) {
-    split_tf32(p[0], h[0], l[0]);
-    split_tf32(p[8 * ld], h[1], l[1]);
-    split_tf32(p[4], h[2], l[2]);
-    split_tf32(p[8 * ld + 4], h[3], l[3]);
+    const float2 u0 = *reinterpret_cast<const float2*>(p);
+    const float2 u1 = *reinterpret_cast<const float2*>(p + 8 * ld);
+    const float2 u2 = *reinterpret_cast<const float2*>(p + 8);
+    const float2 u3 = *reinterpret_cast<const float2*>(p + 8 * ld + 8);
+    split_bf16x2(u0.x, u0.y, h[0], l[0]);
+    split_bf16x2(u1.x, u1.y, h[1], l[1]);
+    split_bf16x2(u2.x, u2.y, h[2], l[2]);
+    split_bf16x2(u3.x, u3.y, h[3], l[3]);
 }
 
-// B fragment of rows (k) t, t + 4 and column (n) g from row-major [k][n] p
-// (stride ld), p pointing at [row t][column g]
+// B fragment (16 x 8) of row pairs 2t, 2t + 8 and column g from row-major
+// [k][n] p (stride ld), p pointing at [row 2t][column g]
 __device__ __forceinline__ void frag_b(const float* p, int ld, uint32_t (&h)[2], uint32_t (&l)[2]) {
-    split_tf32(p[0], h[0], l[0]);
-    split_tf32(p[4 * ld], h[1], l[1]);
+    split_bf16x2(p[0], p[ld], h[0], l[0]);
+    split_bf16x2(p[8 * ld], p[9 * ld], h[1], l[1]);
 }
 
 // the 16 x 8 accumulator tile (rows r0 + g, r0 + g + 8; columns c0 + 2t, + 1)
@@ -474,12 +499,12 @@ __global__ void __launch_bounds__(32 * kDftWarps) fno_analysis_tc(const float* i
     // R = f T1: M = n (x), K = n (y), N = N2 (c)
     for (int mt = 0; mt < n / 16; mt++) {
         float c[4][4] = {};
-        for (int k0 = 0; k0 < n; k0 += 8) {
-            frag_a(f + (mt * 16 + g) * n + k0 + t, n, ah, al);
+        for (int k0 = 0; k0 < n; k0 += 16) {
+            frag_a(f + (mt * 16 + g) * n + k0 + 2 * t, n, ah, al);
 #pragma unroll
             for (int nt = 0; nt < 4; nt++)
                 if (nt < NT) {
-                    frag_b(T1 + (k0 + t) * L.ld1 + nt * 8 + g, L.ld1, bh, bl);
+                    frag_b(T1 + (k0 + 2 * t) * L.ld1 + nt * 8 + g, L.ld1, bh, bl);
                     mma3(c[nt], ah, al, bh, bl);
                 }
         }
@@ -491,12 +516,12 @@ __global__ void __launch_bounds__(32 * kDftWarps) fno_analysis_tc(const float* i
     // P = T2 R: M = R4 (r), K = n (x), N = N2 (c)
     for (int mt = 0; mt < L.R4 / 16; mt++) {
         float c[4][4] = {};
-        for (int k0 = 0; k0 < n; k0 += 8) {
-            frag_a(T2 + (mt * 16 + g) * L.ld2 + k0 + t, L.ld2, ah, al);
+        for (int k0 = 0; k0 < n; k0 += 16) {
+            frag_a(T2 + (mt * 16 + g) * L.ld2 + k0 + 2 * t, L.ld2, ah, al);
 #pragma unroll
             for (int nt = 0; nt < 4; nt++)
                 if (nt < NT) {
-                    frag_b(R + (k0 + t) * L.ldR + nt * 8 + g, L.ldR, bh, bl);
+                    frag_b(R + (k0 + 2 * t) * L.ldR + nt * 8 + g, L.ldR, bh, bl);
                     mma3(c[nt], ah, al, bh, bl);
                 }
         }
@@ -525,10 +550,10 @@ __global__ void __launch_bounds__(32 * kDftWarps) fno_synthesis_tc(const float2*
     extern __shared__ float sd[];
     const DftTc L = dft_tc_layout(n, m);
     float* U = sd;                         // [n][ldU]
-    float* W = U + n * L.ldU;              // [N2][ldW]
-    float* scr = W + L.N2 * L.ldW;
+    float* W = U + n * L.ldU;              // [K2][ldW]
+    float* scr = W + L.K2 * L.ldW;
     for (int e = threadIdx.x; e < n * L.R4; e += blockDim.x) U[(e / L.R4) * L.ldU + e % L.R4] = tS1[e];
-    for (int e = threadIdx.x; e < L.N2 * n; e += blockDim.x) W[(e / n) * L.ldW + e % n] = tS2[e];
+    for (int e = threadIdx.x; e < L.K2 * n; e += blockDim.x) W[(e / n) * L.ldW + e % n] = tS2[e];
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     const long long plane = (long long)blockIdx.x * kDftWarps + warp;
@@ -537,6 +562,8 @@ __global__ void __launch_bounds__(32 * kDftWarps) fno_synthesis_tc(const float2*
     float* Z = V + L.R4 * L.ldV;
     const int M = 2 * m * m, NT = L.N2 / 8;
     for (int e = lane; e < L.R4 * L.ldV; e += 32) V[e] = 0.0f;
+    for (int e = lane; e < n * (L.K2 - L.N2); e += 32)    // Z's padding columns
+        Z[(e / (L.K2 - L.N2)) * L.ldZ + L.N2 + e % (L.K2 - L.N2)] = 0.0f;
     __syncwarp();
     const float2* src = in + plane * M;
     for (int q = lane; q < M; q += 32) {
@@ -551,15 +578,15 @@ __global__ void __launch_bounds__(32 * kDftWarps) fno_synthesis_tc(const float2*
     }
     __syncwarp();
     uint32_t ah[4], al[4], bh[2], bl[2];
-    // Z = U V: M = n (x), K = R4 (k), N = N2 (c)
+    // Z = U V: M = n (x), K = R4 (k), N = N2 (c); columns N2..K2 of Z stay zero
     for (int mt = 0; mt < n / 16; mt++) {
         float c[4][4] = {};
-        for (int k0 = 0; k0 < L.R4; k0 += 8) {
-            frag_a(U + (mt * 16 + g) * L.ldU + k0 + t, L.ldU, ah, al);
+        for (int k0 = 0; k0 < L.R4; k0 += 16) {
+            frag_a(U + (mt * 16 + g) * L.ldU + k0 + 2 * t, L.ldU, ah, al);
 #pragma unroll
             for (int nt = 0; nt < 4; nt++)
                 if (nt < NT) {
-                    frag_b(V + (k0 + t) * L.ldV + nt * 8 + g, L.ldV, bh, bl);
+                    frag_b(V + (k0 + 2 * t) * L.ldV + nt * 8 + g, L.ldV, bh, bl);
                     mma3(c[nt], ah, al, bh, bl);
                 }
         }
@@ -568,16 +595,16 @@ __global__ void __launch_bounds__(32 * kDftWarps) fno_synthesis_tc(const float2*
             if (nt < NT) store_c(Z, L.ldZ, mt * 16, nt * 8, g, t, c[nt]);
     }
     __syncwarp();
-    // f = Z W: M = n (x), K = N2 (c), N = n (y), two column tiles at a time
+    // f = Z W: M = n (x), K = K2 (c), N = n (y), two column tiles at a time
     float* dst = out + plane * n * n;
     for (int mt = 0; mt < n / 16; mt++)
         for (int nt0 = 0; nt0 < n / 8; nt0 += 2) {
             float c[2][4] = {};
-            for (int k0 = 0; k0 < L.N2; k0 += 8) {
-                frag_a(Z + (mt * 16 + g) * L.ldZ + k0 + t, L.ldZ, ah, al);
+            for (int k0 = 0; k0 < L.K2; k0 += 16) {
+                frag_a(Z + (mt * 16 + g) * L.ldZ + k0 + 2 * t, L.ldZ, ah, al);
 #pragma unroll
                 for (int j = 0; j < 2; j++) {
-                    frag_b(W + (k0 + t) * L.ldW + (nt0 + j) * 8 + g, L.ldW, bh, bl);
+                    frag_b(W + (k0 + 2 * t) * L.ldW + (nt0 + j) * 8 + g, L.ldW, bh, bl);
                     mma3(c[j], ah, al, bh, bl);
                 }
             }
@@ -1032,7 +1059,7 @@ void pointwise(sp_fno* f, PW a) {
     const size_t smem = sizeof(float) * (a.cin * a.cout + a.cout);
     const int nb = (int)((n + tb - 1) / tb);
     if (a.cout % 16 == 0 && a.cout <= 64 && a.cin <= 64 && a.P % 32 == 0) {
-        const size_t tsm = sizeof(float) * (a.cout * (((a.cin + 7) & ~7) + 4) + a.cout);
+        const size_t tsm = sizeof(uint32_t) * (a.cout * (((a.cin + 15) & ~15) / 2 + 4) + a.cout);
         switch (a.cout / 16) {
             case 1: fno_pointwise_tc<1><<<nb, tb, tsm, f->st>>>(a); break;
             case 2: fno_pointwise_tc<2><<<nb, tb, tsm, f->st>>>(a); break;
@@ -1272,7 +1299,7 @@ int sp_fno_create(const sp_fno_shape* shape, sp_fno** out) {
         f->tA1 = dalloc<float>(f, (long long)s.n * DL.N2, ok);
         f->tA2 = dalloc<float>(f, (long long)DL.R4 * s.n, ok);
         f->tS1 = dalloc<float>(f, (long long)s.n * DL.R4, ok);
-        f->tS2 = dalloc<float>(f, (long long)DL.N2 * s.n, ok);
+        f->tS2 = dalloc<float>(f, (long long)DL.K2 * s.n, ok);
     }
     f->s_one = dalloc<float>(f, s.modes, ok);
     f->s_inv = dalloc<float>(f, s.modes, ok);
@@ -1339,14 +1366,14 @@ int sp_fno_create(const sp_fno_shape* shape, sp_fno** out) {
     e = cudaMemcpy(f->tw, tw.data(), sizeof(float2) * s.n, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && dft_tc) {
         // the DFT matrices of the tensor-core kernels, from double precision
-        const int n = s.n, m = s.modes, N2 = DL.N2, R4 = DL.R4;
+        const int n = s.n, m = s.modes, N2 = DL.N2, K2 = DL.K2, R4 = DL.R4;
         auto cs = [n](long long k, bool sine) {
             const double th = 6.283185307179586477 * (double)(((k % n) + n) % n) / (double)n;
             return (float)(sine ? std::sin(th) : std::cos(th));
         };
         auto kx_of = [n, m](int kxi) { return kxi < m ? kxi : n - 2 * m + kxi; };
         std::vector<float> a1((size_t)n * N2, 0.0f), a2((size_t)R4 * n, 0.0f);
-        std::vector<float> s1((size_t)n * R4), s2((size_t)N2 * n);
+        std::vector<float> s1((size_t)n * R4), s2((size_t)K2 * n, 0.0f);
         for (int y = 0; y < n; y++)
             for (int c = 0; c < 2 * m; c++)
                 a1[(size_t)y * N2 + c] = c < m ? cs((long long)c * y, false)
