@@ -285,7 +285,9 @@ def run_sdpd(args):
     cpu = None
     if not args.skip_cpu and _reference_engine():
         # the reference engine's flow, one independent replica per host core
-        # (one flow does not gain from its threads: SURVEY F5), steps [2, 4)
+        # (the engine's threaded flow serialises its neighbour searches on one
+        # mutex and races on the densities, so one thread per flow is both
+        # faster and deterministic), steps [2, 4)
         import oracle
         cores = os.cpu_count() or 1
         scb = S.config_dam_break(num_steps=2 + REF_FLOW_STEPS)
