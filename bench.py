@@ -522,10 +522,10 @@ def run_fno(args):
                 "roofline": {"bound": "tensor", "achieved": tflops, "peak": peak,
                              "unit": "TFLOP/s", "frac": tflops / peak, "traffic": None,
                              "peak_source": peak_src,
-                             "note": "algorithmic flops; the channel mixes and DFTs run as "
-                                     "mma.sync bf16, the weight gradients as mma.sync TF32, "
-                                     "with split operands (2-3 products per multiply), the "
-                                     "per-mode mixes on CUDA cores; small contractions at ~8 "
+                             "note": "algorithmic flops; the channel mixes, DFTs and "
+                                     "per-mode mixes run as mma.sync bf16, the pointwise "
+                                     "weight gradients as mma.sync TF32, with split operands "
+                                     "(2-3 products per multiply); small contractions at ~8 "
                                      "flop/byte are latency bound"}}
     except Exception as ex:         # a secondary line never takes the headline down
         return {"metric": "surrogate training samples/s", "error": repr(ex)}

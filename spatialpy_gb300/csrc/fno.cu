@@ -8,11 +8,11 @@
 // Work per sample is small and the contractions are width-32 channel mixes
 // (2 x 32 x 32 flops per voxel and layer against 256 bytes of field traffic,
 // 8 flop/byte), so the kernels are bound by memory and launch latency.  The
-// channel mixes and the truncated DFTs run on the tensor cores as mma.sync
-// bf16, the channel mixes' weight gradients as mma.sync TF32, with fp32
-// operands split into a high part and the rounding of the remainder so that
-// the sums keep fp32-level accuracy; the per-mode complex mixing is fp32
-// CUDA-core code.  A training step (about 70 launches) is captured once per
+// channel mixes, the truncated DFTs and the per-mode complex mixes run on
+// the tensor cores as mma.sync bf16, the channel mixes' weight gradients as
+// mma.sync TF32, with fp32 operands split into a high part and the rounding
+// of the remainder so that the sums keep fp32-level accuracy; shapes outside
+// the tiles keep the fp32 CUDA-core kernels.  A training step (about 70 launches) is captured once per
 // batch size as a CUDA graph and replayed.
 //
 // Kernels:
@@ -27,8 +27,10 @@
 //   fno_synthesis    its adjoint / the truncated inverse real DFT (and
 //                    fno_synthesis_tc)
 //   fno_mix          per-mode complex channel mixing (forward, and the
-//                    conjugate transpose for the backward pass)
+//                    conjugate transpose for the backward pass);
+//                    fno_mix_tc on the tensor cores for width 16, 32, 64
 //   fno_mix_wgrad    per-mode weight gradient, a reduction over the batch
+//                    (fno_mix_wgrad_tc for width 16, 32)
 //   fno_wgrad_*      pointwise weight gradients: per-tile partial products
 //                    on the tensor cores, then an ordered reduction
 //                    (deterministic)
@@ -663,6 +665,161 @@ __global__ void fno_mix(const float2* X, const uint16_t* w, float2* Y, int B, in
     }
 }
 
+// The per-mode mix on the tensor cores (C = 16, 32 or 64): with the
+// inputs of 64 samples as real rows [Re X | Im X] (K = 2C) and the complex
+// (in, out) matrix Wc in real form B = [[Re, Im], [-Im, Re]] (2C x 2C, bf16
+// exact), [Re Y | Im Y] = X B.  One CTA per mode, warp w takes samples
+// 16w .. 16w + 15 and all 2C output columns; mma.sync m16n8k16 bf16 with
+// the inputs split into two bf16 parts.  B is kept transposed as bf16 pairs
+// along K, so a B fragment is two 32-bit loads.
+template <int C>
+__global__ void __launch_bounds__(128) fno_mix_tc(const float2* X, const uint16_t* w, float2* Y,
+                                                  int B, int M, int conj_t) {
+    constexpr int K2 = 2 * C, NT = K2 / 8;
+    constexpr int LDB = C + 4;             // pairs per row of Bt: B-fragment loads hit 32 banks
+    constexpr int LDX = K2 + 8;            // floats per row of Xs: A-fragment float2 loads too
+    extern __shared__ uint32_t smx[];
+    uint32_t* Bt = smx;                                      // [K2 (n)][LDB] pairs along k
+    float* Xs = reinterpret_cast<float*>(smx + K2 * LDB);    // [64][LDX]
+    const int q = blockIdx.x;
+    const uint16_t* wq = w + (long long)q * C * C * 2;
+    for (int e = threadIdx.x; e < K2 * C; e += blockDim.x) {
+        const int n = e / C, kp = e % C;
+        uint32_t pr = 0;
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int k = 2 * kp + h, i = k % C, o = n % C;
+            // Wc[i][o] = W[i][o], or conj(W[o][i]) for the conjugate transpose
+            const int src = conj_t ? o * C + i : i * C + o;
+            const float re = bfv(wq[2 * src]);
+            const float im = conj_t ? -bfv(wq[2 * src + 1]) : bfv(wq[2 * src + 1]);
+            const float v = k < C ? (n < C ? re : im) : (n < C ? -im : re);
+            pr |= (uint32_t)to_bf16(v) << (16 * h);
+        }
+        Bt[n * LDB + kp] = pr;
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    for (int b0 = 0; b0 < B; b0 += 64) {
+        const int nb = min(64, B - b0);
+        __syncthreads();
+        for (int e = threadIdx.x; e < 64 * C; e += blockDim.x) {
+            const int bb = e / C, c = e % C;
+            float2 v = make_float2(0.0f, 0.0f);
+            if (bb < nb) v = X[((long long)(b0 + bb) * C + c) * M + q];
+            Xs[bb * LDX + c] = v.x;
+            Xs[bb * LDX + C + c] = v.y;
+        }
+        __syncthreads();
+        float acc[NT][4];
+#pragma unroll
+        for (int nt = 0; nt < NT; nt++)
+#pragma unroll
+            for (int r = 0; r < 4; r++) acc[nt][r] = 0.0f;
+#pragma unroll
+        for (int k0 = 0; k0 < K2; k0 += 16) {
+            uint32_t ah[4], al[4];
+            frag_a(Xs + (warp * 16 + g) * LDX + k0 + 2 * t, LDX, ah, al);
+#pragma unroll
+            for (int nt = 0; nt < NT; nt++) {
+                const uint32_t* bp = Bt + (nt * 8 + g) * LDB + k0 / 2 + t;
+                const uint32_t b0r = bp[0], b1r = bp[4];
+                mma_bf16(acc[nt], al[0], al[1], al[2], al[3], b0r, b1r);
+                mma_bf16(acc[nt], ah[0], ah[1], ah[2], ah[3], b0r, b1r);
+            }
+        }
+        // column o (< C) of tile nt holds Re Y, the same column of tile nt + NT/2 Im Y
+#pragma unroll
+        for (int nt = 0; nt < NT / 2; nt++)
+#pragma unroll
+            for (int r = 0; r < 2; r++) {
+                const int bb = warp * 16 + g + 8 * r;
+                if (bb >= nb) continue;
+#pragma unroll
+                for (int j = 0; j < 2; j++) {
+                    const int o = nt * 8 + 2 * t + j;
+                    Y[((long long)(b0 + bb) * C + o) * M + q] =
+                        make_float2(acc[nt][2 * r + j], acc[nt + NT / 2][2 * r + j]);
+                }
+            }
+    }
+}
+
+// Its weight gradient on the tensor cores (C = 16 or 32): P = A D with
+// A[i'][b] = [Re X; Im X] (2C x samples) and D[b][n'] = [Re dY | Im dY],
+// then dW re = P[i][o] + P[C+i][C+o], im = P[i][C+o] - P[C+i][o].  Each work
+// unit is the four 16 x 8 tiles (mt, nt), (mt, nt + C/8), (mt + C/16, nt),
+// (mt + C/16, nt + C/8) that one output block needs; samples in chunks of
+// 64, both operands split into two bf16 parts (3 products).
+template <int C>
+__global__ void __launch_bounds__(128) fno_mix_wgrad_tc(const float2* X, const float2* dY,
+                                                        float* gw, int B, int M) {
+    constexpr int K2 = 2 * C, MP = C / 16, NP = C / 8, UNITS = MP * NP, UPW = (UNITS + 3) / 4;
+    constexpr int LDA = 64 + 8, LDY = K2 + 4;
+    extern __shared__ float smw[];
+    float* Xt = smw;                 // [K2][LDA]
+    float* Ys = smw + K2 * LDA;      // [64][LDY]
+    const int q = blockIdx.x;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    float acc[UPW][4][4];
+#pragma unroll
+    for (int u = 0; u < UPW; u++)
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int r = 0; r < 4; r++) acc[u][a][r] = 0.0f;
+    for (int b0 = 0; b0 < B; b0 += 64) {
+        const int nb = min(64, B - b0);
+        __syncthreads();
+        for (int e = threadIdx.x; e < 64 * C; e += blockDim.x) {
+            const int bb = e / C, c = e % C;
+            float2 x = make_float2(0.0f, 0.0f), y = make_float2(0.0f, 0.0f);
+            if (bb < nb) {
+                const long long k = ((long long)(b0 + bb) * C + c) * M + q;
+                x = X[k];
+                y = dY[k];
+            }
+            Xt[c * LDA + bb] = x.x;
+            Xt[(C + c) * LDA + bb] = x.y;
+            Ys[bb * LDY + c] = y.x;
+            Ys[bb * LDY + C + c] = y.y;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < UPW; u++) {
+            const int unit = warp + 4 * u;
+            if (unit >= UNITS) break;
+            const int mt = unit / NP, nt = unit % NP;
+#pragma unroll
+            for (int k0 = 0; k0 < 64; k0 += 16) {
+                uint32_t ah0[4], al0[4], ah1[4], al1[4], bh0[2], bl0[2], bh1[2], bl1[2];
+                frag_a(Xt + (mt * 16 + g) * LDA + k0 + 2 * t, LDA, ah0, al0);
+                frag_a(Xt + ((mt + MP) * 16 + g) * LDA + k0 + 2 * t, LDA, ah1, al1);
+                frag_b(Ys + (k0 + 2 * t) * LDY + nt * 8 + g, LDY, bh0, bl0);
+                frag_b(Ys + (k0 + 2 * t) * LDY + (nt + NP) * 8 + g, LDY, bh1, bl1);
+                mma3(acc[u][0], ah0, al0, bh0, bl0);
+                mma3(acc[u][1], ah0, al0, bh1, bl1);
+                mma3(acc[u][2], ah1, al1, bh0, bl0);
+                mma3(acc[u][3], ah1, al1, bh1, bl1);
+            }
+        }
+    }
+    float* gq = gw + (long long)q * C * C * 2;
+#pragma unroll
+    for (int u = 0; u < UPW; u++) {
+        const int unit = warp + 4 * u;
+        if (unit >= UNITS) break;
+        const int mt = unit / NP, nt = unit % NP;
+#pragma unroll
+        for (int r = 0; r < 2; r++)
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+                const int i = mt * 16 + g + 8 * r, o = nt * 8 + 2 * t + j, a = 2 * r + j;
+                gq[2 * (i * C + o)] = acc[u][0][a] + acc[u][3][a];
+                gq[2 * (i * C + o) + 1] = acc[u][1][a] - acc[u][2][a];
+            }
+    }
+}
+
 // dW[q][i][o] = sum_b conj(X[b][i][q]) dY[b][o][q], written as fp32 pairs
 __global__ void fno_mix_wgrad(const float2* X, const float2* dY, float* gw, int B, int C, int M) {
     extern __shared__ float2 sm2[];
@@ -1115,6 +1272,35 @@ void wgrad(sp_fno* f, const float* dy, const float* x, long long x_bs, int O, in
     fno_wgrad_reduce<<<(E + 31) / 32, 256, 0, f->st>>>(f->part, nblk, O, I, gw, gb);
 }
 
+inline size_t mix_tc_smem(int C) {
+    return sizeof(uint32_t) * (2 * C * (C + 4) + 64 * (2 * C + 8));
+}
+inline size_t mix_wgrad_tc_smem(int C) {
+    return sizeof(float) * (2 * C * (64 + 8) + 64 * (2 * C + 4));
+}
+
+void mix(sp_fno* f, const float2* X, const uint16_t* w, float2* Y, int B, int conj_t) {
+    const int C = f->s.width, M = f->M;
+    switch (C) {
+        case 16: fno_mix_tc<16><<<M, 128, mix_tc_smem(16), f->st>>>(X, w, Y, B, M, conj_t); return;
+        case 32: fno_mix_tc<32><<<M, 128, mix_tc_smem(32), f->st>>>(X, w, Y, B, M, conj_t); return;
+        case 64: fno_mix_tc<64><<<M, 128, mix_tc_smem(64), f->st>>>(X, w, Y, B, M, conj_t); return;
+        default: break;
+    }
+    const size_t msm = sizeof(float2) * (C * C + 16 * C);
+    fno_mix<<<M, 256, msm, f->st>>>(X, w, Y, B, C, M, conj_t);
+}
+
+void mix_wgrad(sp_fno* f, const float2* X, const float2* dY, float* gw, int B) {
+    const int C = f->s.width, M = f->M;
+    switch (C) {
+        case 16: fno_mix_wgrad_tc<16><<<M, 128, mix_wgrad_tc_smem(16), f->st>>>(X, dY, gw, B, M); return;
+        case 32: fno_mix_wgrad_tc<32><<<M, 128, mix_wgrad_tc_smem(32), f->st>>>(X, dY, gw, B, M); return;
+        default: break;
+    }
+    fno_mix_wgrad<<<M, 256, sizeof(float2) * 2 * 16 * C, f->st>>>(X, dY, gw, B, C, M);
+}
+
 // ---- forward / backward enqueue ------------------------------------------
 void enqueue_forward(sp_fno* f, const float* x, long long x_bs, const float* cond, int B,
                      float* out) {
@@ -1137,8 +1323,7 @@ void enqueue_forward(sp_fno* f, const float* x, long long x_bs, const float* con
         float* hk = f->h + k * stride_h;
         float2* Xk = f->X + k * stride_X;
         analysis(f, hk, Xk, B * C, f->s_one);
-        const size_t msm = sizeof(float2) * (C * C + 16 * C);
-        fno_mix<<<f->M, 256, msm, f->st>>>(Xk, f->pb + o.spec[k], f->Y, B, C, f->M, 0);
+        mix(f, Xk, f->pb + o.spec[k], f->Y, B, 0);
         synthesis(f, f->Y, f->sbuf, B * C, f->s_inv, 0);
         PW l = pw_base(f, B);
         l.in = hk; l.in_bs = (long long)C * f->P; l.cin = C; l.cout = C;
@@ -1188,7 +1373,6 @@ void enqueue_backward(sp_fno* f, const float* target, int B) {
     // layers, last to first
     float* dh = f->dhA;
     float* dh_next = f->dhB;
-    const size_t msm = sizeof(float2) * (C * C + 16 * C);
     for (int k = L - 1; k >= 0; k--) {
         const float* hk = f->h + k * stride_h;
         const float2* Xk = f->X + k * stride_X;
@@ -1200,9 +1384,8 @@ void enqueue_backward(sp_fno* f, const float* target, int B) {
         tl.w = f->pb + o.lin_w[k]; tl.trans = 1; tl.out = dh_next;
         pointwise(f, tl);
         analysis(f, f->du, f->dY, B * C, f->s_inv);
-        fno_mix_wgrad<<<f->M, 256, sizeof(float2) * 2 * 16 * C, f->st>>>(Xk, f->dY,
-                                                                        f->grad + o.spec[k], B, C, f->M);
-        fno_mix<<<f->M, 256, msm, f->st>>>(f->dY, f->pb + o.spec[k], f->dX, B, C, f->M, 1);
+        mix_wgrad(f, Xk, f->dY, f->grad + o.spec[k], B);
+        mix(f, f->dY, f->pb + o.spec[k], f->dX, B, 1);
         synthesis(f, f->dX, dh_next, B * C, f->s_one, 1);
         float* t = dh;
         dh = dh_next;
@@ -1347,9 +1530,13 @@ int sp_fno_create(const sp_fno_shape* shape, sp_fno** out) {
         sp_fno_destroy(f);
         return SP_E_CUDA;
     }
-    // the weight-gradient tiles of 64 x 64 channel pairs take 66 KB
+    // the weight-gradient tiles of 64 x 64 channel pairs take 66 KB, the
+    // tensor-core mode mix of width 64 70 KB
     e = cudaFuncSetAttribute(fno_wgrad_partial_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)(sizeof(float) * 128 * kLdTc));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(fno_mix_tc<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)mix_tc_smem(64));
     if (e != cudaSuccess) {
         sp_fno_destroy(f);
         return SP_E_CUDA;
