@@ -24,7 +24,8 @@ void launch_nsm_init(NsmTraj* trajs, const NsmInstance* insts, int ntraj, int ma
                      int max_levels, const uint32_t* const* u0, bool build_queue,
                      cudaStream_t st);
 void launch_nsm_rebuild(NsmTraj* trajs, const NsmInstance* insts, int ntraj, int max_leaf,
-                        int max_levels, double t0, uint32_t build_index, cudaStream_t st);
+                        int max_levels, double t0, uint32_t build_index, int variant,
+                        cudaStream_t st);
 int nsm_warp_smem(const NsmInstance& d, bool with_state);
 void launch_nsm_advance(bool ref, bool smem_state, int variant, int warp_smem, int wpb,
                         NsmTraj* trajs, const NsmInstance* insts, int ntraj, int step_end,
@@ -131,6 +132,7 @@ struct RunState {
     long long chem_tot = 0;
     std::vector<long long> chem_off;        // per instance, in doubles
     int cinst = -1, step = 0, max_leaf = 0, max_levels = 0;
+    int rebuild_variant = 0;   // register-resident network of the per-step queue rebuild
     long long poff = 0, ptot = 0;   // offset of cinst / total, in particles x outputs
     double *d_px = nullptr, *d_pv = nullptr, *d_prho = nullptr;
 };
@@ -909,6 +911,7 @@ int sp_run_start(sp_handle* h, const sp_run_args* a, sp_outputs* out) {
     h->last_kernel = kernel_kind(R);
     R.max_leaf = max_leaf;
     R.max_levels = max_levels;
+    R.rebuild_variant = R.coupled ? net_variant(h, all, R.inst) : 0;
     launch_nsm_init(h->d_trajs, h->d_insts, ntraj, max_leaf, max_levels, d_u0, !R.coupled, st);
     h->launches += R.coupled ? 1 : 3;
     if (R.ngroups == 2) {
@@ -1118,7 +1121,7 @@ static int coupled_steps(sp_handle* h, int target, bool ref, long long budget, l
                                         st);
         sdpd_launch_volumes(I.sdpd, I.mass, I.vol, I.ivol);
         launch_nsm_rebuild(h->d_trajs, h->d_insts, ntraj, R.max_leaf, R.max_levels,
-                           h->dt * (double)R.step, (uint32_t)R.step, st);
+                           h->dt * (double)R.step, (uint32_t)R.step, R.rebuild_variant, st);
         launch_groups(h, ref, R.step + 1, budget, max_ns);
         h->launches += kSdpdLaunchesPerStep + 1 + 1 + 3 + 1;
         R.step++;

@@ -164,6 +164,95 @@ __global__ void nsm_init_leaves(NsmTraj* trajs, const NsmInstance* insts, int nt
     }
 }
 
+// The same rebuild with the network unpacked once per block into shared
+// memory (SmallNet<MS, MR>, the event kernels' variants; a block serves one
+// trajectory): the rates come from rates_small, which sums the same terms
+// in the same order as prop() above, so the leaves are the same bits.  Used
+// for the per-step rebuild of a moving domain.
+template <int MS, int MR, bool EX>
+__global__ void __launch_bounds__(256) nsm_init_leaves_net(NsmTraj* trajs, const NsmInstance* insts,
+                                                           int ntraj, double t0,
+                                                           uint32_t build_index) {
+    const int j = blockIdx.y;
+    if (j >= ntraj) return;
+    NsmTraj& T = trajs[j];
+    const NsmInstance& I = insts[T.inst];
+    __shared__ SmallNet<MS, MR> Q;
+    if (threadIdx.x == 0) {
+        Q.S = I.S;
+        Q.R = I.R;
+    }
+    if (threadIdx.x < MR) {
+        const int r = threadIdx.x;
+        const bool on = EX || r < I.R;
+        Q.kind[r] = on ? I.kind[r] : 0;
+        Q.ra[r] = on ? I.reac[2 * r] : 0;
+        Q.rb[r] = on ? I.reac[2 * r + 1] : 0;
+        Q.rate[r] = on ? I.rate[r] : 0.0f;
+        unsigned long long m = 0;
+        if (on)
+            for (int t = 0; t <= I.T && t < 64; t++)
+                if (!I.allowed || I.allowed[r * (I.T + 1) + t]) m |= 1ull << t;
+        Q.allowed[r] = m;
+    }
+    __syncthreads();
+    const int N = I.N, S = I.S, NT1 = I.level_off[1], stride = I.leaf_stride;
+    const bool tree1 = I.levels >= 1, source = I.has_source != 0;
+    const int* __restrict__ X = T.x;
+    long long* __restrict__ leaf = T.leaf;
+    long long* __restrict__ nt = T.node_t;
+    int* __restrict__ ni = T.node_i;
+    long long* __restrict__ n2 = T.node_t2;
+    const uint32_t k0 = T.key0, k1 = T.key1;
+    const float* __restrict__ ddiag = I.ddiag;
+    const int* __restrict__ vtype = I.type;
+    const float* __restrict__ vvol = I.vol;
+    const float* __restrict__ vivol = I.ivol;
+    const int lane = threadIdx.x & 31;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < stride; v += gridDim.x * blockDim.x) {
+        float a = 0.0f;
+        long long tv = SP_INF_BITS;
+        if (v < N) {
+            int x[MS];
+            float dd[MS];
+            int any = 0;
+#pragma unroll
+            for (int s = 0; s < MS; s++) {
+                const bool on = EX || s < S;
+                x[s] = on ? X[(size_t)v * S + s] : 0;
+                dd[s] = on ? ddiag[(size_t)v * S + s] : 0.0f;
+                any |= x[s];
+            }
+            if (source || any != 0) {
+                float srr, sdr;
+                rates_small<MS, MR, EX>(Q, x, dd, vvol[v], vivol[v], vtype[v], srr, sdr);
+                a = srr + sdr;
+                if (a > 0.0f) {
+                    const u32x4 rr = philox4x32_10((uint32_t)v, build_index, 1u, 0u, k0, k1);
+                    tv = draw_time(t0, neglog_f(u32f(rr.x)), a);
+                }
+            }
+        }
+        leaf[v] = tv;
+        if (tree1) {
+            long long t = tv;
+            int i = v;
+            warp_argmin(t, i);
+            long long t2 = i == v ? SP_INF_BITS : tv;
+            int i2 = i == v ? INT_MAX : v;
+            warp_argmin(t2, i2);
+            if (lane == 0) {
+                nt[NT1 + (v >> 5)] = t;
+                ni[NT1 + (v >> 5)] = i;
+                n2[v >> 5] = t2;
+            }
+        }
+        double ad = a > 0.0f ? (double)a : 0.0;
+        for (int o = 16; o > 0; o >>= 1) ad += __shfl_xor_sync(SP_FULL, ad, o);
+        if (lane == 0 && ad > 0.0) atomicAdd(&T.a_tot, ad);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // event loop
 // ---------------------------------------------------------------------------
@@ -828,12 +917,22 @@ __global__ void nsm_build_upper(NsmTraj* trajs, const NsmInstance* insts, int nt
     }
 }
 
+// variant: the register-resident network of every trajectory (the event
+// kernels' numbering: 1 <4, 8>, 2 <8, 16>, 3 exactly <1, 2>, 4 exactly <3, 4>),
+// 0 for the generic rebuild
 void launch_nsm_rebuild(NsmTraj* trajs, const NsmInstance* insts, int ntraj, int max_leaf,
-                        int max_levels, double t0, uint32_t build_index, cudaStream_t st) {
+                        int max_levels, double t0, uint32_t build_index, int variant,
+                        cudaStream_t st) {
     const int gx = (max_leaf + 255) / 256 < 64 ? (max_leaf + 255) / 256 : 64;
     dim3 g(gx, ntraj);
     nsm_reset_totals<<<(ntraj + 127) / 128, 128, 0, st>>>(trajs, ntraj);
-    nsm_init_leaves<<<g, 256, 0, st>>>(trajs, insts, ntraj, t0, build_index);   // + level 1
+    switch (variant) {   // + level 1
+        case 1: nsm_init_leaves_net<4, 8, false><<<g, 256, 0, st>>>(trajs, insts, ntraj, t0, build_index); break;
+        case 2: nsm_init_leaves_net<8, 16, false><<<g, 256, 0, st>>>(trajs, insts, ntraj, t0, build_index); break;
+        case 3: nsm_init_leaves_net<1, 2, true><<<g, 256, 0, st>>>(trajs, insts, ntraj, t0, build_index); break;
+        case 4: nsm_init_leaves_net<3, 4, true><<<g, 256, 0, st>>>(trajs, insts, ntraj, t0, build_index); break;
+        default: nsm_init_leaves<<<g, 256, 0, st>>>(trajs, insts, ntraj, t0, build_index); break;
+    }
     if (max_levels > 1) nsm_build_upper<<<ntraj, 256, 0, st>>>(trajs, insts, ntraj);
 }
 
