@@ -157,10 +157,12 @@ __global__ void nsm_init_leaves(NsmTraj* trajs, const NsmInstance* insts, int nt
                 n2[v >> 5] = t2;
             }
         }
-        // running total (steers speculation only): one atomic per warp
-        double ad = a > 0.0f ? (double)a : 0.0;
-        for (int o = 16; o > 0; o >>= 1) ad += __shfl_xor_sync(SP_FULL, ad, o);
-        if (lane == 0 && ad > 0.0) atomicAdd(&T.a_tot, ad);
+        // running total (steers speculation only): the warp's 32 rates summed
+        // in fp32, then one fp64 atomic per warp (the fp64 pipe is the
+        // scarce one on this part)
+        float af = a > 0.0f ? a : 0.0f;
+        for (int o = 16; o > 0; o >>= 1) af += __shfl_xor_sync(SP_FULL, af, o);
+        if (lane == 0 && af > 0.0f) atomicAdd(&T.a_tot, (double)af);
     }
 }
 
@@ -247,9 +249,9 @@ __global__ void __launch_bounds__(256) nsm_init_leaves_net(NsmTraj* trajs, const
                 n2[v >> 5] = t2;
             }
         }
-        double ad = a > 0.0f ? (double)a : 0.0;
-        for (int o = 16; o > 0; o >>= 1) ad += __shfl_xor_sync(SP_FULL, ad, o);
-        if (lane == 0 && ad > 0.0) atomicAdd(&T.a_tot, ad);
+        float af = a > 0.0f ? a : 0.0f;
+        for (int o = 16; o > 0; o >>= 1) af += __shfl_xor_sync(SP_FULL, af, o);
+        if (lane == 0 && af > 0.0f) atomicAdd(&T.a_tot, (double)af);
     }
 }
 
